@@ -1,0 +1,343 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 shallow-water hot path (one JSON line).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one time step (all RK stages) of the workload; the default
+workload is the 512x512-cell, 64-level, 8-tracer, 5-stage LSRK case with all
+four dissipation terms on.  ``value`` is cell-level-stage updates per second
+with the state resident in HBM (its 1.6 GB state is larger than L2, so no
+flush is needed between steps); ``e2e`` is the same metric through the
+public API with the state copied host->device and device->host every step
+from pinned memory.  Under torchrun each rank advances its own replica
+(weak scaling; the path needs no communication).
+
+``--impl reference`` times the CPU restatement of the reference (oracle/,
+OpenMP on all host cores) on the same workload; each of its steps is one
+LSRK5 step of a level-subsampled copy of the workload (stated in
+``cpu_baseline.sample``), so the run stays within minutes.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("cell·level·stage updates/s FP64 (% HBM roofline); "
+          "adjoint/forward time ratio")
+UNIT = "cell·level·stage updates/s"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="lsrk5_512x512")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--nx", type=int, default=0,
+                    help="override nx = ny (small profiling cases)")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+# ----------------------------------------------------------- clocks -------
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str):
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", gpu_id, f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap")
+        for line in out.strip().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                smax.append(float(p[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------- CPU baseline -----
+
+def oracle_sample(wl, nlayers_sample, steps, warmup):
+    """Time the oracle (C restatement of the reference, OpenMP) on the
+    workload's mesh and tracers with `nlayers_sample` levels."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import pyoracle
+    from omega_playground_gb300.workloads import initial_state
+    w = wl.scaled(nlayers=nlayers_sample)
+    om = pyoracle.OracleMesh(w.nx, w.ny, w.dc, w.nlayers)
+
+    class _M:  # the tables initial_state reads
+        pass
+    m = _M()
+    for k, v in om.tables.items():
+        setattr(m, "m_" + k, v)
+    m.m_period_x, m.m_period_y = om.period_x, om.period_y
+    h, vn, tr = (np.ascontiguousarray(a) for a in initial_state(m, w))
+    md = pyoracle.OracleModel(om, **w.param_kwargs())
+    for s in range(warmup):
+        md.step(h, vn, tr, s * w.dt, w.dt, 1, w.stepper, w.nstages)
+    times = []
+    for s in range(steps):
+        t0 = time.perf_counter()
+        md.step(h, vn, tr, (warmup + s) * w.dt, w.dt, 1, w.stepper, w.nstages)
+        times.append(time.perf_counter() - t0)
+    units = w.ncells * w.nlayers * w.nstages
+    return units, times, pyoracle.lib().or_num_threads(), w
+
+
+def cpu_baseline(wl, target_s=15.0):
+    """Bounded sample of ~target_s seconds: pick the level count from a
+    probe step, then time whole LSRK/RK4 steps."""
+    units, t, cores, _ = oracle_sample(wl, 1, 1, 0)
+    per_level = t[0]
+    nl = max(1, min(wl.nlayers, int(3.0 / max(per_level, 1e-6))))
+    units, times, cores, w = oracle_sample(wl, nl, 1, 0)
+    nsteps = max(1, min(20, int(target_s / max(times[0], 1e-6))))
+    units, times, cores, w = oracle_sample(wl, nl, nsteps, 0)
+    return {"value": units * len(times) / sum(times), "unit": UNIT,
+            "cores": cores, "kind": "port",
+            "sample": (f"{len(times)} {w.stepper}{w.nstages} step(s) of the "
+                       f"{w.nx}x{w.ny} mesh, {w.ntracers} tracers, "
+                       f"{w.nlayers} of {wl.nlayers} levels; oracle C "
+                       f"restatement, OpenMP {cores} threads")}
+
+
+def run_reference(args, wl):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    # size the sample so (warmup + steps) steps take about two minutes
+    _, t, cores, _ = oracle_sample(wl, 1, 1, 0)
+    budget = 120.0 / max(1, args.steps + args.warmup)
+    nl = max(1, min(wl.nlayers, int(budget / max(t[0], 1e-6))))
+    units, times, cores, w = oracle_sample(wl, nl, args.steps, args.warmup)
+    total = sum(times)
+    value = units * len(times) / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / len(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": wl.name, "nx": wl.nx, "ny": wl.ny,
+                   "nlayers": wl.nlayers, "ntracers": wl.ntracers,
+                   "stepper": f"{wl.stepper}{wl.nstages}",
+                   "sample_nlayers": w.nlayers},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores,
+                         "kind": "port",
+                         "sample": (f"each step: one {w.stepper}{w.nstages} "
+                                    f"step of the {w.nx}x{w.ny} mesh, "
+                                    f"{w.ntracers} tracers, {w.nlayers} of "
+                                    f"{wl.nlayers} levels (oracle C "
+                                    "restatement of the reference, OpenMP)")},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------- GPU arm -------
+
+def run_ours(args, wl):
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import omega_playground_gb300 as og
+
+    mesh = og.PlanarHexagonalMesh(wl.nx, wl.ny, wl.dc, wl.nlayers)
+    params = wl.params()
+    model = og.ShallowWaterModel(mesh, params)
+    state = og.ShallowWaterState(mesh, params)
+    h0, vn0, tr0 = og.workloads.initial_state(mesh, wl)
+    state.upload(h0, vn0, tr0)
+    stepper = (og.RK4Stepper(model) if wl.stepper == "rk4"
+               else og.LSRKStepper(model, wl.nstages))
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    # warm-up (captures the step graph)
+    stepper.step(state, 0.0, wl.dt, args.warmup, use_graph=True, stream=sh)
+    barrier()
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
+    except Exception:
+        uuid = str(local)
+    clocks = ClockSampler(uuid)
+    time.sleep(0.3)
+    barrier()
+    launches0 = og.kernel_launches()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    stepper.step(state, args.warmup * wl.dt, wl.dt, args.steps,
+                 use_graph=True, stream=sh)
+    e1.record(stream)
+    barrier()
+    ms = e0.elapsed_time(e1)
+    launches = og.kernel_launches() - launches0
+    clk = clocks.stop()
+    ms_t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(ms_t.item())
+    units = wl.ncells * wl.nlayers * wl.nstages * args.steps
+    value = world * units / (ms_max / 1e3)
+
+    # per-kernel event timing of one step (direct launches)
+    og.profile_enable(True)
+    stepper.step(state, 0.0, wl.dt, 1, use_graph=False, stream=sh)
+    prof = og.profile_read()
+    og.profile_enable(False)
+    stage_ms = sum(v[0] for v in prof.values()) / wl.nstages
+    dom = max(prof, key=lambda k: prof[k][0])
+    dom_ms = prof[dom][0] / prof[dom][1]
+    CK = wl.ncells * wl.nlayers
+    alg_per_unit = {"k_cell_final": 32 * (1 + wl.ntracers),
+                    "k_edge_final": 32 * 3}
+    peak, peak_kind = hbm_peak()
+    dom_bytes = alg_per_unit.get(dom, 0) * CK
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    stage_bytes = wl.alg_bytes_per_stage()
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved,
+                "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": peak_kind, "traffic": None,
+                "alg_bytes_per_launch": dom_bytes,
+                "launch_ms": dom_ms,
+                "stage": {"achieved": stage_bytes / (stage_ms / 1e3) / 1e9,
+                          "alg_bytes": stage_bytes, "ms": stage_ms,
+                          "frac": stage_bytes / (stage_ms / 1e3) / 1e9 / peak}}
+    kernels = {k: {"ms_per_launch": v[0] / v[1], "launches_per_step": v[1],
+                   "share": v[0] / sum(x[0] for x in prof.values())}
+               for k, v in prof.items()}
+
+    # end to end through the public API, pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        sh_, sv_, st_ = state.shapes()
+
+        def pinned(shape):
+            n = int(np.prod(shape))
+            return torch.empty(max(n, 1), dtype=torch.float64,
+                               pin_memory=True).numpy()[:n].reshape(shape)
+        hh, vv, tt = pinned(sh_), pinned(sv_), pinned(st_)
+        hh[...], vv[...], tt[...] = h0, vn0, tr0
+        nbytes_in = hh.nbytes + vv.nbytes + tt.nbytes
+        barrier()
+        e0.record(stream)
+        for s in range(args.e2e_steps):
+            state.upload(hh, vv, tt, stream=sh)
+            stepper.step(state, s * wl.dt, wl.dt, 1, use_graph=True, stream=sh)
+            state.download(stream=sh, out=(hh, vv, tt))
+        e1.record(stream)
+        barrier()
+        e2e_ms = e0.elapsed_time(e1)
+        e2e = {"value": world * wl.ncells * wl.nlayers * wl.nstages *
+               args.e2e_steps / (e2e_ms / 1e3), "unit": UNIT,
+               "h2d_bytes_per_step": nbytes_in,
+               "d2h_bytes_per_step": nbytes_in, "steps": args.e2e_steps,
+               "ms_per_step": e2e_ms / args.e2e_steps}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(wl)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": wl.name, "nx": wl.nx, "ny": wl.ny,
+                       "nlayers": wl.nlayers, "ntracers": wl.ntracers,
+                       "stepper": f"{wl.stepper}{wl.nstages}", "dt": wl.dt,
+                       "parallelism": f"replicas x{world}",
+                       "l2": "state (%.2f GB) larger than L2; no flush"
+                             % (8 * (wl.ncells * wl.nlayers * (4 + wl.ntracers))
+                                / 1e9)},
+            "roofline": roofline, "kernels": kernels,
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    from omega_playground_gb300.workloads import WORKLOADS
+    wl = WORKLOADS[args.workload]
+    if args.nx:
+        wl = wl.scaled(nx=args.nx, ny=args.nx, name=f"{wl.name}@nx{args.nx}")
+    if args.impl == "reference":
+        run_reference(args, wl)
+    else:
+        run_ours(args, wl)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,206 @@
+/*
+ * swgpu.h - C ABI of the GB300 shallow-water solver (omega_playground_gb300).
+ *
+ * The solver replaces the Kokkos device path of mwarusz/omega_playground:
+ * its mesh tables, model state, tendency terms and time steppers.  The C++
+ * classes in omega_playground_gb300/cxx/omega_gpu.hpp keep the reference's
+ * class names and signatures and call these functions; other hosts (Python
+ * ctypes, Fortran, ...) can bind them directly.  All reference citations are
+ * paths inside the omega_playground checkout.
+ *
+ * Conventions
+ *  - Every function returns an int status (SWG_OK = 0); nothing throws or
+ *    aborts across the ABI.  swg_last_error() gives the calling thread's
+ *    message for the last failed call.
+ *  - Arrays are FP64 [entity][k] row-major with the level index k contiguous;
+ *    tracers are [l][cell][k]; connectivity is int32.  "host" pointers are
+ *    CPU memory, "device" pointers are CUDA global memory on the current
+ *    device.
+ *  - Handles are thread-confined.  Compute calls take a cudaStream_t (passed
+ *    as void*, NULL = legacy default stream) and are asynchronous on it;
+ *    only swg_state_download, swg_diag_* and swg_sync block the host.
+ *  - Connectivity is validated on the host at swg_mesh_create: every index
+ *    is checked against its table's range before any kernel can read it.
+ */
+#ifndef SWGPU_H
+#define SWGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SWG_OK 0
+#define SWG_ERR_ARG 1        /* bad argument or inconsistent sizes */
+#define SWG_ERR_OOM 2        /* device or host allocation failed */
+#define SWG_ERR_CUDA 3       /* a CUDA runtime call failed */
+#define SWG_ERR_TIMEOUT 4    /* a bounded device wait expired */
+#define SWG_ERR_BUDGET 5     /* checkpoint budget too small */
+#define SWG_ERR_STATE 6      /* handle used in the wrong state */
+
+#define SWG_ADD_REPLACE 0    /* AddMode::replace   (shallow_water_model.hpp:11) */
+#define SWG_ADD_INCREMENT 1  /* AddMode::increment (shallow_water_model.hpp:11) */
+
+#define SWG_STEPPER_RK4 0    /* RK4Stepper  (time_stepper.hpp:27-38) */
+#define SWG_STEPPER_LSRK 1   /* LSRKStepper (time_stepper.hpp:16-25) */
+
+typedef struct swg_mesh_s *swg_mesh;
+typedef struct swg_state_s *swg_state;
+typedef struct swg_model_s *swg_model;
+typedef struct swg_stepper_s *swg_stepper;
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char *swg_last_error(void);
+/* Library version string. */
+const char *swg_version(void);
+/* Number of kernels this library launched since load (all entry points). */
+long long swg_kernel_launches(void);
+
+/* ------------------------------------------------------------- mesh ------
+ * MPAS mesh tables, as in struct MPASMesh (src/mesh/mpas_mesh.hpp:7-71).
+ * Host pointers; only the fields the hot path reads are required.  maxedges
+ * is 6 (mpas_mesh.hpp:8); edges_on_edge / weights_on_edge rows have 12
+ * slots of which nedges_on_edge[e] are used.  edge_mask may be NULL (all
+ * ones, which is what MPASMesh::finalize_mesh sets, mpas_mesh.cpp:50);
+ * mesh_scaling_del2/4 may be NULL (all ones, mpas_mesh.cpp:48-49). */
+typedef struct swg_mesh_desc {
+  int ncells, nedges, nvertices, nlayers;
+  const int *nedges_on_cell;      /* [C]      */
+  const int *edges_on_cell;       /* [C][6]   */
+  const int *nedges_on_edge;      /* [E]      */
+  const int *edges_on_edge;       /* [E][12]  */
+  const int *cells_on_edge;       /* [E][2]   */
+  const int *vertices_on_edge;    /* [E][2]   */
+  const int *edges_on_vertex;     /* [V][3]   */
+  const int *cells_on_vertex;     /* [V][3]   */
+  const double *area_cell;        /* [C]      */
+  const double *edge_sign_on_cell;   /* [C][6] */
+  const double *dc_edge, *dv_edge;   /* [E]    */
+  const double *weights_on_edge;     /* [E][12] */
+  const double *area_triangle;       /* [V]    */
+  const double *kiteareas_on_vertex; /* [V][3] */
+  const double *edge_sign_on_vertex; /* [V][3] */
+  const double *mesh_scaling_del2;   /* [E] or NULL */
+  const double *mesh_scaling_del4;   /* [E] or NULL */
+  const double *edge_mask;           /* [E][K] or NULL */
+} swg_mesh_desc;
+
+/* Host tables of the doubly periodic planar hexagonal mesh, identical to
+ * PlanarHexagonalMesh(nx, ny, dc, nlayers) (planar_hexagonal_mesh.cpp:8-398,
+ * mpas_mesh.cpp:5-57).  Caller-allocated arrays, sizes C = nx*ny, E = 3C,
+ * V = 2C; any pointer may be NULL to skip that table. */
+typedef struct swg_hex_tables {
+  int *nedges_on_cell, *edges_on_cell, *cells_on_cell, *vertices_on_cell;
+  int *kite_index_on_cell;
+  int *nedges_on_edge, *edges_on_edge, *cells_on_edge, *vertices_on_edge;
+  int *edges_on_vertex, *cells_on_vertex;
+  double *area_cell, *x_cell, *y_cell, *edge_sign_on_cell;
+  double *dc_edge, *dv_edge, *angle_edge, *x_edge, *y_edge, *weights_on_edge;
+  double *area_triangle, *x_vertex, *y_vertex, *kiteareas_on_vertex;
+  double *edge_sign_on_vertex;
+} swg_hex_tables;
+
+/* replaces PlanarHexagonalMesh::PlanarHexagonalMesh + compute_mesh_arrays +
+ * MPASMesh::finalize_mesh (planar_hexagonal_mesh.cpp:8-62,168-398;
+ * mpas_mesh.cpp:5-57).  Host only, no GPU needed.  ny odd reproduces the
+ * reference's serial construction order (the Kokkos version races there). */
+int swg_planar_hex_mesh_build(int nx, int ny, double dc, swg_hex_tables *out,
+                              double *period_x, double *period_y);
+
+/* Uploads the tables and derives the K-independent coefficient tables the
+ * kernels use.  replaces the device-resident MPASMesh views. */
+int swg_mesh_create(const swg_mesh_desc *desc, swg_mesh *out);
+int swg_mesh_destroy(swg_mesh mesh);
+
+/* ------------------------------------------------------------ state ------
+ * replaces ShallowWaterState (shallow_water_state.hpp:9-16,
+ * shallow_water_state.cpp:7-14): h_cell [C][K], vn_edge [E][K],
+ * tr_cell [T][C][K], device resident, zero-initialised. */
+int swg_state_create(swg_mesh mesh, int ntracers, swg_state *out);
+int swg_state_destroy(swg_state state);
+/* host -> device; tr may be NULL when ntracers == 0 */
+int swg_state_upload(swg_state state, const double *h, const double *vn,
+                     const double *tr, void *stream);
+/* device -> host, synchronous */
+int swg_state_download(swg_state state, double *h, double *vn, double *tr,
+                       void *stream);
+/* device pointers of the three arrays (any out-pointer may be NULL) */
+int swg_state_device_ptrs(swg_state state, double **h, double **vn,
+                          double **tr);
+/* dst <- src, device to device (deep_copy of the three views) */
+int swg_state_copy(swg_state dst, swg_state src, void *stream);
+int swg_state_fill(swg_state state, double value, void *stream);
+
+/* ------------------------------------------------------------ model ------
+ * replaces ShallowWaterParams (shallow_water_params.hpp:7-18). */
+typedef struct swg_params {
+  double f0, grav, drag_coeff, visc_del2, visc_del4, eddy_diff2, eddy_diff4;
+  int ntracers, disable_h_tendency, disable_vn_tendency;
+} swg_params;
+
+/* replaces ShallowWaterModel::ShallowWaterModel (shallow_water_model.cpp:5-41):
+ * each dissipation term is enabled when its coefficient is > 0. */
+int swg_model_create(swg_mesh mesh, const swg_params *params, swg_model *out);
+int swg_model_destroy(swg_model model);
+
+/* replaces the virtual ShallowWaterModel::additional_tendency hook
+ * (shallow_water_model.hpp:42-44).  Called on the host after the built-in
+ * terms of every tendency evaluation with device pointers and the stream the
+ * evaluation runs on; it adds its forcing with its own kernels. */
+typedef void (*swg_forcing_fn)(void *user, double *h_tend, double *vn_tend,
+                               const double *h, const double *vn, double t,
+                               void *stream);
+int swg_model_set_forcing(swg_model model, swg_forcing_fn fn, void *user);
+
+/* replaces ShallowWaterModel::compute_tendency(tend, state, t, add_mode)
+ * (shallow_water_model.cpp:313-347). */
+int swg_compute_tendency(swg_model model, swg_state tend, swg_state state,
+                         double t, int add_mode, void *stream);
+
+/* Named auxiliary field of the last tendency evaluation, device pointer and
+ * element count.  Names: "q_vertex" ((rvort+f)/h at vertices), "rvort_vertex",
+ * "vel_div_cell", "ke_cell", "norm_tr_cell", "thick_flux_edge"
+ * (mean h * vn), "mean_h_edge", "pv_edge" (sum of the two vertex q),
+ * "vel_del2_edge", "vel_del2_rvort_vertex", "vel_del2_div_cell",
+ * "tracer_del2_cell".  Fields a configuration does not need stay unwritten. */
+int swg_model_aux(swg_model model, const char *name, const double **ptr,
+                  long long *count);
+
+/* ---------------------------------------------------------- steppers -----
+ * replaces RK4Stepper / LSRKStepper (time_stepper.hpp:16-38, rk4.cpp,
+ * lsrk.cpp).  kind SWG_STEPPER_RK4 (nstages ignored) or SWG_STEPPER_LSRK
+ * with nstages 5 (Carpenter-Kennedy) or 1 (forward Euler). */
+int swg_stepper_create(swg_model model, int kind, int nstages,
+                       swg_stepper *out);
+int swg_stepper_destroy(swg_stepper stepper);
+/* nsteps calls of TimeStepper::do_step(t0 + s*dt, dt, state)
+ * (time_stepper.hpp:10-11), in place on `state`.  use_graph != 0 replays a
+ * CUDA graph of one step (ignored when a forcing hook is set). */
+int swg_step(swg_stepper stepper, swg_state state, double t0, double dt,
+             int nsteps, int use_graph, void *stream);
+
+/* ------------------------------------------------------- diagnostics -----
+ * replaces energy_integral / mass_integral / circulation_integral
+ * (shallow_water_diagnostics.cpp:5-89).  Synchronous on `stream`. */
+int swg_diag_mass(swg_model model, swg_state state, double *out, void *stream);
+int swg_diag_energy(swg_model model, swg_state state, double *out,
+                    void *stream);
+int swg_diag_circulation(swg_model model, swg_state state, double *out,
+                         void *stream);
+
+/* ---------------------------------------------------------- profiling ----
+ * Diagnostic (no reference counterpart): while enabled, every tendency
+ * kernel is bracketed by a CUDA event pair on its stream and graph replay is
+ * bypassed.  swg_profile_read synchronises those events and returns, per
+ * kernel name (names: max_kernels x 32 chars), the summed milliseconds and
+ * launch count, then clears the record. */
+int swg_profile_enable(int on);
+int swg_profile_read(int max_kernels, char *names, double *total_ms,
+                     long long *launches, int *count);
+
+/* Blocks until `stream` is idle; reports any pending CUDA error. */
+int swg_sync(void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

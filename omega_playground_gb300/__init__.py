@@ -1,0 +1,24 @@
+"""GB300-native shallow-water hot path of omega_playground.
+
+Hand-written sm_103a CUDA kernels (FP64) for the TRiSK tendencies, tracer
+transport / diffusion / hyperdiffusion and the RK4 / low-storage RK stage
+updates on the doubly periodic planar hexagonal MPAS mesh, behind the C ABI
+in include/swgpu.h.  This package is the Python mirror of the reference's
+C++ classes (see shallow_water.py); the C++ mirror is cxx/omega_gpu.hpp.
+"""
+from .shallow_water import (AddMode, LSRKStepper, MPASMesh,  # noqa: F401
+                            PlanarHexagonalMesh, RK4Stepper,
+                            ShallowWaterModel, ShallowWaterParams,
+                            ShallowWaterState, TimeStepper,
+                            circulation_integral, energy_integral,
+                            kernel_launches, mass_integral,
+                            profile_enable, profile_read, sync)
+from ._capi import SwgError, exported_symbols  # noqa: F401
+from . import workloads  # noqa: F401
+
+__all__ = ["AddMode", "LSRKStepper", "MPASMesh", "PlanarHexagonalMesh",
+           "RK4Stepper", "ShallowWaterModel", "ShallowWaterParams",
+           "ShallowWaterState", "TimeStepper", "circulation_integral",
+           "energy_integral", "mass_integral", "sync", "kernel_launches",
+           "profile_enable", "profile_read",
+           "SwgError", "exported_symbols", "workloads"]

@@ -1,0 +1,160 @@
+// Internal declarations of the GB300 shallow-water library (not installed).
+#pragma once
+
+#include "../../include/swgpu.h"
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <string>
+#include <vector>
+
+namespace swg {
+
+// Records the calling thread's error message and returns `code`.
+int fail(int code, const std::string &msg);
+// Maps a CUDA error to SWG_ERR_CUDA (or SWG_ERR_OOM) with context.
+int cuda_fail(cudaError_t err, const char *what);
+int build_planar_hex(int nx, int ny, double dc, swg_hex_tables *t,
+                     double *period_x, double *period_y);
+
+extern std::atomic<long long> g_launches;
+
+constexpr int MAXE = 6; // edges per cell (MPASMesh::maxedges)
+
+// Device views of the K-independent tables derived from the MPAS tables.
+// Per-cell slots beyond nedges_on_cell are padded with coefficient 0 and a
+// valid index, so kernels loop a fixed MAXE times without branches.
+struct MeshView {
+  int ncells, nedges, nvertices, nlayers;
+  int ne;           // compacted edges-on-edge slots per edge (8 or 10)
+  int dv4_differs;  // some edge has dv < dc/4 (the del4 Laplacian differs)
+  // vertices [V][3]
+  const int *ev;      // edges_on_vertex
+  const int *cv;      // cells_on_vertex
+  const double *cvr;  // dc * (1/area_triangle) * edge_sign_on_vertex
+  const double *kvh;  // kiteareas * (1/area_triangle)
+  // cells [C][6]
+  const int *ec;      // edges_on_cell
+  const int *nbc;     // cell across edge j
+  const double *ccd;  // (1/area_cell) * dv * edge_sign_on_cell
+  const double *cke;  // (1/area_cell) * dv * dc * 0.25
+  const double *ckq;  // (1/area_cell) * dv * (1/dc)    (>= 0)
+  const double *ccdh; // -0.5 * ccd
+  // edges
+  const int *ce;      // cells_on_edge [E][2]
+  const int *ve;      // vertices_on_edge [E][2]
+  const double *inv_dc, *inv_dv, *inv_dv4; // [E]
+  const int *eoe;     // nonzero-weight edges_on_edge [E][ne]
+  const double *woe;  // their weights / 4 [E][ne]
+  const double *scale2, *scale4; // [E]
+  const double *mask; // edge_mask [E][K], nullptr when all ones
+  // diagnostics only
+  const double *area_cell_d; // [C]
+  const double *area_tri_d;  // [V]
+  const double *dcs_v;       // [V][3] dc * edge_sign_on_vertex
+};
+
+// Parameters and parameter-scaled coefficient tables of one model.
+struct ModelView {
+  double grav;
+  const double *f_vertex; // [V]
+  const double *gidc;     // [E] grav / dc
+  const double *c2e;      // [E] visc_del2 * scale2
+  const double *c4e;      // [E] -visc_del4 * scale4
+  const double *kd2;      // [C][6] eddy_diff2 * scale2 * ckq
+  const double *r4;       // [C][6] -eddy_diff4 * scale4 * ckq
+  const double *r4sum;    // [C] sum of r4
+  int ntracers;
+  int vel_del2, vel_del4, tr_del2, tr_del4, do_h, do_vn;
+};
+
+// Intermediate fields of one tendency evaluation (device).
+struct AuxView {
+  double *q, *zeta, *z4;          // [V][K]
+  double *div, *ke, *d4;          // [C][K]
+  double *ntr, *lap;              // [T][C][K]
+  double *F, *G, *Q, *mh, *u2, *d2u, *d2u4; // [E][K]
+};
+
+enum EpiMode {
+  EPI_REPLACE = 0,   // tend = x
+  EPI_INCREMENT = 1, // tend += x
+  EPI_LSRK = 2,      // t = a*tend + x; tend = t; state += dtb*t
+  EPI_RK4_FIRST = 3, // acc = old + dtb*x; out = old + dta*x
+  EPI_RK4_MID = 4,   // acc += dtb*x;      out = old + dta*x
+  EPI_RK4_LAST = 5,  // out = acc + dtb*x
+};
+
+struct FieldIO {
+  double *tend;      // REPLACE / INCREMENT / LSRK
+  const double *old; // RK4 first & mid: state at the start of the step
+  double *acc;       // RK4: accumulator
+  double *out;       // LSRK: state; RK4: next stage input or final state
+};
+
+struct Epilogue {
+  int mode;
+  double a, dtb, dta;
+};
+
+struct StageArgs {
+  const double *h, *vn, *tr; // stage input state
+  FieldIO fh, fvn, ftr;
+  Epilogue ep;
+};
+
+void launch_tendency(const MeshView &m, const ModelView &p, const AuxView &a,
+                     const StageArgs &s, cudaStream_t st);
+void launch_axpby(double *y, const double *x, const double *z, double alpha,
+                  double beta, long long n, int kind, cudaStream_t st);
+// opt-in per-kernel CUDA-event timing (swg_profile_enable)
+bool profiling_enabled();
+int profile_enable(int on);
+int profile_read(int max_kernels, char *names, double *total_ms,
+                 long long *launches, int *count);
+int reduce_diag(int which, const MeshView &m, const ModelView &p,
+                const double *h, const double *vn, double *partials,
+                int npart, double *out, cudaStream_t st);
+
+} // namespace swg
+
+// ------------------------------------------------------------- handles ---
+
+struct swg_mesh_s {
+  int ncells, nedges, nvertices, nlayers;
+  swg::MeshView view;
+  std::vector<void *> allocs;
+  // host copies of the per-edge scaling (the model scales them)
+  std::vector<double> scale2_h, scale4_h, ckq_h, inv_dc_h;
+  std::vector<int> ec_h;
+};
+
+struct swg_state_s {
+  swg_mesh mesh;
+  int ntracers;
+  double *h, *vn, *tr;
+  void *block;
+};
+
+struct swg_model_s {
+  swg_mesh mesh;
+  swg_params params;
+  swg::ModelView view;
+  swg::AuxView aux;
+  std::vector<void *> allocs;
+  double *partials; // diagnostic partial sums
+  swg_forcing_fn forcing;
+  void *forcing_user;
+};
+
+struct swg_stepper_s {
+  swg_model model;
+  int kind, nstages;
+  std::vector<double> rka, rkb, rkc;
+  swg_state tend, acc, p0, p1, old;
+  cudaGraphExec_t graph;       // one captured step (fused path)
+  swg_state graph_state;
+  double graph_dt;
+  long long graph_launches;    // kernels per captured step
+};

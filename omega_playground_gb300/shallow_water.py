@@ -1,0 +1,386 @@
+"""Python mirror of omega_playground's C++ interface over the C ABI.
+
+Class and member names follow the reference (src/mesh, src/model,
+src/time_integration) so code written against it reads the same:
+
+    mesh = PlanarHexagonalMesh(nx, ny, dc, nlayers)        # planar_hexagonal_mesh.hpp:8-28
+    params = ShallowWaterParams(m_f0=1e-4, m_ntracers=1)   # shallow_water_params.hpp:7-18
+    model = ShallowWaterModel(mesh, params)                # shallow_water_model.hpp:14-51
+    state = ShallowWaterState(mesh, params)                # shallow_water_state.hpp:9-16
+    stepper = LSRKStepper(model, 5)                        # time_stepper.hpp:16-25
+    stepper.do_step(t, dt, state)                          # time_stepper.hpp:10-11
+    mass_integral(state, model)                            # shallow_water_diagnostics.hpp:7-12
+
+The state lives on the GPU; ``upload`` / ``download`` move numpy arrays
+(FP64, [entity][k], tracers [l][cell][k]).  Every compute call is a CUDA
+launch on ``stream`` (a raw cudaStream_t as int, default the legacy stream).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import enum
+
+import numpy as np
+
+from . import _capi
+from ._capi import check, lib
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def _d(a):
+    if a is None:
+        return None
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError("expected a C-contiguous float64 array")
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    if a is None:
+        return None
+    if a.dtype != np.int32 or not a.flags.c_contiguous:
+        raise TypeError("expected a C-contiguous int32 array")
+    return a.ctypes.data_as(_ip)
+
+
+def _s(stream):
+    return C.c_void_p(int(stream)) if stream else None
+
+
+class AddMode(enum.IntEnum):
+    """shallow_water_model.hpp:11"""
+    replace = 0
+    increment = 1
+
+
+class MPASMesh:
+    """MPAS mesh tables (mpas_mesh.hpp:7-71) uploaded to the GPU.
+
+    Subclasses (PlanarHexagonalMesh) fill ``tables``; ``finalize`` uploads
+    them.  ``mesh_scaling_del2/4`` and ``edge_mask`` default to ones as in
+    MPASMesh::finalize_mesh (mpas_mesh.cpp:48-50)."""
+
+    maxedges = 6
+
+    def __init__(self):
+        self.tables = {}
+        self._h = None
+
+    def finalize(self, mesh_scaling_del2=None, mesh_scaling_del4=None,
+                 edge_mask=None):
+        t = self.tables
+        d = _capi.MeshDesc()
+        d.ncells, d.nedges, d.nvertices = self.m_ncells, self.m_nedges, \
+            self.m_nvertices
+        d.nlayers = self.m_nlayers
+        for n in ("nedges_on_cell", "edges_on_cell", "nedges_on_edge",
+                  "edges_on_edge", "cells_on_edge", "vertices_on_edge",
+                  "edges_on_vertex", "cells_on_vertex"):
+            setattr(d, n, _i(t[n]))
+        for n in ("area_cell", "edge_sign_on_cell", "dc_edge", "dv_edge",
+                  "weights_on_edge", "area_triangle", "kiteareas_on_vertex",
+                  "edge_sign_on_vertex"):
+            setattr(d, n, _d(t[n]))
+        self._keep = [np.ascontiguousarray(x, np.float64) if x is not None
+                      else None for x in (mesh_scaling_del2,
+                                          mesh_scaling_del4, edge_mask)]
+        d.mesh_scaling_del2 = _d(self._keep[0])
+        d.mesh_scaling_del4 = _d(self._keep[1])
+        d.edge_mask = _d(self._keep[2])
+        h = C.c_void_p()
+        check(lib().swg_mesh_create(C.byref(d), C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __getattr__(self, name):
+        t = self.__dict__.get("tables")
+        if t is not None and name.startswith("m_") and name[2:] in t:
+            return t[name[2:]]
+        raise AttributeError(name)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _capi._lib is not None:
+            _capi._lib.swg_mesh_destroy(self._h)
+            self._h = None
+
+
+class PlanarHexagonalMesh(MPASMesh):
+    """Doubly periodic planar hexagonal mesh (planar_hexagonal_mesh.cpp:5-62).
+
+    ``dc`` defaults to 1/nx like the reference's 3-argument constructor."""
+
+    def __init__(self, nx: int, ny: int, dc: float | None = None,
+                 nlayers: int = 1, **finalize_kw):
+        super().__init__()
+        self.m_nx, self.m_ny = int(nx), int(ny)
+        self.m_dc = float(1.0 / nx if dc is None else dc)
+        self.m_nlayers = int(nlayers)
+        self.m_ncells = nx * ny
+        self.m_nedges = 3 * nx * ny
+        self.m_nvertices = 2 * nx * ny
+        sizes = {"C": self.m_ncells, "E": self.m_nedges, "V": self.m_nvertices}
+        ht = _capi.HexTables()
+        for name, (ent, w) in _capi.HEX_SHAPE.items():
+            dt = np.int32 if name in _capi.HEX_INT else np.float64
+            shape = (sizes[ent], w) if w > 1 else (sizes[ent],)
+            self.tables[name] = np.zeros(shape, dt)
+            setattr(ht, name, (_i if dt == np.int32 else _d)(self.tables[name]))
+        px, py = C.c_double(), C.c_double()
+        check(lib().swg_planar_hex_mesh_build(self.m_nx, self.m_ny, self.m_dc,
+                                              C.byref(ht), C.byref(px),
+                                              C.byref(py)))
+        self.m_period_x, self.m_period_y = px.value, py.value
+        self.finalize(**finalize_kw)
+
+
+@dataclasses.dataclass
+class ShallowWaterParams:
+    """shallow_water_params.hpp:7-18"""
+    m_f0: float = 0.0
+    m_grav: float = 9.81
+    m_drag_coeff: float = 0.0
+    m_visc_del2: float = 0.0
+    m_visc_del4: float = 0.0
+    m_eddy_diff2: float = 0.0
+    m_eddy_diff4: float = 0.0
+    m_ntracers: int = 0
+    m_disable_h_tendency: bool = False
+    m_disable_vn_tendency: bool = False
+
+    def _c(self):
+        return _capi.Params(self.m_f0, self.m_grav, self.m_drag_coeff,
+                            self.m_visc_del2, self.m_visc_del4,
+                            self.m_eddy_diff2, self.m_eddy_diff4,
+                            self.m_ntracers, int(self.m_disable_h_tendency),
+                            int(self.m_disable_vn_tendency))
+
+
+class ShallowWaterState:
+    """h_cell [C][K], vn_edge [E][K], tr_cell [T][C][K] on the GPU
+    (shallow_water_state.cpp:7-14)."""
+
+    def __init__(self, mesh: MPASMesh, params_or_ntracers=0):
+        nt = (params_or_ntracers.m_ntracers
+              if isinstance(params_or_ntracers, ShallowWaterParams)
+              else int(params_or_ntracers))
+        self.mesh, self.ntracers = mesh, nt
+        h = C.c_void_p()
+        check(lib().swg_state_create(mesh.handle, nt, C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def shapes(self):
+        m = self.mesh
+        return ((m.m_ncells, m.m_nlayers), (m.m_nedges, m.m_nlayers),
+                (self.ntracers, m.m_ncells, m.m_nlayers))
+
+    def upload(self, h, vn, tr=None, stream=None):
+        sh, sv, st = self.shapes()
+        h = np.ascontiguousarray(h, np.float64).reshape(sh)
+        vn = np.ascontiguousarray(vn, np.float64).reshape(sv)
+        tr = (np.ascontiguousarray(tr, np.float64).reshape(st)
+              if self.ntracers else None)
+        check(lib().swg_state_upload(self._h, _d(h), _d(vn), _d(tr),
+                                     _s(stream)))
+        lib().swg_sync(_s(stream))  # host arrays may be temporaries
+
+    def download(self, stream=None, out=None):
+        """Synchronous copy to host; `out` = (h, vn, tr) preallocated
+        C-contiguous float64 arrays (e.g. pinned) or None for new ones."""
+        sh, sv, st = self.shapes()
+        if out is None:
+            out = (np.empty(sh), np.empty(sv), np.empty(st))
+        h, vn, tr = out
+        check(lib().swg_state_download(self._h, _d(h), _d(vn),
+                                       _d(tr) if self.ntracers else None,
+                                       _s(stream)))
+        return h, vn, tr
+
+    def device_ptrs(self):
+        p = [_dp(), _dp(), _dp()]
+        check(lib().swg_state_device_ptrs(self._h, *[C.byref(x) for x in p]))
+        return tuple(C.cast(x, C.c_void_p).value for x in p)
+
+    def copy_from(self, other: "ShallowWaterState", stream=None):
+        check(lib().swg_state_copy(self._h, other._h, _s(stream)))
+
+    def fill(self, value: float, stream=None):
+        check(lib().swg_state_fill(self._h, float(value), _s(stream)))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _capi._lib is not None:
+            _capi._lib.swg_state_destroy(self._h)
+            self._h = None
+
+
+class ShallowWaterModel:
+    """shallow_water_model.hpp:14-51.  Override ``additional_tendency`` to
+    add forcing (it receives device pointers and the CUDA stream)."""
+
+    def __init__(self, mesh: MPASMesh, params: ShallowWaterParams):
+        self.m_mesh, self.m_params = mesh, params
+        p = params._c()
+        h = C.c_void_p()
+        check(lib().swg_model_create(mesh.handle, C.byref(p), C.byref(h)))
+        self._h = h
+        self._cb = None
+        if type(self).additional_tendency is not \
+                ShallowWaterModel.additional_tendency:
+            def tramp(user, ht, vt, hp, vp, t, stream):
+                self.additional_tendency(C.cast(ht, C.c_void_p).value,
+                                         C.cast(vt, C.c_void_p).value,
+                                         C.cast(hp, C.c_void_p).value,
+                                         C.cast(vp, C.c_void_p).value, t,
+                                         stream or 0)
+            self._cb = _capi.FORCING_FN(tramp)
+            check(lib().swg_model_set_forcing(self._h, self._cb, None))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def additional_tendency(self, h_tend, vn_tend, h, vn, t, stream):
+        """shallow_water_model.hpp:42-44 (no-op)."""
+
+    def compute_tendency(self, tend: ShallowWaterState,
+                         state: ShallowWaterState, t: float,
+                         add_mode: AddMode = AddMode.replace, stream=None):
+        check(lib().swg_compute_tendency(self._h, tend.handle, state.handle,
+                                         float(t), int(add_mode), _s(stream)))
+
+    def aux(self, name: str) -> np.ndarray:
+        """Copy of a named intermediate of the last tendency evaluation."""
+        p, n = _dp(), C.c_longlong()
+        check(lib().swg_model_aux(self._h, name.encode(), C.byref(p),
+                                  C.byref(n)))
+        out = np.empty(n.value)
+        cudart = _cudart()
+        err = cudart.cudaMemcpy(out.ctypes.data_as(C.c_void_p),
+                                C.cast(p, C.c_void_p), C.c_size_t(8 * n.value),
+                                C.c_int(2))
+        if err:
+            raise _capi.SwgError(3, f"cudaMemcpy failed ({err})")
+        return out
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _capi._lib is not None:
+            _capi._lib.swg_model_destroy(self._h)
+            self._h = None
+
+
+_cudart_lib = None
+
+
+def _cudart():
+    global _cudart_lib
+    if _cudart_lib is None:
+        lib()  # loads libcudart.so.13 as a dependency
+        _cudart_lib = C.CDLL("libcudart.so.13")
+        _cudart_lib.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t,
+                                           C.c_int]
+    return _cudart_lib
+
+
+class TimeStepper:
+    """time_stepper.hpp:8-14"""
+
+    _kind = None
+
+    def __init__(self, shallow_water: ShallowWaterModel, nstages: int = 0):
+        self.m_shallow_water = shallow_water
+        h = C.c_void_p()
+        check(lib().swg_stepper_create(shallow_water.handle, self._kind,
+                                       int(nstages), C.byref(h)))
+        self._h = h
+
+    def do_step(self, t: float, dt: float, state: ShallowWaterState,
+                stream=None):
+        check(lib().swg_step(self._h, state.handle, float(t), float(dt), 1, 0,
+                             _s(stream)))
+
+    def step(self, state: ShallowWaterState, t0: float, dt: float,
+             nsteps: int, use_graph: bool = True, stream=None):
+        """nsteps do_step calls (t0 + s*dt); replays a CUDA graph of one
+        step when no forcing hook is set."""
+        check(lib().swg_step(self._h, state.handle, float(t0), float(dt),
+                             int(nsteps), int(use_graph), _s(stream)))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _capi._lib is not None:
+            _capi._lib.swg_stepper_destroy(self._h)
+            self._h = None
+
+
+class RK4Stepper(TimeStepper):
+    """time_stepper.hpp:27-38, rk4.cpp"""
+    _kind = 0
+    nstages = 4
+
+    def __init__(self, shallow_water: ShallowWaterModel):
+        super().__init__(shallow_water, 4)
+
+
+class LSRKStepper(TimeStepper):
+    """time_stepper.hpp:16-25, lsrk.cpp (nstages 5 or 1)"""
+    _kind = 1
+
+    def __init__(self, shallow_water: ShallowWaterModel, nstages: int = 5):
+        self.m_nstages = nstages
+        super().__init__(shallow_water, nstages)
+
+
+def _diag(fn, state, model, stream=None):
+    out = C.c_double()
+    check(fn(model.handle, state.handle, C.byref(out), _s(stream)))
+    return out.value
+
+
+def mass_integral(state, model, stream=None):
+    """shallow_water_diagnostics.cpp:40-58"""
+    return _diag(lib().swg_diag_mass, state, model, stream)
+
+
+def energy_integral(state, model, stream=None):
+    """shallow_water_diagnostics.cpp:5-38"""
+    return _diag(lib().swg_diag_energy, state, model, stream)
+
+
+def circulation_integral(state, model, stream=None):
+    """shallow_water_diagnostics.cpp:60-89"""
+    return _diag(lib().swg_diag_circulation, state, model, stream)
+
+
+def sync(stream=None):
+    check(lib().swg_sync(_s(stream)))
+
+
+def kernel_launches() -> int:
+    return int(lib().swg_kernel_launches())
+
+
+def profile_enable(on: bool = True) -> None:
+    """Per-kernel CUDA-event timing of subsequent tendency launches."""
+    check(lib().swg_profile_enable(int(on)))
+
+
+def profile_read(max_kernels: int = 16) -> dict:
+    """{kernel name: (total ms, launches)} recorded since the last read."""
+    names = C.create_string_buffer(32 * max_kernels)
+    ms = (C.c_double * max_kernels)()
+    n = (C.c_longlong * max_kernels)()
+    cnt = C.c_int()
+    check(lib().swg_profile_read(max_kernels, names, ms, n, C.byref(cnt)))
+    out = {}
+    for j in range(cnt.value):
+        nm = names.raw[32 * j:32 * j + 32].split(b"\0")[0].decode()
+        out[nm] = (ms[j], int(n[j]))
+    return out

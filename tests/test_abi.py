@@ -1,0 +1,81 @@
+"""The C-ABI library loads on a machine without a GPU, exports every entry
+point include/swgpu.h declares, and rejects bad input on the host before any
+CUDA call."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from omega_playground_gb300 import _build, _capi
+
+HEADER = os.path.join(os.path.dirname(_build.PKG), "include", "swgpu.h")
+
+
+def declared():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(swg_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _capi.lib()
+    names = declared()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) == set(_capi.exported_symbols())
+
+
+def test_version_and_launch_counter():
+    assert b"sm_103a" in _capi.lib().swg_version()
+    assert _capi.lib().swg_kernel_launches() >= 0
+
+
+def _desc_for(nx, ny, K):
+    from test_mesh_builder import product_tables
+    t, _, _ = product_tables(nx, ny, 1.0)
+    d = _capi.MeshDesc()
+    d.ncells, d.nedges, d.nvertices, d.nlayers = nx * ny, 3 * nx * ny, \
+        2 * nx * ny, K
+    for n in ("nedges_on_cell", "edges_on_cell", "nedges_on_edge",
+              "edges_on_edge", "cells_on_edge", "vertices_on_edge",
+              "edges_on_vertex", "cells_on_vertex"):
+        setattr(d, n, t[n].ctypes.data_as(C.POINTER(C.c_int)))
+    for n in ("area_cell", "edge_sign_on_cell", "dc_edge", "dv_edge",
+              "weights_on_edge", "area_triangle", "kiteareas_on_vertex",
+              "edge_sign_on_vertex"):
+        setattr(d, n, t[n].ctypes.data_as(C.POINTER(C.c_double)))
+    return d, t
+
+
+def test_mesh_create_rejects_out_of_range_connectivity():
+    d, t = _desc_for(4, 4, 2)
+    t["cells_on_edge"][5, 1] = 16  # == ncells: out of range
+    out = C.c_void_p()
+    rc = _capi.lib().swg_mesh_create(C.byref(d), C.byref(out))
+    assert rc == 1 and not out.value
+    assert b"out of range" in _capi.lib().swg_last_error()
+
+
+def test_mesh_create_rejects_bad_sizes_and_nulls():
+    d, _ = _desc_for(4, 4, 2)
+    d.nlayers = 0
+    out = C.c_void_p()
+    assert _capi.lib().swg_mesh_create(C.byref(d), C.byref(out)) == 1
+    d, _ = _desc_for(4, 4, 2)
+    d.dc_edge = None
+    assert _capi.lib().swg_mesh_create(C.byref(d), C.byref(out)) == 1
+    assert b"NULL" in _capi.lib().swg_last_error()
+    d, t = _desc_for(4, 4, 2)
+    t["nedges_on_cell"][3] = 7
+    assert _capi.lib().swg_mesh_create(C.byref(d), C.byref(out)) == 1
+
+
+def test_null_handles_are_errors_not_crashes():
+    lib = _capi.lib()
+    assert lib.swg_state_create(None, 0, C.byref(C.c_void_p())) == 1
+    assert lib.swg_model_create(None, None, C.byref(C.c_void_p())) == 1
+    assert lib.swg_stepper_create(None, 0, 4, C.byref(C.c_void_p())) == 1
+    assert lib.swg_step(None, None, 0.0, 1.0, 1, 0, None) == 1
+    assert lib.swg_compute_tendency(None, None, None, 0.0, 0, None) == 1
+    assert lib.swg_mesh_destroy(None) == 0
