@@ -262,9 +262,16 @@ def run_ours(args, wl):
     dom_bytes = alg_per_unit.get(dom, 0) * CK
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
     stage_bytes = wl.alg_bytes_per_stage()
+    # DRAM bytes per cell-level of the dominant kernel from one ncu capture
+    # (dram__bytes_read.sum + dram__bytes_write.sum of k_cell_final on the
+    # 256x256x64x8 case: 1.932 GB for 4,194,304 cell-levels), scaled to
+    # this launch by its cell-level count; traffic grows in proportion.
+    ncu_bytes_per_unit = {"k_cell_final": 1.932e9 / 4194304}
+    traffic = (ncu_bytes_per_unit[dom] * CK
+               if dom in ncu_bytes_per_unit and wl.ntracers == 8 else None)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved,
                 "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_source": peak_kind, "traffic": None,
+                "peak_source": peak_kind, "traffic": traffic,
                 "alg_bytes_per_launch": dom_bytes,
                 "launch_ms": dom_ms,
                 "stage": {"achieved": stage_bytes / (stage_ms / 1e3) / 1e9,

@@ -1,0 +1,446 @@
+// omega_gpu.hpp - C++ drop-in for omega_playground's mesh, state, model and
+// time-stepper classes, running on the GB300 CUDA library (libswgpu.so)
+// through the C ABI in swgpu.h.
+//
+// Names and signatures follow the reference (paths inside its checkout):
+//   MPASMesh, PlanarHexagonalMesh      src/mesh/mpas_mesh.hpp:7-71,
+//                                      src/mesh/planar_hexagonal_mesh.hpp:8-28
+//   ShallowWaterParams                 src/model/shallow_water_params.hpp:7-18
+//   ShallowWaterState                  src/model/shallow_water_state.hpp:9-16
+//   ShallowWaterModel, AddMode         src/model/shallow_water_model.hpp:11-51
+//   TimeStepper, LSRKStepper, RK4Stepper
+//                                      src/time_integration/time_stepper.hpp:8-38
+//   energy/mass/circulation_integral   src/model/shallow_water_diagnostics.hpp:7-12
+//
+// Differences a reference user sees:
+//  - Real1d/Real2d/Real3d are DeviceView (a device pointer plus extents,
+//    LayoutRight), usable inside the user's own __global__ kernels, instead
+//    of Kokkos::View.  Mesh tables are host std::vector members with the
+//    reference's names (m_x_cell, m_angle_edge, ...); device copies of the
+//    geometry a forcing kernel needs are available as d_* members.
+//  - ShallowWaterModel::additional_tendency receives DeviceViews and runs on
+//    the library's stream (the legacy default stream here); an override
+//    launches its own kernel.
+//  - Errors throw std::runtime_error with the library's message.
+#pragma once
+
+#include <swgpu.h>
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace omega {
+
+using Real = double;
+using Int = int;
+constexpr Real pi = 3.14159265358979323846;
+constexpr Int vector_length = 1;
+
+inline void swg_check(int rc) {
+  if (rc != SWG_OK)
+    throw std::runtime_error(std::string("swgpu: ") + swg_last_error());
+}
+
+inline void fence() { swg_check(swg_sync(nullptr)); }
+
+// Non-owning view of device memory, LayoutRight like the reference's Views.
+template <class T, int R> struct DeviceView {
+  T *m_data = nullptr;
+  Int m_ext[R] = {};
+  __host__ __device__ T &operator()(Int i) const { return m_data[i]; }
+  __host__ __device__ T &operator()(Int i, Int j) const {
+    return m_data[size_t(i) * m_ext[1] + j];
+  }
+  __host__ __device__ T &operator()(Int i, Int j, Int k) const {
+    return m_data[(size_t(i) * m_ext[1] + j) * m_ext[2] + k];
+  }
+  __host__ __device__ Int extent(int r) const { return m_ext[r]; }
+  __host__ __device__ T *data() const { return m_data; }
+  size_t size() const {
+    size_t n = 1;
+    for (int r = 0; r < R; ++r)
+      n *= size_t(m_ext[r]);
+    return n;
+  }
+  operator DeviceView<const T, R>() const {
+    DeviceView<const T, R> v;
+    v.m_data = m_data;
+    for (int r = 0; r < R; ++r)
+      v.m_ext[r] = m_ext[r];
+    return v;
+  }
+};
+using Real1d = DeviceView<Real, 1>;
+using Real2d = DeviceView<Real, 2>;
+using Real3d = DeviceView<Real, 3>;
+using RealConst1d = DeviceView<const Real, 1>;
+using RealConst2d = DeviceView<const Real, 2>;
+using RealConst3d = DeviceView<const Real, 3>;
+
+// Owning device array (cudaMalloc / cudaFree) with host round trips.
+template <class T> class DeviceArray {
+public:
+  DeviceArray() = default;
+  explicit DeviceArray(const std::vector<T> &host) { assign(host); }
+  DeviceArray(const DeviceArray &) = delete;
+  DeviceArray &operator=(const DeviceArray &) = delete;
+  ~DeviceArray() { cudaFree(m_ptr); }
+  void assign(const std::vector<T> &host) {
+    cudaFree(m_ptr);
+    m_ptr = nullptr;
+    m_n = host.size();
+    if (cudaMalloc(&m_ptr, std::max<size_t>(m_n, 1) * sizeof(T)) != cudaSuccess)
+      throw std::runtime_error("DeviceArray: cudaMalloc failed");
+    if (m_n && cudaMemcpy(m_ptr, host.data(), m_n * sizeof(T),
+                          cudaMemcpyHostToDevice) != cudaSuccess)
+      throw std::runtime_error("DeviceArray: cudaMemcpy failed");
+  }
+  T *data() const { return m_ptr; }
+  size_t size() const { return m_n; }
+  DeviceView<T, 1> view() const {
+    DeviceView<T, 1> v;
+    v.m_data = m_ptr;
+    v.m_ext[0] = Int(m_n);
+    return v;
+  }
+
+private:
+  T *m_ptr = nullptr;
+  size_t m_n = 0;
+};
+
+// ------------------------------------------------------------------- mesh --
+
+struct MPASMesh {
+  static constexpr Int maxedges = 6;
+  Int m_nlayers = 0, m_nlayers_vec = 0, m_ncells = 0, m_nedges = 0,
+      m_nvertices = 0;
+
+  std::vector<Int> m_nedges_on_cell, m_edges_on_cell, m_cells_on_cell,
+      m_vertices_on_cell, m_kite_index_on_cell;
+  std::vector<Real> m_area_cell, m_x_cell, m_y_cell, m_edge_sign_on_cell;
+  std::vector<Int> m_nedges_on_edge, m_edges_on_edge, m_cells_on_edge,
+      m_vertices_on_edge;
+  std::vector<Real> m_dc_edge, m_dv_edge, m_angle_edge, m_x_edge, m_y_edge,
+      m_weights_on_edge, m_mesh_scaling_del2, m_mesh_scaling_del4,
+      m_edge_mask;
+  std::vector<Int> m_edges_on_vertex, m_cells_on_vertex;
+  std::vector<Real> m_area_triangle, m_x_vertex, m_y_vertex,
+      m_kiteareas_on_vertex, m_edge_sign_on_vertex;
+
+  // device copies of the geometry user kernels typically read
+  DeviceArray<Real> d_x_cell, d_y_cell, d_x_edge, d_y_edge, d_angle_edge;
+
+  swg_mesh m_handle = nullptr;
+
+  MPASMesh() = default;
+  MPASMesh(const MPASMesh &) = delete;
+  MPASMesh &operator=(const MPASMesh &) = delete;
+  virtual ~MPASMesh() { swg_mesh_destroy(m_handle); }
+
+  // Uploads the tables (MPASMesh::finalize_mesh, mpas_mesh.cpp:5-57: scaling
+  // and mask default to ones when left empty).
+  void finalize_mesh() {
+    swg_mesh_desc d{};
+    d.ncells = m_ncells;
+    d.nedges = m_nedges;
+    d.nvertices = m_nvertices;
+    d.nlayers = m_nlayers;
+    d.nedges_on_cell = m_nedges_on_cell.data();
+    d.edges_on_cell = m_edges_on_cell.data();
+    d.nedges_on_edge = m_nedges_on_edge.data();
+    d.edges_on_edge = m_edges_on_edge.data();
+    d.cells_on_edge = m_cells_on_edge.data();
+    d.vertices_on_edge = m_vertices_on_edge.data();
+    d.edges_on_vertex = m_edges_on_vertex.data();
+    d.cells_on_vertex = m_cells_on_vertex.data();
+    d.area_cell = m_area_cell.data();
+    d.edge_sign_on_cell = m_edge_sign_on_cell.data();
+    d.dc_edge = m_dc_edge.data();
+    d.dv_edge = m_dv_edge.data();
+    d.weights_on_edge = m_weights_on_edge.data();
+    d.area_triangle = m_area_triangle.data();
+    d.kiteareas_on_vertex = m_kiteareas_on_vertex.data();
+    d.edge_sign_on_vertex = m_edge_sign_on_vertex.data();
+    d.mesh_scaling_del2 =
+        m_mesh_scaling_del2.empty() ? nullptr : m_mesh_scaling_del2.data();
+    d.mesh_scaling_del4 =
+        m_mesh_scaling_del4.empty() ? nullptr : m_mesh_scaling_del4.data();
+    d.edge_mask = m_edge_mask.empty() ? nullptr : m_edge_mask.data();
+    swg_mesh_destroy(m_handle);
+    m_handle = nullptr;
+    swg_check(swg_mesh_create(&d, &m_handle));
+    if (!m_x_cell.empty())
+      d_x_cell.assign(m_x_cell);
+    if (!m_y_cell.empty())
+      d_y_cell.assign(m_y_cell);
+    if (!m_x_edge.empty())
+      d_x_edge.assign(m_x_edge);
+    if (!m_y_edge.empty())
+      d_y_edge.assign(m_y_edge);
+    if (!m_angle_edge.empty())
+      d_angle_edge.assign(m_angle_edge);
+  }
+};
+
+struct PlanarHexagonalMesh : MPASMesh {
+  Int m_nx, m_ny;
+  Real m_dc, m_period_x, m_period_y;
+
+  PlanarHexagonalMesh(Int nx, Int ny, Int nlayers = 1)
+      : PlanarHexagonalMesh(nx, ny, 1. / nx, nlayers) {}
+  PlanarHexagonalMesh(Int nx, Int ny, Real dc, Int nlayers = 1)
+      : m_nx(nx), m_ny(ny), m_dc(dc) {
+    m_nlayers = nlayers;
+    m_nlayers_vec = nlayers;
+    m_ncells = nx * ny;
+    m_nedges = 3 * m_ncells;
+    m_nvertices = 2 * m_ncells;
+    const size_t C = m_ncells, E = m_nedges, V = m_nvertices;
+    m_nedges_on_cell.resize(C);
+    m_edges_on_cell.resize(6 * C);
+    m_cells_on_cell.resize(6 * C);
+    m_vertices_on_cell.resize(6 * C);
+    m_kite_index_on_cell.resize(6 * C);
+    m_area_cell.resize(C);
+    m_x_cell.resize(C);
+    m_y_cell.resize(C);
+    m_edge_sign_on_cell.resize(6 * C);
+    m_nedges_on_edge.resize(E);
+    m_edges_on_edge.resize(12 * E);
+    m_cells_on_edge.resize(2 * E);
+    m_vertices_on_edge.resize(2 * E);
+    m_dc_edge.resize(E);
+    m_dv_edge.resize(E);
+    m_angle_edge.resize(E);
+    m_x_edge.resize(E);
+    m_y_edge.resize(E);
+    m_weights_on_edge.resize(12 * E);
+    m_edges_on_vertex.resize(3 * V);
+    m_cells_on_vertex.resize(3 * V);
+    m_area_triangle.resize(V);
+    m_x_vertex.resize(V);
+    m_y_vertex.resize(V);
+    m_kiteareas_on_vertex.resize(3 * V);
+    m_edge_sign_on_vertex.resize(3 * V);
+    swg_hex_tables t{};
+    t.nedges_on_cell = m_nedges_on_cell.data();
+    t.edges_on_cell = m_edges_on_cell.data();
+    t.cells_on_cell = m_cells_on_cell.data();
+    t.vertices_on_cell = m_vertices_on_cell.data();
+    t.kite_index_on_cell = m_kite_index_on_cell.data();
+    t.nedges_on_edge = m_nedges_on_edge.data();
+    t.edges_on_edge = m_edges_on_edge.data();
+    t.cells_on_edge = m_cells_on_edge.data();
+    t.vertices_on_edge = m_vertices_on_edge.data();
+    t.edges_on_vertex = m_edges_on_vertex.data();
+    t.cells_on_vertex = m_cells_on_vertex.data();
+    t.area_cell = m_area_cell.data();
+    t.x_cell = m_x_cell.data();
+    t.y_cell = m_y_cell.data();
+    t.edge_sign_on_cell = m_edge_sign_on_cell.data();
+    t.dc_edge = m_dc_edge.data();
+    t.dv_edge = m_dv_edge.data();
+    t.angle_edge = m_angle_edge.data();
+    t.x_edge = m_x_edge.data();
+    t.y_edge = m_y_edge.data();
+    t.weights_on_edge = m_weights_on_edge.data();
+    t.area_triangle = m_area_triangle.data();
+    t.x_vertex = m_x_vertex.data();
+    t.y_vertex = m_y_vertex.data();
+    t.kiteareas_on_vertex = m_kiteareas_on_vertex.data();
+    t.edge_sign_on_vertex = m_edge_sign_on_vertex.data();
+    swg_check(swg_planar_hex_mesh_build(nx, ny, dc, &t, &m_period_x,
+                                        &m_period_y));
+    finalize_mesh();
+  }
+};
+
+// ------------------------------------------------------------------ model --
+
+struct ShallowWaterParams {
+  Real m_f0;
+  Real m_grav = 9.81;
+  Real m_drag_coeff = 0;
+  Real m_visc_del2 = 0;
+  Real m_visc_del4 = 0;
+  Real m_eddy_diff2 = 0;
+  Real m_eddy_diff4 = 0;
+  Int m_ntracers = 0;
+  bool m_disable_h_tendency = false;
+  bool m_disable_vn_tendency = false;
+};
+
+struct ShallowWaterState {
+  std::shared_ptr<swg_state_s> m_handle;
+  Real2d m_h_cell;
+  Real2d m_vn_edge;
+  Real3d m_tr_cell;
+
+  ShallowWaterState(const MPASMesh *mesh, Int ntracers) {
+    swg_state s = nullptr;
+    swg_check(swg_state_create(mesh->m_handle, ntracers, &s));
+    m_handle.reset(s, [](swg_state p) { swg_state_destroy(p); });
+    double *h, *vn, *tr;
+    swg_check(swg_state_device_ptrs(s, &h, &vn, &tr));
+    m_h_cell.m_data = h;
+    m_h_cell.m_ext[0] = mesh->m_ncells;
+    m_h_cell.m_ext[1] = mesh->m_nlayers;
+    m_vn_edge.m_data = vn;
+    m_vn_edge.m_ext[0] = mesh->m_nedges;
+    m_vn_edge.m_ext[1] = mesh->m_nlayers;
+    m_tr_cell.m_data = tr;
+    m_tr_cell.m_ext[0] = ntracers;
+    m_tr_cell.m_ext[1] = mesh->m_ncells;
+    m_tr_cell.m_ext[2] = mesh->m_nlayers;
+  }
+  ShallowWaterState(const MPASMesh *mesh, const ShallowWaterParams &params)
+      : ShallowWaterState(mesh, params.m_ntracers) {}
+
+  swg_state handle() const { return m_handle.get(); }
+  // host round trips (reference users filled Views with parallel_for)
+  void upload(const std::vector<Real> &h, const std::vector<Real> &vn,
+              const std::vector<Real> &tr = {}) const {
+    swg_check(swg_state_upload(handle(), h.data(), vn.data(),
+                               tr.empty() ? nullptr : tr.data(), nullptr));
+    fence();
+  }
+  void download(std::vector<Real> &h, std::vector<Real> &vn,
+                std::vector<Real> &tr) const {
+    h.resize(m_h_cell.size());
+    vn.resize(m_vn_edge.size());
+    tr.resize(m_tr_cell.size());
+    swg_check(swg_state_download(handle(), h.data(), vn.data(),
+                                 tr.empty() ? nullptr : tr.data(), nullptr));
+  }
+};
+
+enum class AddMode { replace, increment };
+
+struct ShallowWaterModel {
+  ShallowWaterParams m_params;
+  MPASMesh *m_mesh;
+  swg_model m_handle = nullptr;
+
+  ShallowWaterModel(MPASMesh *mesh, const ShallowWaterParams &params)
+      : m_params(params), m_mesh(mesh) {
+    swg_params p{params.m_f0,         params.m_grav,       params.m_drag_coeff,
+                 params.m_visc_del2,  params.m_visc_del4,  params.m_eddy_diff2,
+                 params.m_eddy_diff4, params.m_ntracers,
+                 params.m_disable_h_tendency ? 1 : 0,
+                 params.m_disable_vn_tendency ? 1 : 0};
+    swg_check(swg_model_create(mesh->m_handle, &p, &m_handle));
+    // The hook stays registered until the base no-op runs once; then the
+    // steppers switch to the fused kernels (models that override
+    // additional_tendency keep the unfused, hooked sequence).
+    swg_check(swg_model_set_forcing(m_handle, &ShallowWaterModel::trampoline,
+                                    this));
+  }
+  ShallowWaterModel(const ShallowWaterModel &) = delete;
+  ShallowWaterModel &operator=(const ShallowWaterModel &) = delete;
+  virtual ~ShallowWaterModel() { swg_model_destroy(m_handle); }
+
+  // shallow_water_model.hpp:42-44
+  virtual void additional_tendency(Real2d h_tend_cell, Real2d vn_tend_edge,
+                                   RealConst2d h_cell, RealConst2d vn_edge,
+                                   Real t) const {
+    m_default_hook = true;
+  }
+
+  void compute_tendency(const ShallowWaterState &tend,
+                        const ShallowWaterState &state, Real t,
+                        AddMode add_mode = AddMode::replace) const {
+    swg_check(swg_compute_tendency(
+        m_handle, tend.handle(), state.handle(), t,
+        add_mode == AddMode::replace ? SWG_ADD_REPLACE : SWG_ADD_INCREMENT,
+        nullptr));
+  }
+
+private:
+  mutable bool m_default_hook = false;
+
+  static void trampoline(void *user, double *h_tend, double *vn_tend,
+                         const double *h, const double *vn, double t,
+                         void *) {
+    auto *self = static_cast<ShallowWaterModel *>(user);
+    const MPASMesh *m = self->m_mesh;
+    Real2d ht, vt;
+    RealConst2d hc, vc;
+    ht.m_data = h_tend;
+    vt.m_data = vn_tend;
+    hc.m_data = h;
+    vc.m_data = vn;
+    ht.m_ext[0] = hc.m_ext[0] = m->m_ncells;
+    vt.m_ext[0] = vc.m_ext[0] = m->m_nedges;
+    ht.m_ext[1] = hc.m_ext[1] = vt.m_ext[1] = vc.m_ext[1] = m->m_nlayers;
+    self->additional_tendency(ht, vt, hc, vc, t);
+    if (self->m_default_hook)
+      swg_model_set_forcing(self->m_handle, nullptr, nullptr);
+  }
+};
+
+// --------------------------------------------------------------- steppers --
+
+struct TimeStepper {
+  ShallowWaterModel *m_shallow_water;
+  swg_stepper m_handle = nullptr;
+  virtual void do_step(Real t, Real dt,
+                       const ShallowWaterState &state) const {
+    swg_check(swg_step(m_handle, state.handle(), t, dt, 1, 1, nullptr));
+  }
+  // nsteps consecutive do_step calls from t0 in one library call
+  void do_steps(Real t0, Real dt, const ShallowWaterState &state,
+                Int nsteps) const {
+    swg_check(swg_step(m_handle, state.handle(), t0, dt, nsteps, 1, nullptr));
+  }
+  TimeStepper(ShallowWaterModel &shallow_water, int kind, int nstages)
+      : m_shallow_water(&shallow_water) {
+    swg_check(swg_stepper_create(shallow_water.m_handle, kind, nstages,
+                                 &m_handle));
+  }
+  TimeStepper(const TimeStepper &) = delete;
+  TimeStepper &operator=(const TimeStepper &) = delete;
+  virtual ~TimeStepper() { swg_stepper_destroy(m_handle); }
+};
+
+struct LSRKStepper : TimeStepper {
+  Int m_nstages;
+  LSRKStepper(ShallowWaterModel &shallow_water, Int nstages = 5)
+      : TimeStepper(shallow_water, SWG_STEPPER_LSRK, nstages),
+        m_nstages(nstages) {}
+};
+
+struct RK4Stepper : TimeStepper {
+  static constexpr Int nstages = 4;
+  explicit RK4Stepper(ShallowWaterModel &shallow_water)
+      : TimeStepper(shallow_water, SWG_STEPPER_RK4, 4) {}
+};
+
+// ------------------------------------------------------------ diagnostics --
+
+inline Real energy_integral(const ShallowWaterState &state,
+                            const ShallowWaterModel &model) {
+  Real out;
+  swg_check(swg_diag_energy(model.m_handle, state.handle(), &out, nullptr));
+  return out;
+}
+inline Real mass_integral(const ShallowWaterState &state,
+                          const ShallowWaterModel &model) {
+  Real out;
+  swg_check(swg_diag_mass(model.m_handle, state.handle(), &out, nullptr));
+  return out;
+}
+inline Real circulation_integral(const ShallowWaterState &state,
+                                 const ShallowWaterModel &model) {
+  Real out;
+  swg_check(
+      swg_diag_circulation(model.m_handle, state.handle(), &out, nullptr));
+  return out;
+}
+
+} // namespace omega

@@ -1,0 +1,95 @@
+"""The reference's six CTest programs and its benchmark driver, re-hosted on
+the C++ drop-in classes (tests/cpp/*.cu over libswgpu.so), run on the GPU.
+
+Each program applies the reference test's own pass criterion (convergence
+rate within 0.05, conservation bounds) and exits non-zero otherwise.  In
+addition its error table must reproduce the one the reference printed
+(tests/golden/reference_tests.txt, 6 significant digits)."""
+import os
+import re
+import subprocess
+
+import pytest
+
+from helpers import GOLDEN
+from omega_playground_gb300 import _build
+
+pytestmark = pytest.mark.gpu
+
+BIN = os.path.join(_build.LIBDIR, "bin")
+
+
+def reference_tables():
+    txt = open(os.path.join(GOLDEN, "reference_tests.txt")).read()
+    out = {}
+    for block in txt.split("=== ")[1:]:
+        name, body = block.split("\n", 1)
+        out[name.strip()] = body
+    return out
+
+
+def errors(text, header):
+    """Error column of the table that follows `header`."""
+    lines = text.split(header, 1)[1].strip().splitlines()
+    vals = []
+    for ln in lines:
+        parts = ln.split()
+        if len(parts) < 2 or not parts[0].isdigit():
+            break
+        vals.append(float(parts[1]))
+    return vals
+
+
+def run(*args, timeout=600):
+    if not os.path.exists(os.path.join(BIN, args[0])):
+        _build.build_cpp_programs()
+    r = subprocess.run([os.path.join(BIN, args[0]), *args[1:]],
+                       capture_output=True, text=True, timeout=timeout)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return r.stdout
+
+
+@pytest.mark.parametrize("prog,args,ref,header", [
+    ("nonlinear_swe_convergence", [], "nonlinear_swe_convergence",
+     "Manufactured solution convergence"),
+    ("tracer_convergence", ["advection"], "tracer_advection_convergence",
+     "Tracer advection convergence"),
+    ("tracer_convergence", ["diffusion"], "tracer_diffusion_convergence",
+     "Tracer diffusion convergence"),
+    ("tracer_convergence", ["hyperdiffusion"],
+     "tracer_hyperdiffusion_convergence", "Tracer hyperdiffusion convergence"),
+])
+def test_convergence_matches_reference(prog, args, ref, header):
+    out = run(prog, *args)
+    got = errors(out, header)
+    want = errors(reference_tables()[ref], header)
+    assert len(got) == len(want) == 2
+    for g, w in zip(got, want):
+        assert abs(g - w) <= 5e-6 * abs(w), (got, want)
+
+
+def test_operator_convergence_matches_reference():
+    out = run("operator_convergence")
+    ref = reference_tables()["operator_convergence"]
+    for header in ("Gradient convergence", "Divergence convergence",
+                   "Curl convergence", "Reconstruction convergence"):
+        got, want = errors(out, header), errors(ref, header)
+        assert len(got) == len(want) == 5
+        for g, w in zip(got, want):
+            assert abs(g - w) <= 5e-6 * abs(w), (header, got, want)
+
+
+def test_double_vortex_conservation():
+    """Odd ny = 29 mesh (the reference's racy construction, reproduced in
+    its serial order); bounds from test/double_vortex.cpp:159-167."""
+    out = run("double_vortex")
+    vals = {k: float(v) for k, v in re.findall(r"(\w+) change: (\S+)", out)}
+    assert abs(vals["Mass"]) < 5e-14
+    assert abs(vals["Circulation"]) < 5e-14
+    assert abs(vals["Energy"]) < 1e-10
+
+
+def test_benchmark_driver_runs():
+    out = run("benchmark", "64", "16", "1", "4")
+    m = re.search(r"updates_per_s=(\S+)", out)
+    assert m and float(m.group(1)) > 0
