@@ -277,6 +277,19 @@ def run_ours(args, wl):
                 "stage": {"achieved": stage_bytes / (stage_ms / 1e3) / 1e9,
                           "alg_bytes": stage_bytes, "ms": stage_ms,
                           "frac": stage_bytes / (stage_ms / 1e3) / 1e9 / peak}}
+    # FP64 issue roof: GB300 issues 2 FP64 thread-instructions per SM per
+    # clock (ncu sm__sass_thread_inst_executed_op_dfma_pred_on.peak_sustained);
+    # instructions per cell-level of k_cell_final measured by ncu on the
+    # 256x256x64x8 case (DFMA 132 + DMUL 15 + DADD 8 = 155 with 8 tracers).
+    fp64 = None
+    if dom == "k_cell_final" and wl.ntracers == 8:
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = clk.get("sm_mhz") or 2070.0
+        peak_inst = 2.0 * sms * mhz * 1e6
+        got_inst = 155.0 * CK / (dom_ms / 1e3)
+        fp64 = {"bound": "fp64", "kernel": dom, "achieved": got_inst / 1e9,
+                "peak": peak_inst / 1e9, "unit": "G FP64 inst/s",
+                "frac": got_inst / peak_inst, "inst_per_cell_level": 155}
     kernels = {k: {"ms_per_launch": v[0] / v[1], "launches_per_step": v[1],
                    "share": v[0] / sum(x[0] for x in prof.values())}
                for k, v in prof.items()}
@@ -325,7 +338,7 @@ def run_ours(args, wl):
                        "l2": "state (%.2f GB) larger than L2; no flush"
                              % (8 * (wl.ncells * wl.nlayers * (4 + wl.ntracers))
                                 / 1e9)},
-            "roofline": roofline, "kernels": kernels,
+            "roofline": roofline, "fp64_roofline": fp64, "kernels": kernels,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk,
         }
