@@ -156,6 +156,29 @@ int swg_model_set_forcing(swg_model model, swg_forcing_fn fn, void *user);
 int swg_compute_tendency(swg_model model, swg_state tend, swg_state state,
                          double t, int add_mode, void *stream);
 
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory while they run (a host framework that owns the whole device pool,
+ * or code that must avoid the synchronisation an allocation brings): the
+ * same tendency as swg_compute_tendency (REPLACE or INCREMENT into the
+ * caller's arrays, no additional_tendency hook), with the parameter tables
+ * and all intermediate fields kept in one static device array of
+ * SWG_NOALLOC_SCRATCH_BYTES (64 MiB) compiled into the library instead of
+ * model-owned buffers.  Inputs h [C][K], vn [E][K], tr [T][C][K] and outputs
+ * h_tend, vn_tend, tr_tend are device pointers; tr/tr_tend may be NULL when
+ * params->ntracers == 0.  It calls no cudaMalloc/cudaFree or other
+ * allocating routine.  Meshes and parameter sets whose scratch exceeds the
+ * maximum are rejected with SWG_ERR_ARG (64x64 cells x 64 levels with one
+ * tracer and del2 viscosity fits).  The first call on each device looks up
+ * the array's address with that device current; make that first call before
+ * any stream capture.  All calls share the array: calls that overlap on the
+ * GPU (unordered streams) race on it. */
+#define SWG_NOALLOC_SCRATCH_BYTES (64ull << 20)
+int swg_compute_tendency_noalloc(swg_mesh mesh, const swg_params *params,
+                                 const double *h, const double *vn,
+                                 const double *tr, double *h_tend,
+                                 double *vn_tend, double *tr_tend,
+                                 int add_mode, void *stream);
+
 /* Named auxiliary field of the last tendency evaluation, device pointer and
  * element count.  Names: "q_vertex" ((rvort+f)/h at vertices), "rvort_vertex",
  * "vel_div_cell", "ke_cell", "norm_tr_cell", "thick_flux_edge"

@@ -101,6 +101,9 @@ _SIGS = {
     "swg_model_set_forcing": (C.c_int, [_vp, FORCING_FN, _vp]),
     "swg_compute_tendency": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int,
                                        _vp]),
+    "swg_compute_tendency_noalloc": (C.c_int, [_vp, C.POINTER(Params), _vp,
+                                               _vp, _vp, _vp, _vp, _vp,
+                                               C.c_int, _vp]),
     "swg_model_aux": (C.c_int, [_vp, C.c_char_p, C.POINTER(_dp),
                                 C.POINTER(C.c_longlong)]),
     "swg_stepper_create": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(_vp)]),

@@ -1,0 +1,197 @@
+// Tendency evaluation that allocates nothing (swg_compute_tendency_noalloc).
+//
+// Some callers cannot allocate device memory while they run: a host
+// framework that owns the whole device pool and forbids libraries from
+// calling cudaMalloc after start-up, or code that must not trigger the
+// implicit synchronisation an allocation can cause.  swg_model_create
+// allocates the parameter tables and the intermediate fields of a tendency
+// evaluation, so it is out of reach for them.  This entry point instead
+// keeps both in one fixed device array compiled into the library, and takes
+// the state and tendency arrays as device pointers from the caller.
+//
+// The array holds SWG_NOALLOC_SCRATCH_BYTES (64 MiB); every GPU that loads
+// the library holds it until the process exits.  Its device address is
+// looked up with cudaGetSymbolAddress on the first call on each device (with
+// that device current) and cached; in host code the array's name is only a
+// host-side stand-in, never a device address.  All calls share the array:
+// each call rewrites every scratch element it later reads, so nothing has to
+// start at zero, but calls that overlap on the GPU (different streams, no
+// ordering between them) race on it.
+#include "swg_internal.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+
+namespace swg {
+namespace {
+
+constexpr size_t kScratchBytes = size_t(64) << 20;
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+std::atomic<unsigned char *> g_scratch_addr[kMaxDevices];
+
+// Parameter-scaled tables of a model, the same expressions swg_model_create
+// evaluates on the host (shallow_water_model.cpp:5-41 enables the terms).
+__global__ void k_noalloc_tables(MeshView m, double f0, double grav,
+                                 double visc2, double visc4, double kappa2,
+                                 double kappa4, double *f_vertex, double *gidc,
+                                 double *c2e, double *c4e, double *kd2,
+                                 double *r4, double *r4sum) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < m.nvertices)
+    f_vertex[i] = f0;
+  if (i < m.nedges) {
+    gidc[i] = grav * m.inv_dc[i];
+    c2e[i] = visc2 * m.scale2[i];
+    c4e[i] = -(visc4 * m.scale4[i]);
+  }
+  if (i < m.ncells) {
+    double s = 0;
+    for (int j = 0; j < MAXE; ++j) {
+      const int e = m.ec[6 * i + j];
+      kd2[6 * i + j] = kappa2 * m.scale2[e] * m.ckq[6 * i + j];
+      const double r = -(kappa4 * m.scale4[e] * m.ckq[6 * i + j]);
+      r4[6 * i + j] = r;
+      s += r;
+    }
+    r4sum[i] = s;
+  }
+}
+
+// Bump allocator over the scratch array: offsets only, 256-byte aligned.
+struct Carve {
+  unsigned char *base;
+  size_t used = 0;
+  double *take(size_t words) {
+    used = (used + 255) & ~size_t(255);
+    double *p = base ? reinterpret_cast<double *>(base + used) : nullptr;
+    used += words * sizeof(double);
+    return p;
+  }
+};
+
+// Lays out the model tables and the intermediates the enabled terms need;
+// with base == nullptr it only measures.
+size_t layout(const swg_mesh_s *mesh, const ModelView &pv, unsigned char *base,
+              double *tab[7], AuxView &a) {
+  const size_t C = mesh->ncells, E = mesh->nedges, V = mesh->nvertices,
+               K = mesh->nlayers, T = pv.ntracers;
+  Carve cv{base};
+  tab[0] = cv.take(V);     // f_vertex
+  tab[1] = cv.take(E);     // gidc
+  tab[2] = cv.take(E);     // c2e
+  tab[3] = cv.take(E);     // c4e
+  tab[4] = cv.take(6 * C); // kd2
+  tab[5] = cv.take(6 * C); // r4
+  tab[6] = cv.take(C);     // r4sum
+  const bool vn = pv.do_vn;
+  const bool vdiss = vn && (pv.vel_del2 || pv.vel_del4);
+  const bool v4 = vn && pv.vel_del4;
+  const bool trd = T > 0 && (pv.tr_del2 || pv.tr_del4);
+  a = AuxView{};
+  if (vn) a.q = cv.take(V * K);
+  if (vdiss) a.zeta = cv.take(V * K);
+  if (v4) a.z4 = cv.take(V * K);
+  if (vdiss) a.div = cv.take(C * K);
+  if (vn) a.ke = cv.take(C * K);
+  if (v4) a.d4 = cv.take(C * K);
+  if (T > 0) a.ntr = cv.take(T * C * K);
+  if (T > 0 && pv.tr_del4) a.lap = cv.take(T * C * K);
+  a.F = cv.take(E * K);
+  if (vn) a.G = cv.take(E * K);
+  if (vn) a.Q = cv.take(E * K);
+  if (trd) a.mh = cv.take(E * K);
+  if (vn) a.u2 = cv.take(E * K);
+  if (vdiss) a.d2u = cv.take(E * K);
+  a.d2u4 = (v4 && mesh->view.dv4_differs) ? cv.take(E * K) : a.d2u;
+  return cv.used;
+}
+
+} // namespace
+} // namespace swg
+
+using namespace swg;
+
+extern "C" int swg_compute_tendency_noalloc(swg_mesh mesh,
+                                            const swg_params *params,
+                                            const double *h, const double *vn,
+                                            const double *tr, double *h_tend,
+                                            double *vn_tend, double *tr_tend,
+                                            int add_mode, void *stream) {
+  if (!mesh || !params || !h || !vn || !h_tend || !vn_tend ||
+      params->ntracers < 0 || (params->ntracers > 0 && (!tr || !tr_tend)))
+    return fail(SWG_ERR_ARG, "swg_compute_tendency_noalloc: bad argument");
+  if (add_mode != SWG_ADD_REPLACE && add_mode != SWG_ADD_INCREMENT)
+    return fail(SWG_ERR_ARG, "swg_compute_tendency_noalloc: bad add_mode");
+  ModelView pv{};
+  pv.grav = params->grav;
+  pv.ntracers = params->ntracers;
+  pv.vel_del2 = params->visc_del2 > 0;
+  pv.vel_del4 = params->visc_del4 > 0;
+  pv.tr_del2 = params->eddy_diff2 > 0;
+  pv.tr_del4 = params->eddy_diff4 > 0;
+  pv.do_h = !params->disable_h_tendency;
+  pv.do_vn = !params->disable_vn_tendency;
+  double *tab[7];
+  AuxView a;
+  const size_t need = layout(mesh, pv, nullptr, tab, a);
+  if (need > kScratchBytes) {
+    char msg[200];
+    std::snprintf(msg, sizeof msg,
+                  "swg_compute_tendency_noalloc: this mesh and parameter set "
+                  "need %zu bytes of scratch; the static maximum is %zu bytes "
+                  "(64 MiB)", need, kScratchBytes);
+    return fail(SWG_ERR_ARG, msg);
+  }
+  // once per device: the array's device address, with that device current
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess)
+    return cuda_fail(err, "swg_compute_tendency_noalloc: cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices)
+    return fail(SWG_ERR_ARG, "swg_compute_tendency_noalloc: device ordinal "
+                             "above 63");
+  unsigned char *base = g_scratch_addr[dev].load();
+  if (!base) {
+    void *ptr = nullptr;
+    err = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (err != cudaSuccess || !ptr)
+      return cuda_fail(err != cudaSuccess ? err : cudaErrorInvalidSymbol,
+                       "swg_compute_tendency_noalloc: cudaGetSymbolAddress");
+    base = static_cast<unsigned char *>(ptr);
+    g_scratch_addr[dev].store(base);
+  }
+  layout(mesh, pv, base, tab, a);
+  pv.f_vertex = tab[0];
+  pv.gidc = tab[1];
+  pv.c2e = tab[2];
+  pv.c4e = tab[3];
+  pv.kd2 = tab[4];
+  pv.r4 = tab[5];
+  pv.r4sum = tab[6];
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const MeshView &m = mesh->view;
+  const long long n = std::max<long long>(
+      std::max<long long>(m.nvertices, m.nedges), m.ncells);
+  k_noalloc_tables<<<unsigned((n + 255) / 256), 256, 0, st>>>(
+      m, params->f0, params->grav, params->visc_del2, params->visc_del4,
+      params->eddy_diff2, params->eddy_diff4, tab[0], tab[1], tab[2], tab[3],
+      tab[4], tab[5], tab[6]);
+  ++g_launches;
+  StageArgs s{};
+  s.h = h;
+  s.vn = vn;
+  s.tr = tr;
+  s.fh.tend = h_tend;
+  s.fvn.tend = vn_tend;
+  s.ftr.tend = tr_tend;
+  s.ep.mode = add_mode == SWG_ADD_REPLACE ? EPI_REPLACE : EPI_INCREMENT;
+  launch_tendency(m, pv, a, s, st);
+  err = cudaGetLastError();
+  return err == cudaSuccess
+             ? SWG_OK
+             : cuda_fail(err, "swg_compute_tendency_noalloc: launch");
+}

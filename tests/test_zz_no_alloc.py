@@ -1,0 +1,116 @@
+"""swg_compute_tendency_noalloc: the tendency entry point for callers that
+cannot allocate device memory while they run.  It keeps its parameter tables
+and intermediate fields in a static 64 MiB device array instead of
+model-owned buffers, so here it is checked through the C ABI against the
+allocating entry point, swg_compute_tendency, on two calls in a row (the
+second reuses the array the first one wrote), and its size limit is checked.
+
+This file is named to be collected last so that a run stopping at its first
+failure has already run every other test."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import omega_playground_gb300 as og
+from helpers import load_golden, rel_diff
+from omega_playground_gb300 import _capi
+from omega_playground_gb300.workloads import WORKLOADS, initial_state
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def _setup(cfg):
+    mesh = og.PlanarHexagonalMesh(cfg["nx"], cfg["ny"], cfg["dc"], cfg["K"])
+    params = og.ShallowWaterParams(
+        m_f0=cfg["f0"], m_grav=cfg["grav"], m_visc_del2=cfg["visc_del2"],
+        m_visc_del4=cfg["visc_del4"], m_eddy_diff2=cfg["eddy_diff2"],
+        m_eddy_diff4=cfg["eddy_diff4"], m_ntracers=cfg["T"],
+        m_disable_h_tendency=cfg.get("disable_h", False),
+        m_disable_vn_tendency=cfg.get("disable_vn", False))
+    return mesh, params
+
+
+def _noalloc(mesh, params, state, tend, add_mode=0):
+    h, vn, tr = state.device_ptrs()
+    th, tv, tt = tend.device_ptrs()
+    p = params._c()
+    T = params.m_ntracers
+    rc = _capi.lib().swg_compute_tendency_noalloc(
+        mesh.handle, C.byref(p), C.c_void_p(h), C.c_void_p(vn),
+        C.c_void_p(tr) if T else None, C.c_void_p(th), C.c_void_p(tv),
+        C.c_void_p(tt) if T else None, add_mode, None)
+    return rc
+
+
+def _allocating(mesh, params, state):
+    model = og.ShallowWaterModel(mesh, params)
+    tend = og.ShallowWaterState(mesh, params)
+    model.compute_tendency(tend, state, 0.0)
+    return tend.download()
+
+
+def test_noalloc_matches_compute_tendency_two_calls():
+    # call 1: every term on, two tracers (golden inputs)
+    g = load_golden("rk4_all_terms")
+    cfg = g["cfg"]
+    mesh1, params1 = _setup(cfg)
+    s1 = og.ShallowWaterState(mesh1, params1)
+    s1.upload(g["in_h"], g["in_vn"], g["in_tr"])
+    # call 2: a different mesh, parameter set and state (three tracers,
+    # velocity noise), so the second call reuses the array differently
+    wl = WORKLOADS["lsrk5_512x512"].scaled(nx=24, ny=20, nlayers=37,
+                                           ntracers=3)
+    cfg2 = dict(nx=wl.nx, ny=wl.ny, dc=wl.dc, K=wl.nlayers, T=wl.ntracers,
+                f0=wl.f0, grav=wl.grav, visc_del2=wl.visc_del2,
+                visc_del4=wl.visc_del4, eddy_diff2=wl.eddy_diff2,
+                eddy_diff4=wl.eddy_diff4)
+    mesh2, params2 = _setup(cfg2)
+    s2 = og.ShallowWaterState(mesh2, params2)
+    s2.upload(*initial_state(mesh2, wl))
+
+    results = []
+    for mesh, params, state in ((mesh1, params1, s1), (mesh2, params2, s2)):
+        tend = og.ShallowWaterState(mesh, params)
+        assert _noalloc(mesh, params, state, tend) == 0, \
+            _capi.lib().swg_last_error()
+        results.append((tend.download(), mesh, params, state))
+    og.sync()
+    for got, mesh, params, state in results:
+        ref = _allocating(mesh, params, state)
+        for a, b in zip(got, ref):
+            assert rel_diff(a, b) <= TOL
+    # and the golden tendency itself
+    (th, tv, tt) = results[0][0]
+    assert rel_diff(th, g["tend_h"]) <= TOL
+    assert rel_diff(tv, g["tend_vn"]) <= TOL
+    assert rel_diff(tt, g["tend_tr"]) <= TOL
+
+
+def test_noalloc_increment_and_size_limit():
+    g = load_golden("lsrk5_all_terms")
+    cfg = g["cfg"]
+    mesh, params = _setup(cfg)
+    state = og.ShallowWaterState(mesh, params)
+    state.upload(g["in_h"], g["in_vn"], g["in_tr"])
+    tend = og.ShallowWaterState(mesh, params)
+    assert _noalloc(mesh, params, state, tend, 0) == 0
+    assert _noalloc(mesh, params, state, tend, 1) == 0
+    th, tv, tt = tend.download()
+    assert rel_diff(th, 2 * g["tend_h"]) <= TOL
+    assert rel_diff(tv, 2 * g["tend_vn"]) <= TOL
+    assert rel_diff(tt, 2 * g["tend_tr"]) <= TOL
+    # 128x128 cells x 64 levels x 8 tracers needs far more than 64 MiB
+    big = dict(nx=128, ny=128, dc=1e4, K=64, T=8, f0=1e-4, grav=9.81,
+               visc_del2=1e3, visc_del4=1e9, eddy_diff2=1e3, eddy_diff4=1e9)
+    mesh_b, params_b = _setup(big)
+    sb = og.ShallowWaterState(mesh_b, params_b)
+    tb = og.ShallowWaterState(mesh_b, params_b)
+    rc = _noalloc(mesh_b, params_b, sb, tb)
+    assert rc == 1
+    msg = _capi.lib().swg_last_error().decode()
+    assert "static maximum" in msg and "64 MiB" in msg
+    h, vn, tr = tb.download()
+    assert not h.any() and not vn.any() and not tr.any()
