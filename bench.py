@@ -347,8 +347,84 @@ def run_ours(args, wl):
         torch.distributed.destroy_process_group()
 
 
+def run_ensemble(args):
+    """The batched ensemble: 64 members (nx from {32..192}, 16-96 levels,
+    1-4 tracers, RK4) advanced by one persistent kernel per stage, against
+    the same members advanced one at a time by the single-instance path."""
+    import torch
+    import omega_playground_gb300 as og
+    from omega_playground_gb300.workloads import ensemble, initial_state
+    torch.cuda.set_device(0)
+    wls = ensemble(n=64)
+    members, states = [], []
+    for wl in wls:
+        mesh = og.PlanarHexagonalMesh(wl.nx, wl.ny, wl.dc, wl.nlayers)
+        params = wl.params()
+        model = og.ShallowWaterModel(mesh, params)
+        st = og.ShallowWaterState(mesh, params)
+        ic = initial_state(mesh, wl)
+        st.upload(*ic)
+        members.append((mesh, params, model, ic))
+        states.append(st)
+    units_step = sum(w.ncells * w.nlayers * 4 for w in wls)
+    dt = wls[0].dt
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    batch = og.Batch([m[2] for m in members], states, "rk4", 4)
+    cfg, tune_ms = batch.autotune(dt, reps=2, stream=sh)
+    for st, m in zip(states, members):
+        st.upload(*m[3])
+    batch.step(0.0, dt, args.warmup, stream=sh)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    l0 = og.kernel_launches()
+    e0.record(stream)
+    batch.step(0.0, dt, args.steps, stream=sh, check_status=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batch.check(sh)
+    ms = e0.elapsed_time(e1)
+    launches = og.kernel_launches() - l0
+    value = units_step * args.steps / (ms / 1e3)
+    # the same members one at a time (single-instance fused path, graph)
+    single_ms = 0.0
+    for (mesh, params, model, ic), st in zip(members, states):
+        stp = og.RK4Stepper(model)
+        stp.step(st, 0.0, dt, 1, stream=sh)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        stp.step(st, 0.0, dt, args.steps, stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        single_ms += e0.elapsed_time(e1)
+    single = units_step * args.steps / (single_ms / 1e3)
+    big = max(range(len(wls)), key=lambda i: wls[i].ncells * wls[i].nlayers)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "ensemble64", "members": len(wls),
+                       "cell_levels": units_step // 4,
+                       "nx": sorted({w.nx for w in wls}),
+                       "levels": [min(w.nlayers for w in wls),
+                                  max(w.nlayers for w in wls)],
+                       "tracers": [min(w.ntracers for w in wls),
+                                   max(w.ntracers for w in wls)],
+                       "stepper": "rk4", "launch_config": cfg,
+                       "largest_member": wls[big].name},
+            "single_instance_sequential": {"value": single,
+                                           "ms_per_step": single_ms / args.steps},
+            "batch_over_single": value / single, "gpu_launches": launches}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "ensemble64":
+        run_ensemble(args)
+        return
     from omega_playground_gb300.workloads import WORKLOADS
     wl = WORKLOADS[args.workload]
     if args.nx:

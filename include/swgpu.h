@@ -47,6 +47,7 @@ typedef struct swg_mesh_s *swg_mesh;
 typedef struct swg_state_s *swg_state;
 typedef struct swg_model_s *swg_model;
 typedef struct swg_stepper_s *swg_stepper;
+typedef struct swg_batch_s *swg_batch;
 
 /* Message of the calling thread's last failed call ("" if none). */
 const char *swg_last_error(void);
@@ -200,6 +201,38 @@ int swg_stepper_destroy(swg_stepper stepper);
  * CUDA graph of one step (ignored when a forcing hook is set). */
 int swg_step(swg_stepper stepper, swg_state state, double t0, double dt,
              int nsteps, int use_graph, void *stream);
+
+/* ----------------------------------------------------------- batches -----
+ * Ensembles of independent members with uneven mesh size, level count and
+ * tracer count, advanced together (no counterpart in the reference, which
+ * runs one instance per process; each member's step is the reference's
+ * do_step).  Members are (model, state) pairs whose models have no forcing
+ * hook and share the edges-on-edge width; the batch owns the stepper scratch
+ * of every member.  One RK stage of all members is one persistent
+ * cooperative kernel (six passes separated by bounded grid barriers), or one
+ * launch per pass, whichever launch configuration is selected. */
+int swg_batch_create(int nmembers, const swg_model *models,
+                     const swg_state *states, int kind, int nstages,
+                     swg_batch *out);
+int swg_batch_destroy(swg_batch batch);
+/* nsteps steps of every member (dt shared), asynchronous on `stream`;
+ * use_graph != 0 replays a CUDA graph of one step. */
+int swg_batch_step(swg_batch batch, double t0, double dt, int nsteps,
+                   int use_graph, void *stream);
+/* Synchronises `stream` and reports SWG_ERR_TIMEOUT if a grid-barrier wait
+ * expired since the last check (the kernel then returned early). */
+int swg_batch_check(swg_batch batch, void *stream);
+/* Launch configurations: count, explicit choice, and autotuning (times
+ * `reps` steps of every configuration on the batch itself and keeps the
+ * fastest; the timed steps advance the members). */
+int swg_batch_config_count(void);
+int swg_batch_set_config(swg_batch batch, int config);
+int swg_batch_autotune(swg_batch batch, double dt, int reps, void *stream,
+                       int *best, double *best_ms_per_step);
+/* Failure-detection test: launches a wait that nothing releases with a
+ * limit of limit_ms (<= 2000) and returns the resulting SWG_ERR_TIMEOUT. */
+int swg_batch_selftest_timeout(swg_batch batch, double limit_ms,
+                               void *stream);
 
 /* ------------------------------------------------------- diagnostics -----
  * replaces energy_integral / mass_integral / circulation_integral

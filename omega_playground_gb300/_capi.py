@@ -110,6 +110,17 @@ _SIGS = {
     "swg_stepper_destroy": (C.c_int, [_vp]),
     "swg_step": (C.c_int, [_vp, _vp, C.c_double, C.c_double, C.c_int,
                            C.c_int, _vp]),
+    "swg_batch_create": (C.c_int, [C.c_int, C.POINTER(_vp), C.POINTER(_vp),
+                                   C.c_int, C.c_int, C.POINTER(_vp)]),
+    "swg_batch_destroy": (C.c_int, [_vp]),
+    "swg_batch_step": (C.c_int, [_vp, C.c_double, C.c_double, C.c_int,
+                                 C.c_int, _vp]),
+    "swg_batch_check": (C.c_int, [_vp, _vp]),
+    "swg_batch_config_count": (C.c_int, []),
+    "swg_batch_set_config": (C.c_int, [_vp, C.c_int]),
+    "swg_batch_autotune": (C.c_int, [_vp, C.c_double, C.c_int, _vp,
+                                     C.POINTER(C.c_int), _dp]),
+    "swg_batch_selftest_timeout": (C.c_int, [_vp, C.c_double, _vp]),
     "swg_diag_mass": (C.c_int, [_vp, _vp, _dp, _vp]),
     "swg_diag_energy": (C.c_int, [_vp, _vp, _dp, _vp]),
     "swg_diag_circulation": (C.c_int, [_vp, _vp, _dp, _vp]),

@@ -1,0 +1,314 @@
+// Per-element passes of one tendency evaluation + stage update, shared by
+// the single-instance kernels (swg_kernels.cu) and the batched persistent
+// kernel (swg_batch.cu).  Each function handles one flat index i of its pass
+// domain: (entity, level) with the level fastest.  Callers guarantee i is in
+// range (pt_aux2: i < (V + C) K, vertices first).
+#pragma once
+
+#include "swg_internal.h"
+
+namespace swg {
+
+// 1/x: hardware estimate refined by two Newton-Raphson steps
+// r <- r + r (1 - x r); each step squares the relative error of the estimate.
+__device__ __forceinline__ double rcp_nr(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+}
+
+__device__ __forceinline__ void epilogue(const Epilogue &ep, const FieldIO &f,
+                                         size_t i, double x) {
+  switch (ep.mode) {
+  case EPI_REPLACE:
+    f.tend[i] = x;
+    break;
+  case EPI_INCREMENT:
+    f.tend[i] += x;
+    break;
+  case EPI_LSRK: {
+    const double t = fma(ep.a, f.tend[i], x);
+    f.tend[i] = t;
+    f.out[i] = fma(ep.dtb, t, f.out[i]);
+  } break;
+  case EPI_RK4_FIRST: {
+    const double s = f.old[i];
+    f.acc[i] = fma(ep.dtb, x, s);
+    f.out[i] = fma(ep.dta, x, s);
+  } break;
+  case EPI_RK4_MID:
+    f.acc[i] = fma(ep.dtb, x, f.acc[i]);
+    f.out[i] = fma(ep.dta, x, f.old[i]);
+    break;
+  default: // EPI_RK4_LAST
+    f.out[i] = fma(ep.dtb, x, f.acc[i]);
+    break;
+  }
+}
+
+// Vertex pass: relative vorticity and (rvort + f) / h_vertex.
+__device__ __forceinline__ void
+pt_vertex(const MeshView &m, const ModelView &p, const AuxView &a,
+          const double *__restrict__ h, const double *__restrict__ vn,
+          unsigned i) {
+  const int K = m.nlayers;
+  const int v = int(i / unsigned(K)), k = int(i - unsigned(v) * unsigned(K));
+  double z, hv;
+  {
+    const int e = __ldg(m.ev + 3 * v), c = __ldg(m.cv + 3 * v);
+    z = __ldg(m.cvr + 3 * v) * vn[size_t(e) * K + k];
+    hv = __ldg(m.kvh + 3 * v) * h[size_t(c) * K + k];
+  }
+#pragma unroll
+  for (int j = 1; j < 3; ++j) {
+    const int e = __ldg(m.ev + 3 * v + j), c = __ldg(m.cv + 3 * v + j);
+    z = fma(__ldg(m.cvr + 3 * v + j), vn[size_t(e) * K + k], z);
+    hv = fma(__ldg(m.kvh + 3 * v + j), h[size_t(c) * K + k], hv);
+  }
+  a.q[i] = (z + __ldg(p.f_vertex + v)) * rcp_nr(hv);
+  if (p.vel_del2 | p.vel_del4)
+    a.zeta[i] = z;
+}
+
+// Cell pass 1: velocity divergence (for the dissipation terms) and the
+// normalised tracers tr / h.
+__device__ __forceinline__ void
+pt_cell1(const MeshView &m, const ModelView &p, const AuxView &a,
+         const double *__restrict__ h, const double *__restrict__ vn,
+         const double *__restrict__ tr, unsigned i) {
+  const int K = m.nlayers;
+  const unsigned CK = unsigned(m.ncells) * unsigned(K);
+  const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * unsigned(K));
+  if (p.do_vn && (p.vel_del2 | p.vel_del4)) {
+    double dv = __ldg(m.ccd + 6 * c) * vn[size_t(__ldg(m.ec + 6 * c)) * K + k];
+#pragma unroll
+    for (int j = 1; j < MAXE; ++j)
+      dv = fma(__ldg(m.ccd + 6 * c + j),
+               vn[size_t(__ldg(m.ec + 6 * c + j)) * K + k], dv);
+    a.div[i] = dv;
+  }
+  if (p.ntracers > 0) {
+    const double r = rcp_nr(h[i]);
+    for (int l = 0; l < p.ntracers; ++l) {
+      const size_t t = size_t(l) * CK + i;
+      a.ntr[t] = tr[t] * r;
+    }
+  }
+}
+
+// Edge pass 1: mean thickness, thickness flux F = mean_h vn, vn^2, edge PV
+// sum Q = q(v0) + q(v1), G = F Q, and the edge Laplacian of the velocity.
+__device__ __forceinline__ void
+pt_edge1(const MeshView &m, const ModelView &p, const AuxView &a,
+         const double *__restrict__ h, const double *__restrict__ vn,
+         unsigned i) {
+  const int K = m.nlayers;
+  const int e = int(i / unsigned(K)), k = int(i - unsigned(e) * unsigned(K));
+  const int c0 = __ldg(m.ce + 2 * e), c1 = __ldg(m.ce + 2 * e + 1);
+  const double mh = 0.5 * (h[size_t(c0) * K + k] + h[size_t(c1) * K + k]);
+  const double u = vn[i];
+  const double F = mh * u;
+  a.F[i] = F;
+  if (p.ntracers > 0 && (p.tr_del2 | p.tr_del4))
+    a.mh[i] = mh;
+  if (p.do_vn) {
+    const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
+    const double Q = a.q[size_t(v0) * K + k] + a.q[size_t(v1) * K + k];
+    a.Q[i] = Q;
+    a.G[i] = F * Q;
+    a.u2[i] = u * u;
+    if (p.vel_del2 | p.vel_del4) {
+      const double dd = a.div[size_t(c1) * K + k] - a.div[size_t(c0) * K + k];
+      const double dz = a.zeta[size_t(v1) * K + k] - a.zeta[size_t(v0) * K + k];
+      const double idc = __ldg(m.inv_dc + e);
+      a.d2u[i] = fma(dd, idc, -(dz * __ldg(m.inv_dv + e)));
+      if (p.vel_del4 && m.dv4_differs)
+        a.d2u4[i] = fma(dd, idc, -(dz * __ldg(m.inv_dv4 + e)));
+    }
+  }
+}
+
+// Second auxiliary pass: kinetic energy (cells), curl (vertices) and
+// divergence (cells) of the edge Laplacian, and the thickness-weighted
+// tracer Laplacian L (cells).  The first V*K threads take vertices, the
+// rest cells.
+__device__ __forceinline__ void pt_aux2(const MeshView &m, const ModelView &p,
+                                        const AuxView &a, unsigned i) {
+  const int K = m.nlayers;
+  const unsigned VK = unsigned(m.nvertices) * unsigned(K);
+  const unsigned CK = unsigned(m.ncells) * unsigned(K);
+  const bool vel = p.do_vn && p.vel_del4;
+  if (i < VK) {
+    if (!vel)
+      return;
+    const int v = int(i / unsigned(K)), k = int(i - unsigned(v) * unsigned(K));
+    double z = __ldg(m.cvr + 3 * v) * a.d2u4[size_t(__ldg(m.ev + 3 * v)) * K + k];
+#pragma unroll
+    for (int j = 1; j < 3; ++j)
+      z = fma(__ldg(m.cvr + 3 * v + j),
+              a.d2u4[size_t(__ldg(m.ev + 3 * v + j)) * K + k], z);
+    a.z4[i] = z;
+    return;
+  }
+  i -= VK;
+  if (i >= CK)
+    return;
+  const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * unsigned(K));
+  if (p.do_vn) {
+    // ke = sum_j dv dc / (4 area) vn_j^2
+    double ke = __ldg(m.cke + 6 * c) * a.u2[size_t(__ldg(m.ec + 6 * c)) * K + k];
+#pragma unroll
+    for (int j = 1; j < MAXE; ++j)
+      ke = fma(__ldg(m.cke + 6 * c + j),
+               a.u2[size_t(__ldg(m.ec + 6 * c + j)) * K + k], ke);
+    a.ke[i] = ke;
+  }
+  if (vel) {
+    double d = __ldg(m.ccd + 6 * c) * a.d2u4[size_t(__ldg(m.ec + 6 * c)) * K + k];
+#pragma unroll
+    for (int j = 1; j < MAXE; ++j)
+      d = fma(__ldg(m.ccd + 6 * c + j),
+              a.d2u4[size_t(__ldg(m.ec + 6 * c + j)) * K + k], d);
+    a.d4[i] = d;
+  }
+  if (p.ntracers > 0 && p.tr_del4) {
+    // L = sum_j w_j (n_nb - n_c), w_j = ckq_j mean_h_j
+    double w[MAXE], M;
+    int nb[MAXE];
+#pragma unroll
+    for (int j = 0; j < MAXE; ++j) {
+      w[j] = __ldg(m.ckq + 6 * c + j) * a.mh[size_t(__ldg(m.ec + 6 * c + j)) * K + k];
+      nb[j] = __ldg(m.nbc + 6 * c + j);
+    }
+    M = w[0] + w[1];
+#pragma unroll
+    for (int j = 2; j < MAXE; ++j)
+      M += w[j];
+    for (int l = 0; l < p.ntracers; ++l) {
+      const double *n = a.ntr + size_t(l) * CK;
+      double acc = w[0] * n[size_t(nb[0]) * K + k];
+#pragma unroll
+      for (int j = 1; j < MAXE; ++j)
+        acc = fma(w[j], n[size_t(nb[j]) * K + k], acc);
+      a.lap[size_t(l) * CK + i] = fma(-M, n[i], acc);
+    }
+  }
+}
+
+// Edge final pass: normal-velocity tendency (PV flux, Bernoulli gradient,
+// del2 and del4 dissipation) and its stage update.
+template <int NE>
+__device__ __forceinline__ void pt_edge_final(const MeshView &m,
+                                              const ModelView &p,
+                                              const AuxView &a,
+                                              const StageArgs &s, unsigned i) {
+  const int K = m.nlayers;
+  const int e = int(i / unsigned(K)), k = int(i - unsigned(e) * unsigned(K));
+  // potential-vorticity flux: sum_j w_j F_j (Q_e + Q_j) / 4 with w/4 in woe
+  double S1, S2;
+  {
+    const int je = __ldg(m.eoe + NE * e);
+    const double w = __ldg(m.woe + NE * e);
+    S1 = w * a.F[size_t(je) * K + k];
+    S2 = w * a.G[size_t(je) * K + k];
+  }
+#pragma unroll
+  for (int j = 1; j < NE; ++j) {
+    const int je = __ldg(m.eoe + NE * e + j);
+    const double w = __ldg(m.woe + NE * e + j);
+    S1 = fma(w, a.F[size_t(je) * K + k], S1);
+    S2 = fma(w, a.G[size_t(je) * K + k], S2);
+  }
+  double t = fma(a.Q[i], S1, S2);
+  const int c0 = __ldg(m.ce + 2 * e), c1 = __ldg(m.ce + 2 * e + 1);
+  const double idc = __ldg(m.inv_dc + e);
+  // kinetic-energy and sea-surface-height gradients (the differences are
+  // taken before scaling, as in the reference, so g h ~ 1e4 never rounds)
+  t = fma(-idc, a.ke[size_t(c1) * K + k] - a.ke[size_t(c0) * K + k], t);
+  t = fma(-__ldg(p.gidc + e), s.h[size_t(c1) * K + k] - s.h[size_t(c0) * K + k],
+          t);
+  const double mk = m.mask ? m.mask[i] : 1.0;
+  if (p.vel_del2)
+    t = fma(m.mask ? __ldg(p.c2e + e) * mk : __ldg(p.c2e + e), a.d2u[i], t);
+  if (p.vel_del4) {
+    const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
+    const double dd = a.d4[size_t(c1) * K + k] - a.d4[size_t(c0) * K + k];
+    const double dz = a.z4[size_t(v1) * K + k] - a.z4[size_t(v0) * K + k];
+    const double l = fma(dd, idc, -(dz * __ldg(m.inv_dv + e)));
+    t = fma(m.mask ? __ldg(p.c4e + e) * mk : __ldg(p.c4e + e), l, t);
+  }
+  epilogue(s.ep, s.fvn, i, t);
+}
+
+// Cell final pass: thickness tendency and tracer tendencies (advection,
+// del2, del4) with their stage updates.
+__device__ __forceinline__ void pt_cell_final(const MeshView &m,
+                                              const ModelView &p,
+                                              const AuxView &a,
+                                              const StageArgs &s,
+                                              unsigned i) {
+  const int K = m.nlayers;
+  const unsigned CK = unsigned(m.ncells) * unsigned(K);
+  const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * unsigned(K));
+  // a_j = -F_j ccd_j / 2: half the flux divergence weight of edge j
+  double w[MAXE], Sa;
+  int ej[MAXE];
+#pragma unroll
+  for (int j = 0; j < MAXE; ++j) {
+    ej[j] = __ldg(m.ec + 6 * c + j);
+    w[j] = __ldg(m.ccdh + 6 * c + j) * a.F[size_t(ej[j]) * K + k];
+  }
+  Sa = w[0] + w[1];
+#pragma unroll
+  for (int j = 2; j < MAXE; ++j)
+    Sa += w[j];
+  if (p.do_h)
+    epilogue(s.ep, s.fh, i, 2.0 * Sa); // -sum_j ccd_j F_j
+  if (p.ntracers == 0)
+    return;
+  // advection + del2: sum_j a_j (n_c + n_j) + b_j (n_j - n_c)
+  double wc = Sa;
+  if (p.tr_del2) {
+    double b[MAXE], Sb;
+#pragma unroll
+    for (int j = 0; j < MAXE; ++j) {
+      b[j] = __ldg(p.kd2 + 6 * c + j) * a.mh[size_t(ej[j]) * K + k];
+      w[j] += b[j];
+    }
+    Sb = b[0] + b[1];
+#pragma unroll
+    for (int j = 2; j < MAXE; ++j)
+      Sb += b[j];
+    wc = Sa - Sb;
+  }
+  int nb[MAXE];
+#pragma unroll
+  for (int j = 0; j < MAXE; ++j)
+    nb[j] = __ldg(m.nbc + 6 * c + j);
+  for (int l = 0; l < p.ntracers; ++l) {
+    const size_t base = size_t(l) * CK;
+    const double *n = a.ntr + base;
+    double acc = wc * n[i];
+#pragma unroll
+    for (int j = 0; j < MAXE; ++j)
+      acc = fma(w[j], n[size_t(nb[j]) * K + k], acc);
+    if (p.tr_del4) {
+      const double *L = a.lap + base;
+      acc = fma(-__ldg(p.r4sum + c), L[i], acc);
+#pragma unroll
+      for (int j = 0; j < MAXE; ++j)
+        acc = fma(__ldg(p.r4 + 6 * c + j), L[size_t(nb[j]) * K + k], acc);
+    }
+    epilogue(s.ep, s.ftr, base + i, acc);
+  }
+}
+
+
+// Pass domain sizes (threads) of pass `pass` for one instance.
+enum Pass { P_VERTEX = 0, P_CELL1, P_EDGE1, P_AUX2, P_EDGE_FINAL,
+            P_CELL_FINAL, NPASS };
+
+} // namespace swg

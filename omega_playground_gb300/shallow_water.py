@@ -338,6 +338,62 @@ class LSRKStepper(TimeStepper):
         super().__init__(shallow_water, nstages)
 
 
+class Batch:
+    """Ensemble of independent members (uneven nx, levels, tracers) advanced
+    together by one persistent kernel per RK stage (swg_batch_* in swgpu.h).
+    Members are (ShallowWaterModel, ShallowWaterState) pairs."""
+
+    def __init__(self, models, states, kind: str = "rk4", nstages: int = 4):
+        n = len(models)
+        assert n == len(states) and n > 0
+        self.models, self.states = list(models), list(states)
+        mh = (C.c_void_p * n)(*[m.handle.value for m in models])
+        sh = (C.c_void_p * n)(*[s.handle.value for s in states])
+        h = C.c_void_p()
+        check(lib().swg_batch_create(n, mh, sh, 0 if kind == "rk4" else 1,
+                                     int(nstages), C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def step(self, t0: float, dt: float, nsteps: int, use_graph: bool = True,
+             stream=None, check_status: bool = True):
+        check(lib().swg_batch_step(self._h, float(t0), float(dt), int(nsteps),
+                                   int(use_graph), _s(stream)))
+        if check_status:
+            self.check(stream)
+
+    def check(self, stream=None):
+        check(lib().swg_batch_check(self._h, _s(stream)))
+
+    @staticmethod
+    def config_count() -> int:
+        return int(lib().swg_batch_config_count())
+
+    def set_config(self, config: int):
+        check(lib().swg_batch_set_config(self._h, int(config)))
+
+    def autotune(self, dt: float, reps: int = 2, stream=None):
+        """Times every launch configuration and keeps the fastest; returns
+        (config, ms per step).  The tuning steps advance the members."""
+        best, ms = C.c_int(), C.c_double()
+        check(lib().swg_batch_autotune(self._h, float(dt), int(reps),
+                                       _s(stream), C.byref(best), C.byref(ms)))
+        return best.value, ms.value
+
+    def selftest_timeout(self, limit_ms: float = 50.0, stream=None) -> int:
+        """Status code of a barrier wait that nothing releases."""
+        return int(lib().swg_batch_selftest_timeout(self._h, float(limit_ms),
+                                                    _s(stream)))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _capi._lib is not None:
+            _capi._lib.swg_batch_destroy(self._h)
+            self._h = None
+
+
 def _diag(fn, state, model, stream=None):
     out = C.c_double()
     check(fn(model.handle, state.handle, C.byref(out), _s(stream)))

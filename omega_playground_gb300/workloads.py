@@ -117,6 +117,26 @@ WORKLOADS = {
 }
 
 
+ENSEMBLE_NX = (32, 48, 64, 96, 128, 192)
+
+
+def ensemble(n: int = 64, seed: int = 20240602, nx_choices=ENSEMBLE_NX,
+             levels=(16, 96), tracers=(1, 4), nsteps: int = 200):
+    """Members of the batched ensemble: nx drawn from `nx_choices`, level
+    count uniform in `levels`, tracer count uniform in `tracers`, RK4, the
+    64x64 workload's physics (del2 viscosity 1e3), each with its own seed."""
+    r = uniform(seed, 3 * n).reshape(n, 3)
+    base = WORKLOADS["rk4_64x64"]
+    out = []
+    for i in range(n):
+        nx = nx_choices[int(r[i, 0] * len(nx_choices))]
+        K = levels[0] + int(r[i, 1] * (levels[1] - levels[0] + 1))
+        T = tracers[0] + int(r[i, 2] * (tracers[1] - tracers[0] + 1))
+        out.append(base.scaled(name=f"member{i}", nx=nx, ny=nx, nlayers=K,
+                               ntracers=T, nsteps=nsteps, seed=seed + 1000 * i))
+    return out
+
+
 def _min_image(d: np.ndarray, L: float) -> np.ndarray:
     return d - L * np.round(d / L)
 
