@@ -21,6 +21,8 @@ from __future__ import annotations
 
 import argparse
 import json
+
+import numpy as np
 import os
 import subprocess
 import sys
@@ -46,6 +48,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--nx", type=int, default=0,
                     help="override nx = ny (small profiling cases)")
     return ap.parse_args()
@@ -193,8 +196,68 @@ def run_reference(args, wl):
 
 # ---------------------------------------------------------- GPU arm -------
 
+def adjoint_ratio(stream):
+    """Checkpointed adjoint of the 128x128x32, 2-tracer RK4 workload (1000
+    steps, 32 snapshots): device time of the forward sweep (checkpoints +
+    taped last step) plus the backward sweep, over a plain 1000-step forward
+    on the same GPU.  The region loss and its gradient (host) are outside
+    both timings."""
+    import torch
+    import omega_playground_gb300 as og
+    from omega_playground_gb300.workloads import (ADJOINT_SNAPSHOTS, WORKLOADS,
+                                                  initial_state, loss_and_grad,
+                                                  region_cells)
+    wl = WORKLOADS["rk4_128x128_adjoint"]
+    mesh = og.PlanarHexagonalMesh(wl.nx, wl.ny, wl.dc, wl.nlayers)
+    params = wl.params()
+    model = og.ShallowWaterModel(mesh, params)
+    x0 = initial_state(mesh, wl)
+    region = region_cells(mesh, wl.seed + 99)
+    sh = stream.cuda_stream
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+    st = og.ShallowWaterState(mesh, params)
+    stepper = og.RK4Stepper(model)
+    st.upload(*x0)
+    stepper.step(st, 0.0, wl.dt, 3, stream=sh)        # warm-up, graph capture
+    st.upload(*x0)
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    stepper.step(st, 0.0, wl.dt, wl.nsteps, stream=sh)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    fwd_ms = ev[0].elapsed_time(ev[1])
+    adj = og.Adjoint(model, ADJOINT_SNAPSHOTS)
+    X0 = og.ShallowWaterState(mesh, params)
+    X0.upload(*x0)
+    XN = og.ShallowWaterState(mesh, params)
+    adj.forward(X0, 0.0, wl.dt, 2, XN, stream=sh)      # warm-up
+    G = og.ShallowWaterState(mesh, params)
+    G.fill(0.0, stream=sh)
+    adj.backward(G, stream=sh)
+    torch.cuda.synchronize()
+    ev[2].record(stream)
+    adj.forward(X0, 0.0, wl.dt, wl.nsteps, XN, stream=sh)
+    ev[3].record(stream)
+    torch.cuda.synchronize()
+    L, g = loss_and_grad(*XN.download(stream=sh), region)
+    G.upload(*g, stream=sh)
+    torch.cuda.synchronize()
+    ev[4].record(stream)
+    adj.backward(G, stream=sh)
+    ev[5].record(stream)
+    torch.cuda.synchronize()
+    f_ms, b_ms = ev[2].elapsed_time(ev[3]), ev[4].elapsed_time(ev[5])
+    plain, taped = adj.info()
+    grad = G.download(stream=sh)
+    return {"workload": wl.name, "steps": wl.nsteps,
+            "snapshots": ADJOINT_SNAPSHOTS, "plain_forward_ms": fwd_ms,
+            "checkpointed_forward_ms": f_ms, "backward_ms": b_ms,
+            "ratio": (f_ms + b_ms) / fwd_ms, "plain_advances": plain,
+            "taped_steps": taped, "loss": L,
+            "grad_h_norm": float(np.sqrt(np.sum(grad[0] ** 2)))}
+
+
 def run_ours(args, wl):
-    import numpy as np
     import torch
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -321,6 +384,9 @@ def run_ours(args, wl):
                "d2h_bytes_per_step": nbytes_in, "steps": args.e2e_steps,
                "ms_per_step": e2e_ms / args.e2e_steps}
 
+    adjoint = None
+    if rank == 0 and world == 1 and not args.no_adjoint:
+        adjoint = adjoint_ratio(stream)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl)
@@ -339,7 +405,8 @@ def run_ours(args, wl):
                              % (8 * (wl.ncells * wl.nlayers * (4 + wl.ntracers))
                                 / 1e9)},
             "roofline": roofline, "fp64_roofline": fp64, "kernels": kernels,
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "cpu_baseline": cpu, "e2e": e2e, "adjoint": adjoint,
+            "gpu_launches": launches,
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)

@@ -48,6 +48,7 @@ typedef struct swg_state_s *swg_state;
 typedef struct swg_model_s *swg_model;
 typedef struct swg_stepper_s *swg_stepper;
 typedef struct swg_batch_s *swg_batch;
+typedef struct swg_adjoint_s *swg_adjoint;
 
 /* Message of the calling thread's last failed call ("" if none). */
 const char *swg_last_error(void);
@@ -233,6 +234,36 @@ int swg_batch_autotune(swg_batch batch, double dt, int reps, void *stream,
  * limit of limit_ms (<= 2000) and returns the resulting SWG_ERR_TIMEOUT. */
 int swg_batch_selftest_timeout(swg_batch batch, double limit_ms,
                                void *stream);
+
+/* ------------------------------------------ adjoint and tangent-linear ----
+ * Differentiation of the RK4 step (no counterpart in the reference).  An
+ * adjoint object is tied to a model (no forcing hook, edge_mask all ones,
+ * dv >= dc/4) and owns `nsnapshots` state checkpoints for the binomial
+ * checkpointing schedule, the stage tape of one step and the adjoint work
+ * arrays.  Tendency level, in the style of an autograd Function's jvp/vjp:
+ *   swg_tlm_tendency: dtend = J(x) dx        (exact forward-mode derivative)
+ *   swg_adj_tendency: lambda = J(x)^T mu     (hand-written reverse mode)
+ * Trajectory level (RK4, dt fixed):
+ *   swg_tlm_apply:   dx <- d x_N (propagated tangent of nsteps steps)
+ *   swg_adj_forward: runs nsteps steps from state0 storing checkpoints,
+ *                    writes x_N to final_out;
+ *   swg_adj_backward: lambda (in: dL/dx_N) <- dL/dx_0. */
+int swg_adjoint_create(swg_model model, int nsnapshots, swg_adjoint *out);
+int swg_adjoint_destroy(swg_adjoint adj);
+int swg_tlm_tendency(swg_adjoint adj, swg_state x, swg_state dx,
+                     swg_state dtend_out, void *stream);
+int swg_adj_tendency(swg_adjoint adj, swg_state x, swg_state mu,
+                     swg_state lambda_out, void *stream);
+int swg_tlm_apply(swg_adjoint adj, swg_state x0, swg_state dx, double t0,
+                  double dt, int nsteps, void *stream);
+int swg_adj_forward(swg_adjoint adj, swg_state state0, double t0, double dt,
+                    int nsteps, swg_state final_out, void *stream);
+int swg_adj_backward(swg_adjoint adj, swg_state lambda, void *stream);
+/* plain (re-)advanced and taped steps of the last forward/backward pair */
+int swg_adj_info(swg_adjoint adj, long long *plain_steps,
+                 long long *taped_steps);
+/* plain advances of the optimal binomial schedule (host only) */
+long long swg_checkpoint_cost(int nsteps, int nsnapshots);
 
 /* ------------------------------------------------------- diagnostics -----
  * replaces energy_integral / mass_integral / circulation_integral

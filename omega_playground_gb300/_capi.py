@@ -121,6 +121,18 @@ _SIGS = {
     "swg_batch_autotune": (C.c_int, [_vp, C.c_double, C.c_int, _vp,
                                      C.POINTER(C.c_int), _dp]),
     "swg_batch_selftest_timeout": (C.c_int, [_vp, C.c_double, _vp]),
+    "swg_adjoint_create": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
+    "swg_adjoint_destroy": (C.c_int, [_vp]),
+    "swg_tlm_tendency": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "swg_adj_tendency": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "swg_tlm_apply": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double,
+                                C.c_int, _vp]),
+    "swg_adj_forward": (C.c_int, [_vp, _vp, C.c_double, C.c_double, C.c_int,
+                                  _vp, _vp]),
+    "swg_adj_backward": (C.c_int, [_vp, _vp, _vp]),
+    "swg_adj_info": (C.c_int, [_vp, C.POINTER(C.c_longlong),
+                               C.POINTER(C.c_longlong)]),
+    "swg_checkpoint_cost": (C.c_longlong, [C.c_int, C.c_int]),
     "swg_diag_mass": (C.c_int, [_vp, _vp, _dp, _vp]),
     "swg_diag_energy": (C.c_int, [_vp, _vp, _dp, _vp]),
     "swg_diag_circulation": (C.c_int, [_vp, _vp, _dp, _vp]),

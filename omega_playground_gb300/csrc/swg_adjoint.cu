@@ -1,0 +1,1034 @@
+// Adjoint (reverse mode) and tangent-linear (forward mode) models of the
+// RK4 shallow-water step, with binomial checkpointing.
+//
+// Tangent-linear model: the tendency passes of swg_device.cuh instantiated
+// on dual numbers (value, tangent); their value part is the forward's exact
+// operation sequence, so the TLM is the exact derivative of the discrete
+// forward.  Used by swg_tlm_tendency / swg_tlm_apply and to check the
+// adjoint with dot-product tests.
+//
+// Adjoint of one tendency evaluation F at a state X: given mu (adjoint of the
+// tendency), lambda = J(X)^T mu.  Hand-written, seven gather-only passes (no
+// atomics): every transposed stencil reads its neighbours' coefficients from
+// transposed tables built on the host (the neighbour's coefficient for a
+// shared edge, per-edge copies of the two cells' / vertices' coefficients,
+// and the transposed edges-on-edge list).  Intermediates of F at X come from
+// the forward auxiliary passes (launch_aux).  Reference terms transposed:
+// thickness_hadv_cell.hpp:59-83, pv_flux_edge.hpp:149-177,
+// ke_grad_edge.hpp:223-237, ssh_grad_edge.hpp:281-294,
+// vel_diff_edge.hpp:61-86, vel_hyperdiff_edge.hpp:237-334,
+// tracer_hadv_cell.hpp:60-90, tracer_diff_cell.hpp:162-193,
+// tracer_hyperdiff_cell.hpp:301-368, and the auxiliary variables
+// (vorticity_aux.hpp, kinetic_aux.hpp, thickness_aux.hpp, tracer_aux.hpp).
+//
+// RK4 step adjoint (rk4.cpp:28-104): with stage inputs X0..X3 recorded by a
+// taped forward step, mu_3 = dt b3 lam, mu_s = dt b_s lam + dt a_s lamX_{s+1},
+// lamX_s = J(X_s)^T mu_s, and lam_i = lam_{i+1} + sum_s lamX_s.
+//
+// Checkpointing: the optimal binomial schedule (Griewank-Walther) for n
+// steps and s snapshots, computed by dynamic programming over (n, s); the
+// forward sweep stores the schedule's checkpoints, the backward sweep
+// restores, re-advances and tapes each step once, in reverse order.
+#include "swg_device.cuh"
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+
+namespace swg {
+namespace {
+
+constexpr int ATPB = 256;
+
+struct AdjView {
+  // cells [C][6]
+  const double *ccdh_nb, *ckq_nb, *kd2_nb, *r4_nb; // neighbour's coefficient
+  const double *keadj, *d4adj, *hsadj, *divadj;    // transposed edge terms
+  const int *cvtx;                                 // vertices of the cell
+  const double *ckvh;                              // their kite weight for c
+  // edges [E][2]: coefficients of cells (c0, c1) / vertices (v0, v1) for e
+  const double *ccd_e2, *ccdh_e2, *cke_e2, *ckq_e2, *kd2_e2, *cvr_e2;
+  // transposed edges-on-edge [E][nt] with weights / 4
+  const int *eoeT;
+  const double *woeT;
+  int nt;
+  // vertices [V][3]
+  const double *z4adj, *zetaadj;
+};
+
+struct AdjWork {
+  double *lL, *ln;                      // [T][C][K]
+  double *lke, *ld4, *lhs, *lhtr, *ldiv; // [C][K]
+  double *lz4, *lzeta, *lhv;            // [V][K]
+  double *lQ, *lmh, *lvnp, *ld2u;       // [E][K]
+};
+
+struct AdjIO {
+  const double *h, *vn, *tr;    // state X
+  const double *mh_, *mvn, *mtr; // mu (adjoint of the tendency)
+  double *lh, *lvn, *ltr;        // lambda = J^T mu (written)
+};
+
+// --- pass 1: transposed edge stencils of the velocity tendency (cells and
+// vertices); the first V*K threads take vertices.
+__global__ void __launch_bounds__(ATPB)
+    ka_vel(MeshView m, ModelView p, AdjView v, AdjWork w, AdjIO io) {
+  const int K = m.nlayers;
+  unsigned i = blockIdx.x * ATPB + threadIdx.x;
+  const unsigned VK = unsigned(m.nvertices) * K, CK = unsigned(m.ncells) * K;
+  if (i < VK) {
+    if (!p.vel_del4)
+      return;
+    const int vx = int(i / unsigned(K)), k = int(i - unsigned(vx) * K);
+    double z = 0;
+    for (int j = 0; j < 3; ++j)
+      z = fma(__ldg(v.z4adj + 3 * vx + j),
+              io.mvn[size_t(__ldg(m.ev + 3 * vx + j)) * K + k], z);
+    w.lz4[i] = z;
+    return;
+  }
+  i -= VK;
+  if (i >= CK)
+    return;
+  const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
+  double ke = 0, d4 = 0, hs = 0;
+  for (int j = 0; j < MAXE; ++j) {
+    const double mu = io.mvn[size_t(__ldg(m.ec + 6 * c + j)) * K + k];
+    ke = fma(__ldg(v.keadj + 6 * c + j), mu, ke);
+    hs = fma(__ldg(v.hsadj + 6 * c + j), mu, hs);
+    if (p.vel_del4)
+      d4 = fma(__ldg(v.d4adj + 6 * c + j), mu, d4);
+  }
+  w.lke[i] = ke;
+  w.lhs[i] = hs;
+  if (p.vel_del4)
+    w.ld4[i] = d4;
+}
+
+__device__ __forceinline__ double mean_h(const MeshView &m, const double *h,
+                                         int e, int k) {
+  const int K = m.nlayers;
+  return 0.5 * (h[size_t(__ldg(m.ce + 2 * e)) * K + k] +
+                h[size_t(__ldg(m.ce + 2 * e + 1)) * K + k]);
+}
+
+// --- pass 2: tracer tendency transposed to the normalised tracers (partial)
+// and to the tracer Laplacian.
+__global__ void __launch_bounds__(ATPB)
+    ka_tr1(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
+           AdjIO io) {
+  const int K = m.nlayers;
+  const unsigned i = blockIdx.x * ATPB + threadIdx.x;
+  const unsigned CK = unsigned(m.ncells) * K;
+  if (i >= CK)
+    return;
+  const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
+  double wnb[MAXE], wc = 0;
+  int nb[MAXE];
+  for (int j = 0; j < MAXE; ++j) {
+    const int e = __ldg(m.ec + 6 * c + j);
+    nb[j] = __ldg(m.nbc + 6 * c + j);
+    const double F = a.F[size_t(e) * K + k];
+    double x = __ldg(v.ccdh_nb + 6 * c + j) * F;
+    double own = __ldg(m.ccdh + 6 * c + j) * F;
+    if (p.tr_del2) {
+      const double mh = mean_h(m, io.h, e, k);
+      x = fma(__ldg(v.kd2_nb + 6 * c + j), mh, x);
+      own = fma(-__ldg(p.kd2 + 6 * c + j), mh, own);
+    }
+    wnb[j] = x;
+    wc += own;
+  }
+  for (int l = 0; l < p.ntracers; ++l) {
+    const double *mu = io.mtr + size_t(l) * CK;
+    double acc = wc * mu[i];
+    for (int j = 0; j < MAXE; ++j)
+      acc = fma(wnb[j], mu[size_t(nb[j]) * K + k], acc);
+    w.ln[size_t(l) * CK + i] = acc;
+    if (p.tr_del4) {
+      double L = -__ldg(p.r4sum + c) * mu[i];
+      for (int j = 0; j < MAXE; ++j)
+        L = fma(__ldg(v.r4_nb + 6 * c + j), mu[size_t(nb[j]) * K + k], L);
+      w.lL[size_t(l) * CK + i] = L;
+    }
+  }
+}
+
+// --- pass 3: through the tracer Laplacian and n = tr / h to the tracers;
+// the h part of n = tr / h is kept for pass 6.
+__global__ void __launch_bounds__(ATPB)
+    ka_tr2(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
+           AdjIO io) {
+  const int K = m.nlayers;
+  const unsigned i = blockIdx.x * ATPB + threadIdx.x;
+  const unsigned CK = unsigned(m.ncells) * K;
+  if (i >= CK)
+    return;
+  const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
+  double mnb[MAXE], M = 0;
+  int nb[MAXE];
+  if (p.tr_del4)
+    for (int j = 0; j < MAXE; ++j) {
+      const int e = __ldg(m.ec + 6 * c + j);
+      const double mh = mean_h(m, io.h, e, k);
+      nb[j] = __ldg(m.nbc + 6 * c + j);
+      mnb[j] = __ldg(v.ckq_nb + 6 * c + j) * mh;
+      M = fma(__ldg(m.ckq + 6 * c + j), mh, M);
+    }
+  // 1/h: the forward's own reciprocal
+  double r;
+  {
+    double x = io.h[i];
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+  }
+  double hsum = 0;
+  for (int l = 0; l < p.ntracers; ++l) {
+    const size_t t = size_t(l) * CK + i;
+    double ln = w.ln[t];
+    if (p.tr_del4) {
+      const double *lL = w.lL + size_t(l) * CK;
+      ln = fma(-M, lL[i], ln);
+      for (int j = 0; j < MAXE; ++j)
+        ln = fma(mnb[j], lL[size_t(nb[j]) * K + k], ln);
+    }
+    io.ltr[t] = ln * r;
+    hsum = fma(ln, a.ntr[t], hsum);
+  }
+  w.lhtr[i] = -(r * hsum);
+}
+
+// --- pass 4: edges: PV flux (transposed edges-on-edge), thickness flux,
+// mean thickness, kinetic energy, edge Laplacian.
+template <int NE>
+__global__ void __launch_bounds__(ATPB)
+    ka_edge(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
+            AdjIO io) {
+  const int K = m.nlayers;
+  const unsigned i = blockIdx.x * ATPB + threadIdx.x;
+  if (i >= unsigned(m.nedges) * K)
+    return;
+  const unsigned CK = unsigned(m.ncells) * K;
+  const int e = int(i / unsigned(K)), k = int(i - unsigned(e) * K);
+  const int c0 = __ldg(m.ce + 2 * e), c1 = __ldg(m.ce + 2 * e + 1);
+  const size_t i0 = size_t(c0) * K + k, i1 = size_t(c1) * K + k;
+  const double F = a.F[i], u = io.vn[i];
+  double lF = 0, lmh = 0;
+  if (p.do_vn) {
+    // PV flux: t_e = Q_e S1_e + S2_e, S1 = sum w F_j, S2 = sum w G_j
+    double lG = 0, lFq = 0;
+    for (int t = 0; t < v.nt; ++t) {
+      const int es = __ldg(v.eoeT + v.nt * e + t);
+      const double ws = __ldg(v.woeT + v.nt * e + t);
+      const double mus = io.mvn[size_t(es) * K + k];
+      lG = fma(ws, mus, lG);
+      lFq = fma(ws, a.Q[size_t(es) * K + k] * mus, lFq);
+    }
+    double S1 = 0;
+    for (int j = 0; j < NE; ++j)
+      S1 = fma(__ldg(m.woe + NE * e + j),
+               a.F[size_t(__ldg(m.eoe + NE * e + j)) * K + k], S1);
+    const double Q = a.Q[i], mu = io.mvn[i];
+    w.lQ[i] = fma(S1, mu, F * lG);
+    lF = fma(Q, lG, lFq);
+    // kinetic energy from vn^2
+    const double lu2 = fma(__ldg(v.cke_e2 + 2 * e), w.lke[i0],
+                           __ldg(v.cke_e2 + 2 * e + 1) * w.lke[i1]);
+    w.lvnp[i] = 2.0 * u * lu2; // mean-h term added below
+    if (p.vel_del2 | p.vel_del4) {
+      const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
+      double d = p.vel_del2 ? __ldg(p.c2e + e) * mu : 0.0;
+      if (p.vel_del4) {
+        d = fma(__ldg(v.cvr_e2 + 2 * e), w.lz4[size_t(v0) * K + k], d);
+        d = fma(__ldg(v.cvr_e2 + 2 * e + 1), w.lz4[size_t(v1) * K + k], d);
+        d = fma(__ldg(v.ccd_e2 + 2 * e), w.ld4[i0], d);
+        d = fma(__ldg(v.ccd_e2 + 2 * e + 1), w.ld4[i1], d);
+      }
+      w.ld2u[i] = d;
+    }
+  } else {
+    w.lvnp[i] = 0.0;
+  }
+  const double g0 = __ldg(v.ccdh_e2 + 2 * e), g1 = __ldg(v.ccdh_e2 + 2 * e + 1);
+  if (p.do_h)
+    lF = fma(2.0 * g0, io.mh_[i0], fma(2.0 * g1, io.mh_[i1], lF));
+  if (p.ntracers > 0) {
+    const double k20 = __ldg(v.kd2_e2 + 2 * e), k21 = __ldg(v.kd2_e2 + 2 * e + 1);
+    const double q0 = __ldg(v.ckq_e2 + 2 * e), q1 = __ldg(v.ckq_e2 + 2 * e + 1);
+    for (int l = 0; l < p.ntracers; ++l) {
+      const size_t b = size_t(l) * CK;
+      const double n0 = a.ntr[b + i0], n1 = a.ntr[b + i1];
+      const double m0 = io.mtr[b + i0], m1 = io.mtr[b + i1];
+      lF = fma(n0 + n1, fma(g0, m0, g1 * m1), lF);
+      const double dn = n1 - n0;
+      if (p.tr_del2)
+        lmh = fma(dn, fma(k20, m0, -(k21 * m1)), lmh);
+      if (p.tr_del4)
+        lmh = fma(dn, fma(q0, w.lL[b + i0], -(q1 * w.lL[b + i1])), lmh);
+    }
+  }
+  const double mh = mean_h(m, io.h, e, k);
+  lmh = fma(u, lF, lmh);
+  w.lmh[i] = lmh;
+  w.lvnp[i] = fma(mh, lF, w.lvnp[i]);
+}
+
+// --- pass 5: vertices: PV q = (zeta + f) / h_v, vorticity.
+__global__ void __launch_bounds__(ATPB)
+    ka_vertex(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
+              AdjIO io) {
+  const int K = m.nlayers;
+  const unsigned i = blockIdx.x * ATPB + threadIdx.x;
+  if (i >= unsigned(m.nvertices) * K)
+    return;
+  const int vx = int(i / unsigned(K)), k = int(i - unsigned(vx) * K);
+  double lq = 0, hv = 0, lz = 0;
+  for (int j = 0; j < 3; ++j) {
+    const int e = __ldg(m.ev + 3 * vx + j);
+    lq += w.lQ[size_t(e) * K + k];
+    hv = fma(__ldg(m.kvh + 3 * vx + j),
+             io.h[size_t(__ldg(m.cv + 3 * vx + j)) * K + k], hv);
+    if (p.vel_del2 | p.vel_del4)
+      lz = fma(__ldg(v.zetaadj + 3 * vx + j), w.ld2u[size_t(e) * K + k], lz);
+  }
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(hv));
+  double er = fma(-hv, r, 1.0);
+  r = fma(r, er, r);
+  er = fma(-hv, r, 1.0);
+  r = fma(r, er, r);
+  w.lzeta[i] = fma(r, lq, lz);
+  w.lhv[i] = -(a.q[i] * r * lq);
+}
+
+// --- pass 6: cells: thickness adjoint, velocity divergence adjoint.
+__global__ void __launch_bounds__(ATPB)
+    ka_cell(MeshView m, ModelView p, AdjView v, AdjWork w, AdjIO io) {
+  const int K = m.nlayers;
+  const unsigned i = blockIdx.x * ATPB + threadIdx.x;
+  if (i >= unsigned(m.ncells) * K)
+    return;
+  const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
+  double lh = 0, ld = 0, smh = 0;
+  for (int j = 0; j < MAXE; ++j) {
+    const int e = __ldg(m.ec + 6 * c + j);
+    smh += w.lmh[size_t(e) * K + k] * (__ldg(m.ccd + 6 * c + j) != 0.0);
+    if (p.do_vn) {
+      lh = fma(__ldg(v.ckvh + 6 * c + j),
+               w.lhv[size_t(__ldg(v.cvtx + 6 * c + j)) * K + k], lh);
+      if (p.vel_del2 | p.vel_del4)
+        ld = fma(__ldg(v.divadj + 6 * c + j), w.ld2u[size_t(e) * K + k], ld);
+    }
+  }
+  lh = fma(0.5, smh, lh);
+  if (p.do_vn)
+    lh += w.lhs[i];
+  if (p.ntracers > 0)
+    lh += w.lhtr[i];
+  io.lh[i] = lh;
+  if (p.do_vn && (p.vel_del2 | p.vel_del4))
+    w.ldiv[i] = ld;
+}
+
+// --- pass 7: edges: normal velocity adjoint.
+__global__ void __launch_bounds__(ATPB)
+    ka_vn(MeshView m, ModelView p, AdjView v, AdjWork w, AdjIO io) {
+  const int K = m.nlayers;
+  const unsigned i = blockIdx.x * ATPB + threadIdx.x;
+  if (i >= unsigned(m.nedges) * K)
+    return;
+  const int e = int(i / unsigned(K)), k = int(i - unsigned(e) * K);
+  double l = w.lvnp[i];
+  if (p.do_vn) {
+    const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
+    l = fma(__ldg(v.cvr_e2 + 2 * e), w.lzeta[size_t(v0) * K + k], l);
+    l = fma(__ldg(v.cvr_e2 + 2 * e + 1), w.lzeta[size_t(v1) * K + k], l);
+    if (p.vel_del2 | p.vel_del4) {
+      const int c0 = __ldg(m.ce + 2 * e), c1 = __ldg(m.ce + 2 * e + 1);
+      l = fma(__ldg(v.ccd_e2 + 2 * e), w.ldiv[size_t(c0) * K + k], l);
+      l = fma(__ldg(v.ccd_e2 + 2 * e + 1), w.ldiv[size_t(c1) * K + k], l);
+    }
+  }
+  io.lvn[i] = l;
+}
+
+// y = alpha x1 + beta x2 (x2 may be null), y += x (axpy), dual pack/unpack
+__global__ void ka_lincomb(double *y, const double *x1, const double *x2,
+                           double alpha, double beta, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n)
+    y[i] = x2 ? fma(alpha, x1[i], beta * x2[i]) : alpha * x1[i];
+}
+__global__ void ka_add(double *y, const double *x, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n)
+    y[i] += x[i];
+}
+__global__ void ka_pack(Dual *y, const double *v, const double *d,
+                        long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n)
+    y[i] = Dual{v[i], d ? d[i] : 0.0};
+}
+__global__ void ka_unpack(double *v, double *d, const Dual *x, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) {
+    if (v)
+      v[i] = x[i].v;
+    if (d)
+      d[i] = x[i].d;
+  }
+}
+
+unsigned nb(long long n) { return unsigned((n + ATPB - 1) / ATPB); }
+
+} // namespace
+} // namespace swg
+
+using namespace swg;
+
+struct AdjAction {
+  int type; // 0 advance(i, n), 1 store(slot), 2 restore(slot), 3 tape+adjoint(i)
+  int a, b;
+};
+
+struct swg_adjoint_s {
+  swg_model model;
+  int nsnap;
+  AdjView av{};
+  AdjWork aw{};
+  std::vector<void *> allocs;
+  swg_stepper stepper = nullptr; // plain advances (graph replay)
+  std::vector<swg_state> snaps;
+  swg_state cur = nullptr, next = nullptr, X[4] = {}, acc = nullptr,
+            lam = nullptr, lacc = nullptr, mu = nullptr, lX = nullptr;
+  // tangent-linear model buffers
+  AuxViewT<Dual> daux{};
+  Dual *dS = nullptr, *dacc = nullptr, *dP0 = nullptr, *dP1 = nullptr,
+       *dT = nullptr;
+  // schedule
+  std::vector<AdjAction> actions;
+  size_t pos = 0;
+  int nsteps = 0;
+  double t0 = 0, dt = 0;
+  long long plain_steps = 0, taped_steps = 0;
+  int state = 0; // 0 idle, 1 forward done (first step taped)
+};
+
+namespace {
+
+#define TRY(x)                                                                 \
+  do {                                                                         \
+    int rc_ = (x);                                                             \
+    if (rc_ != SWG_OK)                                                         \
+      return rc_;                                                              \
+  } while (0)
+
+template <class T>
+int up(std::vector<void *> &allocs, const std::vector<T> &h, const T **d) {
+  void *p = nullptr;
+  cudaError_t err = cudaMalloc(&p, std::max<size_t>(h.size(), 1) * sizeof(T));
+  if (err != cudaSuccess)
+    return cuda_fail(err, "swg_adjoint: cudaMalloc");
+  allocs.push_back(p);
+  if (!h.empty() && (err = cudaMemcpy(p, h.data(), h.size() * sizeof(T),
+                                      cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_fail(err, "swg_adjoint: cudaMemcpy");
+  *d = static_cast<const T *>(p);
+  return SWG_OK;
+}
+
+template <class T> int zal(std::vector<void *> &allocs, size_t n, T **d) {
+  void *p = nullptr;
+  cudaError_t err = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
+  if (err == cudaSuccess)
+    err = cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(T));
+  if (err != cudaSuccess)
+    return cuda_fail(err, "swg_adjoint: work allocation");
+  allocs.push_back(p);
+  *d = static_cast<T *>(p);
+  return SWG_OK;
+}
+
+size_t words(swg_model md) {
+  return (size_t(md->mesh->ncells) + md->mesh->nedges +
+          size_t(md->params.ntracers) * md->mesh->ncells) *
+         md->mesh->nlayers;
+}
+
+int slot_of(const std::vector<int> &list, int base, int n, int x) {
+  for (int j = 0; j < n; ++j)
+    if (list[base + j] == x)
+      return j;
+  return -1;
+}
+
+int build_tables(swg_adjoint ad) {
+  swg_model md = ad->model;
+  swg_mesh me = md->mesh;
+  const swg_params &P = md->params;
+  const int C = me->ncells, E = me->nedges, V = me->nvertices;
+  std::vector<double> ccdh_nb(6 * C, 0), ckq_nb(6 * C, 0), kd2_nb(6 * C, 0),
+      r4_nb(6 * C, 0), keadj(6 * C, 0), d4adj(6 * C, 0), hsadj(6 * C, 0),
+      divadj(6 * C, 0), ckvh(6 * C, 0);
+  std::vector<int> cvtx(6 * C, 0);
+  std::vector<double> ccd_e2(2 * E), ccdh_e2(2 * E), cke_e2(2 * E),
+      ckq_e2(2 * E), kd2_e2(2 * E), cvr_e2(2 * E), z4adj(3 * V), zetaadj(3 * V);
+  auto kd2 = [&](int c, int j) {
+    return P.eddy_diff2 * me->scale2_h[me->ec_h[6 * c + j]] * me->ckq_h[6 * c + j];
+  };
+  auto r4 = [&](int c, int j) {
+    return -(P.eddy_diff4 * me->scale4_h[me->ec_h[6 * c + j]] * me->ckq_h[6 * c + j]);
+  };
+  for (int c = 0; c < C; ++c)
+    for (int j = 0; j < MAXE; ++j) {
+      if (me->ccd_h[6 * c + j] == 0.0 && me->ckq_h[6 * c + j] == 0.0)
+        continue; // padding slot
+      const int e = me->ec_h[6 * c + j], n = me->nbc_h[6 * c + j];
+      const int jn = slot_of(me->ec_h, 6 * n, MAXE, e);
+      if (jn < 0)
+        return fail(SWG_ERR_ARG, "swg_adjoint: edge missing from its neighbour");
+      ccdh_nb[6 * c + j] = me->ccdh_h[6 * n + jn];
+      ckq_nb[6 * c + j] = me->ckq_h[6 * n + jn];
+      kd2_nb[6 * c + j] = kd2(n, jn);
+      r4_nb[6 * c + j] = r4(n, jn);
+      const double sg = me->ce_h[2 * e] == c ? 1.0 : -1.0;
+      keadj[6 * c + j] = sg * me->inv_dc_h[e];
+      hsadj[6 * c + j] = sg * (P.grav * me->inv_dc_h[e]);
+      d4adj[6 * c + j] = -(sg * (-(P.visc_del4 * me->scale4_h[e])) * me->inv_dc_h[e]);
+      divadj[6 * c + j] = -(sg * me->inv_dc_h[e]);
+    }
+  // cells' vertices and kite weights (inverse of cells_on_vertex)
+  std::vector<int> cnt(C, 0);
+  for (int v = 0; v < V; ++v)
+    for (int j = 0; j < 3; ++j) {
+      const int c = me->cv_h[3 * v + j];
+      if (me->kvh_h[3 * v + j] == 0.0)
+        continue;
+      if (cnt[c] >= MAXE)
+        return fail(SWG_ERR_ARG, "swg_adjoint: a cell is on more than 6 vertices");
+      cvtx[6 * c + cnt[c]] = v;
+      ckvh[6 * c + cnt[c]] = me->kvh_h[3 * v + j];
+      ++cnt[c];
+    }
+  for (int e = 0; e < E; ++e)
+    for (int s = 0; s < 2; ++s) {
+      const int c = me->ce_h[2 * e + s];
+      const int j = slot_of(me->ec_h, 6 * c, MAXE, e);
+      const int v = me->ve_h[2 * e + s];
+      const int jv = slot_of(me->ev_h, 3 * v, 3, e);
+      if (j < 0 || jv < 0)
+        return fail(SWG_ERR_ARG, "swg_adjoint: inconsistent edge tables");
+      ccd_e2[2 * e + s] = me->ccd_h[6 * c + j];
+      ccdh_e2[2 * e + s] = me->ccdh_h[6 * c + j];
+      cke_e2[2 * e + s] = me->cke_h[6 * c + j];
+      ckq_e2[2 * e + s] = me->ckq_h[6 * c + j];
+      kd2_e2[2 * e + s] = kd2(c, j);
+      cvr_e2[2 * e + s] = me->cvr_h[3 * v + jv];
+    }
+  for (int v = 0; v < V; ++v)
+    for (int j = 0; j < 3; ++j) {
+      const int e = me->ev_h[3 * v + j];
+      const double sg = me->ve_h[2 * e] == v ? -1.0 : 1.0;
+      z4adj[3 * v + j] = -(sg * (-(P.visc_del4 * me->scale4_h[e])) * me->inv_dv_h[e]);
+      zetaadj[3 * v + j] = -(sg * me->inv_dv_h[e]);
+    }
+  // transposed edges-on-edge
+  const int NE = me->view.ne;
+  std::vector<int> tc(E, 0);
+  for (int e = 0; e < E; ++e)
+    for (int j = 0; j < NE; ++j)
+      if (me->woe_h[NE * e + j] != 0.0)
+        ++tc[me->eoe_h[NE * e + j]];
+  int nt = 1;
+  for (int e = 0; e < E; ++e)
+    nt = std::max(nt, tc[e]);
+  std::vector<int> eoeT(size_t(nt) * E);
+  std::vector<double> woeT(size_t(nt) * E, 0.0);
+  std::fill(tc.begin(), tc.end(), 0);
+  for (int e = 0; e < E; ++e)
+    for (int t = 0; t < nt; ++t)
+      eoeT[size_t(nt) * e + t] = e;
+  for (int e = 0; e < E; ++e)
+    for (int j = 0; j < NE; ++j) {
+      const double w = me->woe_h[NE * e + j];
+      if (w == 0.0)
+        continue;
+      const int t = me->eoe_h[NE * e + j];
+      eoeT[size_t(nt) * t + tc[t]] = e;
+      woeT[size_t(nt) * t + tc[t]] = w;
+      ++tc[t];
+    }
+  AdjView &a = ad->av;
+  auto &A = ad->allocs;
+  int rc;
+  if ((rc = up(A, ccdh_nb, &a.ccdh_nb)) || (rc = up(A, ckq_nb, &a.ckq_nb)) ||
+      (rc = up(A, kd2_nb, &a.kd2_nb)) || (rc = up(A, r4_nb, &a.r4_nb)) ||
+      (rc = up(A, keadj, &a.keadj)) || (rc = up(A, d4adj, &a.d4adj)) ||
+      (rc = up(A, hsadj, &a.hsadj)) || (rc = up(A, divadj, &a.divadj)) ||
+      (rc = up(A, cvtx, &a.cvtx)) || (rc = up(A, ckvh, &a.ckvh)) ||
+      (rc = up(A, ccd_e2, &a.ccd_e2)) || (rc = up(A, ccdh_e2, &a.ccdh_e2)) ||
+      (rc = up(A, cke_e2, &a.cke_e2)) || (rc = up(A, ckq_e2, &a.ckq_e2)) ||
+      (rc = up(A, kd2_e2, &a.kd2_e2)) || (rc = up(A, cvr_e2, &a.cvr_e2)) ||
+      (rc = up(A, eoeT, &a.eoeT)) || (rc = up(A, woeT, &a.woeT)) ||
+      (rc = up(A, z4adj, &a.z4adj)) || (rc = up(A, zetaadj, &a.zetaadj)))
+    return rc;
+  a.nt = nt;
+  return SWG_OK;
+}
+
+// aux arrays of the tangent-linear model (same set as the model's)
+int alloc_dual_aux(swg_adjoint ad) {
+  swg_model md = ad->model;
+  const ModelView &pv = md->view;
+  const AuxView &a = md->aux;
+  const size_t C = md->mesh->ncells, E = md->mesh->nedges,
+               V = md->mesh->nvertices, K = md->mesh->nlayers,
+               T = md->params.ntracers;
+  AuxViewT<Dual> &d = ad->daux;
+  auto &A = ad->allocs;
+  struct {
+    const double *on;
+    size_t n;
+    Dual **p;
+  } t[] = {{a.q, V * K, &d.q},       {a.zeta, V * K, &d.zeta},
+           {a.z4, V * K, &d.z4},     {a.div, C * K, &d.div},
+           {a.ke, C * K, &d.ke},     {a.d4, C * K, &d.d4},
+           {a.ntr, T * C * K, &d.ntr}, {a.lap, T * C * K, &d.lap},
+           {a.F, E * K, &d.F},       {a.G, E * K, &d.G},
+           {a.Q, E * K, &d.Q},       {a.mh, E * K, &d.mh},
+           {a.u2, E * K, &d.u2},     {a.d2u, E * K, &d.d2u}};
+  for (auto &x : t)
+    if (x.on)
+      TRY(zal(A, x.n, x.p));
+  d.d2u4 = d.d2u;
+  (void)pv;
+  return SWG_OK;
+}
+
+void adj_tendency(swg_adjoint ad, const double *h, const double *vn,
+                  const double *tr, swg_state mu, swg_state out,
+                  cudaStream_t st) {
+  swg_model md = ad->model;
+  const MeshView &m = md->mesh->view;
+  const ModelView &p = md->view;
+  const long long K = m.nlayers, CK = m.ncells * K, EK = m.nedges * K,
+                  VK = m.nvertices * K;
+  launch_aux(m, p, md->aux, h, vn, tr, st);
+  AdjIO io{h, vn, tr, mu->h, mu->vn, mu->tr, out->h, out->vn, out->tr};
+  const AdjView &v = ad->av;
+  const AdjWork &w = ad->aw;
+  if (p.do_vn) {
+    ka_vel<<<nb(VK + CK), ATPB, 0, st>>>(m, p, v, w, io);
+    ++g_launches;
+  }
+  if (p.ntracers > 0) {
+    ka_tr1<<<nb(CK), ATPB, 0, st>>>(m, p, md->aux, v, w, io);
+    ka_tr2<<<nb(CK), ATPB, 0, st>>>(m, p, md->aux, v, w, io);
+    g_launches += 2;
+  }
+  if (m.ne == 8)
+    ka_edge<8><<<nb(EK), ATPB, 0, st>>>(m, p, md->aux, v, w, io);
+  else
+    ka_edge<10><<<nb(EK), ATPB, 0, st>>>(m, p, md->aux, v, w, io);
+  ++g_launches;
+  if (p.do_vn) {
+    ka_vertex<<<nb(VK), ATPB, 0, st>>>(m, p, md->aux, v, w, io);
+    ++g_launches;
+  }
+  ka_cell<<<nb(CK), ATPB, 0, st>>>(m, p, v, w, io);
+  ka_vn<<<nb(EK), ATPB, 0, st>>>(m, p, v, w, io);
+  g_launches += 2;
+}
+
+void lincomb(swg_state y, swg_state x1, swg_state x2, double a, double b,
+             long long n, cudaStream_t st) {
+  ka_lincomb<<<nb(n), ATPB, 0, st>>>(y->h, x1->h, x2 ? x2->h : nullptr, a, b, n);
+  ++g_launches;
+}
+
+void addto(swg_state y, swg_state x, long long n, cudaStream_t st) {
+  ka_add<<<nb(n), ATPB, 0, st>>>(y->h, x->h, n);
+  ++g_launches;
+}
+
+// stage input of the tape: a disabled field keeps its start-of-step value
+void stage_ptrs(swg_adjoint ad, int s, const double **h, const double **vn,
+                const double **tr) {
+  const ModelView &p = ad->model->view;
+  *h = p.do_h ? ad->X[s]->h : ad->X[0]->h;
+  *vn = p.do_vn ? ad->X[s]->vn : ad->X[0]->vn;
+  *tr = ad->X[s]->tr;
+}
+
+// Taped RK4 step from `cur`: X0 = cur, X1..X3 the stage inputs, and (when
+// `out` is given) the step's result.
+int tape_step(swg_adjoint ad, double dt, swg_state out, cudaStream_t st) {
+  swg_model md = ad->model;
+  const ModelView &pv = md->view;
+  static const double rka[3] = {1. / 2, 1. / 2, 1};
+  static const double rkb[4] = {1. / 6, 1. / 3, 1. / 3, 1. / 6};
+  TRY(swg_state_copy(ad->X[0], ad->cur, st));
+  swg_state S = ad->X[0];
+  const int last = out ? 3 : 2;
+  for (int s = 0; s <= last; ++s) {
+    StageArgs a{};
+    const double *h, *vn, *tr;
+    stage_ptrs(ad, s, &h, &vn, &tr);
+    a.h = h;
+    a.vn = vn;
+    a.tr = tr;
+    swg_state o = s < 3 ? ad->X[s + 1] : out;
+    a.fh = {nullptr, S->h, ad->acc->h, o->h};
+    a.fvn = {nullptr, S->vn, ad->acc->vn, o->vn};
+    a.ftr = {nullptr, S->tr, ad->acc->tr, o->tr};
+    const int mode = s == 0 ? EPI_RK4_FIRST : (s < 3 ? EPI_RK4_MID : EPI_RK4_LAST);
+    a.ep = {mode, 0.0, dt * rkb[s], s < 3 ? dt * rka[s] : 0.0};
+    launch_tendency(md->mesh->view, pv, md->aux, a, st);
+  }
+  // a disabled field is not written by the stages: keep X_s meaningful
+  ++ad->taped_steps;
+  cudaError_t err = cudaGetLastError();
+  return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_adjoint: taped step");
+}
+
+// lam <- adjoint of the taped step applied to lam
+int adjoint_step(swg_adjoint ad, double dt, cudaStream_t st) {
+  static const double rka[3] = {1. / 2, 1. / 2, 1};
+  static const double rkb[4] = {1. / 6, 1. / 3, 1. / 3, 1. / 6};
+  const long long n = (long long)words(ad->model);
+  cudaError_t err = cudaMemcpyAsync(ad->lacc->h, ad->lam->h, n * 8,
+                                    cudaMemcpyDeviceToDevice, st);
+  if (err != cudaSuccess)
+    return cuda_fail(err, "swg_adjoint: copy");
+  for (int s = 3; s >= 0; --s) {
+    if (s == 3)
+      lincomb(ad->mu, ad->lam, nullptr, dt * rkb[3], 0.0, n, st);
+    else
+      lincomb(ad->mu, ad->lam, ad->lX, dt * rkb[s], dt * rka[s], n, st);
+    const double *h, *vn, *tr;
+    stage_ptrs(ad, s, &h, &vn, &tr);
+    adj_tendency(ad, h, vn, tr, ad->mu, ad->lX, st);
+    addto(ad->lacc, ad->lX, n, st);
+  }
+  err = cudaMemcpyAsync(ad->lam->h, ad->lacc->h, n * 8,
+                        cudaMemcpyDeviceToDevice, st);
+  if (err == cudaSuccess)
+    err = cudaGetLastError();
+  return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_adjoint: adjoint step");
+}
+
+// ---- binomial schedule
+struct Planner {
+  int N, S;
+  std::vector<long long> cost; // (n, s) -> plain advances; n in [0,N], s in [0,S]
+  std::vector<int> split;
+  long long &C(int n, int s) { return cost[size_t(n) * (S + 1) + s]; }
+  int &M(int n, int s) { return split[size_t(n) * (S + 1) + s]; }
+  Planner(int n, int s) : N(n), S(s), cost(size_t(n + 1) * (s + 1), 0),
+                          split(size_t(n + 1) * (s + 1), 0) {
+    for (int nn = 1; nn <= N; ++nn) {
+      C(nn, 0) = (long long)nn * (nn - 1) / 2;
+      for (int ss = 1; ss <= S; ++ss) {
+        if (nn == 1) {
+          C(nn, ss) = 0;
+          continue;
+        }
+        long long best = -1;
+        int bm = 1;
+        for (int m = 1; m < nn; ++m) {
+          const long long c = m + C(nn - m, ss - 1) + C(m, ss);
+          if (best < 0 || c < best) {
+            best = c;
+            bm = m;
+          }
+        }
+        C(nn, ss) = best;
+        M(nn, ss) = bm;
+      }
+    }
+  }
+  // reverse steps [i0, i0+n) with x_{i0} in `cur` and in slot `slot`;
+  // `s` further slots free (slot+1 ...)
+  void gen(std::vector<AdjAction> &out, int i0, int n, int s, int slot,
+           bool cur_ok) {
+    if (n == 1) {
+      if (!cur_ok)
+        out.push_back({2, slot, 0});
+      out.push_back({3, i0, 0});
+      return;
+    }
+    if (s == 0) {
+      for (int j = n - 1; j >= 0; --j) {
+        if (!cur_ok || j < n - 1)
+          out.push_back({2, slot, 0});
+        if (j > 0)
+          out.push_back({0, i0, j});
+        out.push_back({3, i0 + j, 0});
+      }
+      return;
+    }
+    const int m = M(n, s);
+    if (!cur_ok)
+      out.push_back({2, slot, 0});
+    out.push_back({0, i0, m});
+    out.push_back({1, slot + 1, 0});
+    gen(out, i0 + m, n - m, s - 1, slot + 1, true);
+    gen(out, i0, m, s, slot, false);
+  }
+};
+
+int run_action(swg_adjoint ad, const AdjAction &a, cudaStream_t st) {
+  switch (a.type) {
+  case 0:
+    ad->plain_steps += a.b;
+    return swg_step(ad->stepper, ad->cur, ad->t0 + a.a * ad->dt, ad->dt, a.b,
+                    1, st);
+  case 1:
+    return swg_state_copy(ad->snaps[a.a], ad->cur, st);
+  case 2:
+    return swg_state_copy(ad->cur, ad->snaps[a.a], st);
+  default:
+    TRY(tape_step(ad, ad->dt, nullptr, st));
+    return adjoint_step(ad, ad->dt, st);
+  }
+}
+
+int check_model(swg_model md) {
+  if (!md)
+    return fail(SWG_ERR_ARG, "swg_adjoint: NULL model");
+  if (md->forcing)
+    return fail(SWG_ERR_ARG, "swg_adjoint: models with an additional_tendency "
+                             "hook are not differentiated");
+  if (md->mesh->view.mask)
+    return fail(SWG_ERR_ARG, "swg_adjoint: edge_mask other than ones is not "
+                             "supported");
+  if (md->mesh->view.dv4_differs)
+    return fail(SWG_ERR_ARG, "swg_adjoint: meshes with dv < dc/4 are not "
+                             "supported");
+  return SWG_OK;
+}
+
+} // namespace
+
+extern "C" int swg_adjoint_destroy(swg_adjoint ad);
+
+extern "C" int swg_adjoint_create(swg_model md, int nsnapshots,
+                                  swg_adjoint *out) {
+  if (!out || nsnapshots < 1)
+    return fail(SWG_ERR_ARG, "swg_adjoint_create: bad argument");
+  *out = nullptr;
+  TRY(check_model(md));
+  swg_adjoint ad = new (std::nothrow) swg_adjoint_s();
+  if (!ad)
+    return fail(SWG_ERR_OOM, "swg_adjoint_create: host allocation");
+  ad->model = md;
+  ad->nsnap = nsnapshots;
+  const int T = md->params.ntracers;
+  const size_t C = md->mesh->ncells, E = md->mesh->nedges,
+               V = md->mesh->nvertices, K = md->mesh->nlayers;
+  int rc = build_tables(ad);
+  auto &A = ad->allocs;
+  AdjWork &w = ad->aw;
+  if (rc == SWG_OK &&
+      ((rc = zal(A, T * C * K, &w.lL)) || (rc = zal(A, T * C * K, &w.ln)) ||
+       (rc = zal(A, C * K, &w.lke)) || (rc = zal(A, C * K, &w.ld4)) ||
+       (rc = zal(A, C * K, &w.lhs)) || (rc = zal(A, C * K, &w.lhtr)) ||
+       (rc = zal(A, C * K, &w.ldiv)) || (rc = zal(A, V * K, &w.lz4)) ||
+       (rc = zal(A, V * K, &w.lzeta)) || (rc = zal(A, V * K, &w.lhv)) ||
+       (rc = zal(A, E * K, &w.lQ)) || (rc = zal(A, E * K, &w.lmh)) ||
+       (rc = zal(A, E * K, &w.lvnp)) || (rc = zal(A, E * K, &w.ld2u))))
+    ;
+  swg_state *st[] = {&ad->cur, &ad->next, &ad->X[0], &ad->X[1], &ad->X[2],
+                     &ad->X[3], &ad->acc, &ad->lam, &ad->lacc, &ad->mu,
+                     &ad->lX};
+  for (auto *p : st)
+    if (rc == SWG_OK)
+      rc = swg_state_create(md->mesh, T, p);
+  for (int s = 0; s < nsnapshots && rc == SWG_OK; ++s) {
+    swg_state x = nullptr;
+    rc = swg_state_create(md->mesh, T, &x);
+    ad->snaps.push_back(x);
+  }
+  if (rc == SWG_OK)
+    rc = swg_stepper_create(md, SWG_STEPPER_RK4, 4, &ad->stepper);
+  const size_t n = words(md);
+  if (rc == SWG_OK && ((rc = alloc_dual_aux(ad)) || (rc = zal(A, n, &ad->dS)) ||
+                       (rc = zal(A, n, &ad->dacc)) || (rc = zal(A, n, &ad->dP0)) ||
+                       (rc = zal(A, n, &ad->dP1)) || (rc = zal(A, n, &ad->dT))))
+    ;
+  if (rc != SWG_OK) {
+    swg_adjoint_destroy(ad);
+    return rc;
+  }
+  *out = ad;
+  return SWG_OK;
+}
+
+extern "C" int swg_adjoint_destroy(swg_adjoint ad) {
+  if (!ad)
+    return SWG_OK;
+  swg_stepper_destroy(ad->stepper);
+  swg_state st[] = {ad->cur, ad->next, ad->X[0], ad->X[1], ad->X[2], ad->X[3],
+                    ad->acc, ad->lam, ad->lacc, ad->mu, ad->lX};
+  for (auto s : st)
+    swg_state_destroy(s);
+  for (auto s : ad->snaps)
+    swg_state_destroy(s);
+  for (void *p : ad->allocs)
+    cudaFree(p);
+  delete ad;
+  return SWG_OK;
+}
+
+static bool same_layout(swg_adjoint ad, swg_state s) {
+  return s && s->mesh == ad->model->mesh &&
+         s->ntracers == ad->model->params.ntracers;
+}
+
+extern "C" int swg_adj_tendency(swg_adjoint ad, swg_state x, swg_state mu,
+                                swg_state lambda_out, void *stream) {
+  if (!ad || !same_layout(ad, x) || !same_layout(ad, mu) ||
+      !same_layout(ad, lambda_out))
+    return fail(SWG_ERR_ARG, "swg_adj_tendency: bad argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  adj_tendency(ad, x->h, x->vn, x->tr, mu, lambda_out, st);
+  cudaError_t err = cudaGetLastError();
+  return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_adj_tendency");
+}
+
+extern "C" int swg_tlm_tendency(swg_adjoint ad, swg_state x, swg_state dx,
+                                swg_state dtend_out, void *stream) {
+  if (!ad || !same_layout(ad, x) || !same_layout(ad, dx) ||
+      !same_layout(ad, dtend_out))
+    return fail(SWG_ERR_ARG, "swg_tlm_tendency: bad argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  swg_model md = ad->model;
+  const long long n = (long long)words(md);
+  ka_pack<<<nb(n), ATPB, 0, st>>>(ad->dS, x->h, dx->h, n);
+  ++g_launches;
+  const size_t CKn = size_t(md->mesh->ncells) * md->mesh->nlayers;
+  const size_t EKn = size_t(md->mesh->nedges) * md->mesh->nlayers;
+  StageArgsT<Dual> a{};
+  a.h = ad->dS;
+  a.vn = ad->dS + CKn;
+  a.tr = ad->dS + CKn + EKn;
+  a.fh.tend = ad->dT;
+  a.fvn.tend = ad->dT + CKn;
+  a.ftr.tend = ad->dT + CKn + EKn;
+  a.ep.mode = EPI_REPLACE;
+  // fields whose tendency is disabled stay untouched: start from zero
+  cudaMemsetAsync(ad->dT, 0, n * sizeof(Dual), st);
+  launch_tendency_dual(md->mesh->view, md->view, ad->daux, a, st);
+  ka_unpack<<<nb(n), ATPB, 0, st>>>(nullptr, dtend_out->h, ad->dT, n);
+  g_launches += 2;
+  cudaError_t err = cudaGetLastError();
+  return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_tlm_tendency");
+}
+
+extern "C" int swg_tlm_apply(swg_adjoint ad, swg_state x0, swg_state dx,
+                             double t0, double dt, int nsteps, void *stream) {
+  (void)t0;
+  if (!ad || !same_layout(ad, x0) || !same_layout(ad, dx) || nsteps < 0)
+    return fail(SWG_ERR_ARG, "swg_tlm_apply: bad argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  swg_model md = ad->model;
+  const ModelView &pv = md->view;
+  const long long n = (long long)words(md);
+  const size_t CKn = size_t(md->mesh->ncells) * md->mesh->nlayers;
+  const size_t EKn = size_t(md->mesh->nedges) * md->mesh->nlayers;
+  ka_pack<<<nb(n), ATPB, 0, st>>>(ad->dS, x0->h, dx->h, n);
+  ++g_launches;
+  static const double rka[3] = {1. / 2, 1. / 2, 1};
+  static const double rkb[4] = {1. / 6, 1. / 3, 1. / 3, 1. / 6};
+  Dual *S = ad->dS, *A = ad->dacc, *P[2] = {ad->dP0, ad->dP1};
+  auto fio = [&](Dual *base, size_t off) { return base ? base + off : nullptr; };
+  for (int step = 0; step < nsteps; ++step) {
+    Dual *in = S;
+    for (int s = 0; s < 4; ++s) {
+      Dual *o = s < 3 ? P[s % 2] : S;
+      StageArgsT<Dual> a{};
+      a.h = pv.do_h ? in : S;
+      a.vn = (pv.do_vn ? in : S) + CKn;
+      a.tr = in + CKn + EKn;
+      a.fh = {nullptr, S, A, o};
+      a.fvn = {nullptr, fio(S, CKn), fio(A, CKn), fio(o, CKn)};
+      a.ftr = {nullptr, fio(S, CKn + EKn), fio(A, CKn + EKn), fio(o, CKn + EKn)};
+      const int mode = s == 0 ? EPI_RK4_FIRST : (s < 3 ? EPI_RK4_MID : EPI_RK4_LAST);
+      a.ep = {mode, 0.0, dt * rkb[s], s < 3 ? dt * rka[s] : 0.0};
+      launch_tendency_dual(md->mesh->view, pv, ad->daux, a, st);
+      in = o;
+    }
+  }
+  ka_unpack<<<nb(n), ATPB, 0, st>>>(nullptr, dx->h, S, n);
+  ++g_launches;
+  cudaError_t err = cudaGetLastError();
+  return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_tlm_apply");
+}
+
+extern "C" int swg_adj_forward(swg_adjoint ad, swg_state state0, double t0,
+                               double dt, int nsteps, swg_state final_out,
+                               void *stream) {
+  if (!ad || !same_layout(ad, state0) || !same_layout(ad, final_out) ||
+      nsteps < 1)
+    return fail(SWG_ERR_ARG, "swg_adj_forward: bad argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  ad->t0 = t0;
+  ad->dt = dt;
+  ad->nsteps = nsteps;
+  ad->plain_steps = ad->taped_steps = 0;
+  ad->actions.clear();
+  Planner pl(nsteps, ad->nsnap - 1);
+  ad->actions.push_back({1, 0, 0});
+  pl.gen(ad->actions, 0, nsteps, ad->nsnap - 1, 0, true);
+  TRY(swg_state_copy(ad->cur, state0, st));
+  // execute up to the first tape+adjoint action: that is step nsteps-1
+  size_t i = 0;
+  for (; i < ad->actions.size() && ad->actions[i].type != 3; ++i)
+    TRY(run_action(ad, ad->actions[i], st));
+  if (i == ad->actions.size() || ad->actions[i].a != nsteps - 1)
+    return fail(SWG_ERR_STATE, "swg_adj_forward: unexpected schedule");
+  TRY(tape_step(ad, dt, ad->next, st));
+  TRY(swg_state_copy(final_out, ad->next, st));
+  ad->pos = i;
+  ad->state = 1;
+  return SWG_OK;
+}
+
+extern "C" int swg_adj_backward(swg_adjoint ad, swg_state lambda,
+                                void *stream) {
+  if (!ad || !same_layout(ad, lambda))
+    return fail(SWG_ERR_ARG, "swg_adj_backward: bad argument");
+  if (ad->state != 1)
+    return fail(SWG_ERR_STATE, "swg_adj_backward: call swg_adj_forward first");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  TRY(swg_state_copy(ad->lam, lambda, st));
+  // the last step is already taped
+  TRY(adjoint_step(ad, ad->dt, st));
+  for (size_t i = ad->pos + 1; i < ad->actions.size(); ++i)
+    TRY(run_action(ad, ad->actions[i], st));
+  TRY(swg_state_copy(lambda, ad->lam, st));
+  ad->state = 0;
+  return SWG_OK;
+}
+
+extern "C" int swg_adj_info(swg_adjoint ad, long long *plain_steps,
+                            long long *taped_steps) {
+  if (!ad)
+    return fail(SWG_ERR_ARG, "swg_adj_info: NULL");
+  if (plain_steps)
+    *plain_steps = ad->plain_steps;
+  if (taped_steps)
+    *taped_steps = ad->taped_steps;
+  return SWG_OK;
+}
+
+extern "C" long long swg_checkpoint_cost(int nsteps, int nsnapshots) {
+  if (nsteps < 1 || nsnapshots < 1)
+    return -1;
+  Planner pl(nsteps, nsnapshots - 1);
+  return pl.C(nsteps, nsnapshots - 1);
+}

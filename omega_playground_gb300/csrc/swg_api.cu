@@ -234,6 +234,19 @@ extern "C" int swg_mesh_create(const swg_mesh_desc *d, swg_mesh *out) {
   m->ckq_h = ckq;
   m->ec_h = ec;
   m->inv_dc_h = inv_dc;
+  m->ev_h.assign(d->edges_on_vertex, d->edges_on_vertex + 3 * V);
+  m->cv_h.assign(d->cells_on_vertex, d->cells_on_vertex + 3 * V);
+  m->ce_h.assign(d->cells_on_edge, d->cells_on_edge + 2 * E);
+  m->ve_h.assign(d->vertices_on_edge, d->vertices_on_edge + 2 * E);
+  m->nbc_h = nbc;
+  m->eoe_h = eoe;
+  m->cvr_h = cvr;
+  m->kvh_h = kvh;
+  m->ccd_h = ccd;
+  m->cke_h = cke;
+  m->ccdh_h = ccdh;
+  m->inv_dv_h = inv_dv;
+  m->woe_h = woe;
   bool mask_ones = true;
   if (d->edge_mask)
     for (long long i = 0; i < E * K && mask_ones; ++i)

@@ -89,7 +89,7 @@ __device__ __forceinline__ void run_pass(int pass, const Member &M, int stage,
   case P_CELL1: pt_cell1(M.m, M.p, M.a, s.h, s.vn, s.tr, i); break;
   case P_EDGE1: pt_edge1(M.m, M.p, M.a, s.h, s.vn, i); break;
   case P_AUX2: pt_aux2(M.m, M.p, M.a, M.aux2_base + i); break;
-  case P_EDGE_FINAL: pt_edge_final<NE>(M.m, M.p, M.a, s, i); break;
+  case P_EDGE_FINAL: pt_edge_final<NE, double>(M.m, M.p, M.a, s, i); break;
   default: pt_cell_final(M.m, M.p, M.a, s, i); break;
   }
 }

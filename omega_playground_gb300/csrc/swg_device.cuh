@@ -9,6 +9,30 @@
 
 namespace swg {
 
+// Forward-mode dual number (value, tangent): the pass functions instantiated
+// with it are the exact tangent-linear model of the double instantiation
+// (the value part runs the identical operation sequence).
+using ::fma; // keep the double overload visible beside the Dual ones
+__device__ __forceinline__ Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+__device__ __forceinline__ Dual operator+(Dual a, double b) { return {a.v + b, a.d}; }
+__device__ __forceinline__ Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+__device__ __forceinline__ Dual operator-(Dual a) { return {-a.v, -a.d}; }
+__device__ __forceinline__ Dual operator*(Dual a, Dual b) {
+  return {a.v * b.v, fma(a.d, b.v, a.v * b.d)};
+}
+__device__ __forceinline__ Dual operator*(double a, Dual b) { return {a * b.v, a * b.d}; }
+__device__ __forceinline__ Dual operator*(Dual a, double b) { return {a.v * b, a.d * b}; }
+__device__ __forceinline__ Dual &operator+=(Dual &a, Dual b) { a = a + b; return a; }
+__device__ __forceinline__ Dual fma(double a, Dual b, Dual c) {
+  return {::fma(a, b.v, c.v), ::fma(a, b.d, c.d)};
+}
+__device__ __forceinline__ Dual fma(Dual a, double b, Dual c) {
+  return {::fma(a.v, b, c.v), ::fma(a.d, b, c.d)};
+}
+__device__ __forceinline__ Dual fma(Dual a, Dual b, Dual c) {
+  return {::fma(a.v, b.v, c.v), ::fma(a.d, b.v, ::fma(a.v, b.d, c.d))};
+}
+
 // 1/x: hardware estimate refined by two Newton-Raphson steps
 // r <- r + r (1 - x r); each step squares the relative error of the estimate.
 __device__ __forceinline__ double rcp_nr(double x) {
@@ -19,9 +43,14 @@ __device__ __forceinline__ double rcp_nr(double x) {
   e = fma(-x, r, 1.0);
   return fma(r, e, r);
 }
+__device__ __forceinline__ Dual rcp_nr(Dual x) {
+  const double r = rcp_nr(x.v);
+  return {r, -(r * r) * x.d};
+}
 
-__device__ __forceinline__ void epilogue(const Epilogue &ep, const FieldIO &f,
-                                         size_t i, double x) {
+template <class T>
+__device__ __forceinline__ void epilogue(const Epilogue &ep,
+                                         const FieldIOT<T> &f, size_t i, T x) {
   switch (ep.mode) {
   case EPI_REPLACE:
     f.tend[i] = x;
@@ -30,12 +59,12 @@ __device__ __forceinline__ void epilogue(const Epilogue &ep, const FieldIO &f,
     f.tend[i] += x;
     break;
   case EPI_LSRK: {
-    const double t = fma(ep.a, f.tend[i], x);
+    const T t = fma(ep.a, f.tend[i], x);
     f.tend[i] = t;
     f.out[i] = fma(ep.dtb, t, f.out[i]);
   } break;
   case EPI_RK4_FIRST: {
-    const double s = f.old[i];
+    const T s = f.old[i];
     f.acc[i] = fma(ep.dtb, x, s);
     f.out[i] = fma(ep.dta, x, s);
   } break;
@@ -50,13 +79,13 @@ __device__ __forceinline__ void epilogue(const Epilogue &ep, const FieldIO &f,
 }
 
 // Vertex pass: relative vorticity and (rvort + f) / h_vertex.
+template <class T>
 __device__ __forceinline__ void
-pt_vertex(const MeshView &m, const ModelView &p, const AuxView &a,
-          const double *__restrict__ h, const double *__restrict__ vn,
-          unsigned i) {
+pt_vertex(const MeshView &m, const ModelView &p, const AuxViewT<T> &a,
+          const T *__restrict__ h, const T *__restrict__ vn, unsigned i) {
   const int K = m.nlayers;
   const int v = int(i / unsigned(K)), k = int(i - unsigned(v) * unsigned(K));
-  double z, hv;
+  T z, hv;
   {
     const int e = __ldg(m.ev + 3 * v), c = __ldg(m.cv + 3 * v);
     z = __ldg(m.cvr + 3 * v) * vn[size_t(e) * K + k];
@@ -75,15 +104,16 @@ pt_vertex(const MeshView &m, const ModelView &p, const AuxView &a,
 
 // Cell pass 1: velocity divergence (for the dissipation terms) and the
 // normalised tracers tr / h.
+template <class T>
 __device__ __forceinline__ void
-pt_cell1(const MeshView &m, const ModelView &p, const AuxView &a,
-         const double *__restrict__ h, const double *__restrict__ vn,
-         const double *__restrict__ tr, unsigned i) {
+pt_cell1(const MeshView &m, const ModelView &p, const AuxViewT<T> &a,
+         const T *__restrict__ h, const T *__restrict__ vn,
+         const T *__restrict__ tr, unsigned i) {
   const int K = m.nlayers;
   const unsigned CK = unsigned(m.ncells) * unsigned(K);
   const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * unsigned(K));
   if (p.do_vn && (p.vel_del2 | p.vel_del4)) {
-    double dv = __ldg(m.ccd + 6 * c) * vn[size_t(__ldg(m.ec + 6 * c)) * K + k];
+    T dv = __ldg(m.ccd + 6 * c) * vn[size_t(__ldg(m.ec + 6 * c)) * K + k];
 #pragma unroll
     for (int j = 1; j < MAXE; ++j)
       dv = fma(__ldg(m.ccd + 6 * c + j),
@@ -91,7 +121,7 @@ pt_cell1(const MeshView &m, const ModelView &p, const AuxView &a,
     a.div[i] = dv;
   }
   if (p.ntracers > 0) {
-    const double r = rcp_nr(h[i]);
+    const T r = rcp_nr(h[i]);
     for (int l = 0; l < p.ntracers; ++l) {
       const size_t t = size_t(l) * CK + i;
       a.ntr[t] = tr[t] * r;
@@ -101,28 +131,28 @@ pt_cell1(const MeshView &m, const ModelView &p, const AuxView &a,
 
 // Edge pass 1: mean thickness, thickness flux F = mean_h vn, vn^2, edge PV
 // sum Q = q(v0) + q(v1), G = F Q, and the edge Laplacian of the velocity.
+template <class T>
 __device__ __forceinline__ void
-pt_edge1(const MeshView &m, const ModelView &p, const AuxView &a,
-         const double *__restrict__ h, const double *__restrict__ vn,
-         unsigned i) {
+pt_edge1(const MeshView &m, const ModelView &p, const AuxViewT<T> &a,
+         const T *__restrict__ h, const T *__restrict__ vn, unsigned i) {
   const int K = m.nlayers;
   const int e = int(i / unsigned(K)), k = int(i - unsigned(e) * unsigned(K));
   const int c0 = __ldg(m.ce + 2 * e), c1 = __ldg(m.ce + 2 * e + 1);
-  const double mh = 0.5 * (h[size_t(c0) * K + k] + h[size_t(c1) * K + k]);
-  const double u = vn[i];
-  const double F = mh * u;
+  const T mh = 0.5 * (h[size_t(c0) * K + k] + h[size_t(c1) * K + k]);
+  const T u = vn[i];
+  const T F = mh * u;
   a.F[i] = F;
   if (p.ntracers > 0 && (p.tr_del2 | p.tr_del4))
     a.mh[i] = mh;
   if (p.do_vn) {
     const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
-    const double Q = a.q[size_t(v0) * K + k] + a.q[size_t(v1) * K + k];
+    const T Q = a.q[size_t(v0) * K + k] + a.q[size_t(v1) * K + k];
     a.Q[i] = Q;
     a.G[i] = F * Q;
     a.u2[i] = u * u;
     if (p.vel_del2 | p.vel_del4) {
-      const double dd = a.div[size_t(c1) * K + k] - a.div[size_t(c0) * K + k];
-      const double dz = a.zeta[size_t(v1) * K + k] - a.zeta[size_t(v0) * K + k];
+      const T dd = a.div[size_t(c1) * K + k] - a.div[size_t(c0) * K + k];
+      const T dz = a.zeta[size_t(v1) * K + k] - a.zeta[size_t(v0) * K + k];
       const double idc = __ldg(m.inv_dc + e);
       a.d2u[i] = fma(dd, idc, -(dz * __ldg(m.inv_dv + e)));
       if (p.vel_del4 && m.dv4_differs)
@@ -135,8 +165,9 @@ pt_edge1(const MeshView &m, const ModelView &p, const AuxView &a,
 // divergence (cells) of the edge Laplacian, and the thickness-weighted
 // tracer Laplacian L (cells).  The first V*K threads take vertices, the
 // rest cells.
+template <class T>
 __device__ __forceinline__ void pt_aux2(const MeshView &m, const ModelView &p,
-                                        const AuxView &a, unsigned i) {
+                                        const AuxViewT<T> &a, unsigned i) {
   const int K = m.nlayers;
   const unsigned VK = unsigned(m.nvertices) * unsigned(K);
   const unsigned CK = unsigned(m.ncells) * unsigned(K);
@@ -145,7 +176,7 @@ __device__ __forceinline__ void pt_aux2(const MeshView &m, const ModelView &p,
     if (!vel)
       return;
     const int v = int(i / unsigned(K)), k = int(i - unsigned(v) * unsigned(K));
-    double z = __ldg(m.cvr + 3 * v) * a.d2u4[size_t(__ldg(m.ev + 3 * v)) * K + k];
+    T z = __ldg(m.cvr + 3 * v) * a.d2u4[size_t(__ldg(m.ev + 3 * v)) * K + k];
 #pragma unroll
     for (int j = 1; j < 3; ++j)
       z = fma(__ldg(m.cvr + 3 * v + j),
@@ -159,7 +190,7 @@ __device__ __forceinline__ void pt_aux2(const MeshView &m, const ModelView &p,
   const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * unsigned(K));
   if (p.do_vn) {
     // ke = sum_j dv dc / (4 area) vn_j^2
-    double ke = __ldg(m.cke + 6 * c) * a.u2[size_t(__ldg(m.ec + 6 * c)) * K + k];
+    T ke = __ldg(m.cke + 6 * c) * a.u2[size_t(__ldg(m.ec + 6 * c)) * K + k];
 #pragma unroll
     for (int j = 1; j < MAXE; ++j)
       ke = fma(__ldg(m.cke + 6 * c + j),
@@ -167,7 +198,7 @@ __device__ __forceinline__ void pt_aux2(const MeshView &m, const ModelView &p,
     a.ke[i] = ke;
   }
   if (vel) {
-    double d = __ldg(m.ccd + 6 * c) * a.d2u4[size_t(__ldg(m.ec + 6 * c)) * K + k];
+    T d = __ldg(m.ccd + 6 * c) * a.d2u4[size_t(__ldg(m.ec + 6 * c)) * K + k];
 #pragma unroll
     for (int j = 1; j < MAXE; ++j)
       d = fma(__ldg(m.ccd + 6 * c + j),
@@ -176,7 +207,7 @@ __device__ __forceinline__ void pt_aux2(const MeshView &m, const ModelView &p,
   }
   if (p.ntracers > 0 && p.tr_del4) {
     // L = sum_j w_j (n_nb - n_c), w_j = ckq_j mean_h_j
-    double w[MAXE], M;
+    T w[MAXE], M;
     int nb[MAXE];
 #pragma unroll
     for (int j = 0; j < MAXE; ++j) {
@@ -188,8 +219,8 @@ __device__ __forceinline__ void pt_aux2(const MeshView &m, const ModelView &p,
     for (int j = 2; j < MAXE; ++j)
       M += w[j];
     for (int l = 0; l < p.ntracers; ++l) {
-      const double *n = a.ntr + size_t(l) * CK;
-      double acc = w[0] * n[size_t(nb[0]) * K + k];
+      const T *n = a.ntr + size_t(l) * CK;
+      T acc = w[0] * n[size_t(nb[0]) * K + k];
 #pragma unroll
       for (int j = 1; j < MAXE; ++j)
         acc = fma(w[j], n[size_t(nb[j]) * K + k], acc);
@@ -200,15 +231,16 @@ __device__ __forceinline__ void pt_aux2(const MeshView &m, const ModelView &p,
 
 // Edge final pass: normal-velocity tendency (PV flux, Bernoulli gradient,
 // del2 and del4 dissipation) and its stage update.
-template <int NE>
+template <int NE, class T>
 __device__ __forceinline__ void pt_edge_final(const MeshView &m,
                                               const ModelView &p,
-                                              const AuxView &a,
-                                              const StageArgs &s, unsigned i) {
+                                              const AuxViewT<T> &a,
+                                              const StageArgsT<T> &s,
+                                              unsigned i) {
   const int K = m.nlayers;
   const int e = int(i / unsigned(K)), k = int(i - unsigned(e) * unsigned(K));
   // potential-vorticity flux: sum_j w_j F_j (Q_e + Q_j) / 4 with w/4 in woe
-  double S1, S2;
+  T S1, S2;
   {
     const int je = __ldg(m.eoe + NE * e);
     const double w = __ldg(m.woe + NE * e);
@@ -222,7 +254,7 @@ __device__ __forceinline__ void pt_edge_final(const MeshView &m,
     S1 = fma(w, a.F[size_t(je) * K + k], S1);
     S2 = fma(w, a.G[size_t(je) * K + k], S2);
   }
-  double t = fma(a.Q[i], S1, S2);
+  T t = fma(a.Q[i], S1, S2);
   const int c0 = __ldg(m.ce + 2 * e), c1 = __ldg(m.ce + 2 * e + 1);
   const double idc = __ldg(m.inv_dc + e);
   // kinetic-energy and sea-surface-height gradients (the differences are
@@ -235,9 +267,9 @@ __device__ __forceinline__ void pt_edge_final(const MeshView &m,
     t = fma(m.mask ? __ldg(p.c2e + e) * mk : __ldg(p.c2e + e), a.d2u[i], t);
   if (p.vel_del4) {
     const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
-    const double dd = a.d4[size_t(c1) * K + k] - a.d4[size_t(c0) * K + k];
-    const double dz = a.z4[size_t(v1) * K + k] - a.z4[size_t(v0) * K + k];
-    const double l = fma(dd, idc, -(dz * __ldg(m.inv_dv + e)));
+    const T dd = a.d4[size_t(c1) * K + k] - a.d4[size_t(c0) * K + k];
+    const T dz = a.z4[size_t(v1) * K + k] - a.z4[size_t(v0) * K + k];
+    const T l = fma(dd, idc, -(dz * __ldg(m.inv_dv + e)));
     t = fma(m.mask ? __ldg(p.c4e + e) * mk : __ldg(p.c4e + e), l, t);
   }
   epilogue(s.ep, s.fvn, i, t);
@@ -245,16 +277,17 @@ __device__ __forceinline__ void pt_edge_final(const MeshView &m,
 
 // Cell final pass: thickness tendency and tracer tendencies (advection,
 // del2, del4) with their stage updates.
+template <class T>
 __device__ __forceinline__ void pt_cell_final(const MeshView &m,
                                               const ModelView &p,
-                                              const AuxView &a,
-                                              const StageArgs &s,
+                                              const AuxViewT<T> &a,
+                                              const StageArgsT<T> &s,
                                               unsigned i) {
   const int K = m.nlayers;
   const unsigned CK = unsigned(m.ncells) * unsigned(K);
   const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * unsigned(K));
   // a_j = -F_j ccd_j / 2: half the flux divergence weight of edge j
-  double w[MAXE], Sa;
+  T w[MAXE], Sa;
   int ej[MAXE];
 #pragma unroll
   for (int j = 0; j < MAXE; ++j) {
@@ -270,9 +303,9 @@ __device__ __forceinline__ void pt_cell_final(const MeshView &m,
   if (p.ntracers == 0)
     return;
   // advection + del2: sum_j a_j (n_c + n_j) + b_j (n_j - n_c)
-  double wc = Sa;
+  T wc = Sa;
   if (p.tr_del2) {
-    double b[MAXE], Sb;
+    T b[MAXE], Sb;
 #pragma unroll
     for (int j = 0; j < MAXE; ++j) {
       b[j] = __ldg(p.kd2 + 6 * c + j) * a.mh[size_t(ej[j]) * K + k];
@@ -290,13 +323,13 @@ __device__ __forceinline__ void pt_cell_final(const MeshView &m,
     nb[j] = __ldg(m.nbc + 6 * c + j);
   for (int l = 0; l < p.ntracers; ++l) {
     const size_t base = size_t(l) * CK;
-    const double *n = a.ntr + base;
-    double acc = wc * n[i];
+    const T *n = a.ntr + base;
+    T acc = wc * n[i];
 #pragma unroll
     for (int j = 0; j < MAXE; ++j)
       acc = fma(w[j], n[size_t(nb[j]) * K + k], acc);
     if (p.tr_del4) {
-      const double *L = a.lap + base;
+      const T *L = a.lap + base;
       acc = fma(-__ldg(p.r4sum + c), L[i], acc);
 #pragma unroll
       for (int j = 0; j < MAXE; ++j)

@@ -69,13 +69,22 @@ struct ModelView {
   int vel_del2, vel_del4, tr_del2, tr_del4, do_h, do_vn;
 };
 
-// Intermediate fields of one tendency evaluation (device).
-struct AuxView {
-  double *q, *zeta, *z4;          // [V][K]
-  double *div, *ke, *d4;          // [C][K]
-  double *ntr, *lap;              // [T][C][K]
-  double *F, *G, *Q, *mh, *u2, *d2u, *d2u4; // [E][K]
+// Forward-mode dual number (value, tangent) of the tangent-linear model;
+// its device arithmetic is in swg_device.cuh.
+struct Dual {
+  double v, d;
 };
+
+// Intermediate fields of one tendency evaluation (device), templated on
+// the value type: double, or Dual (value + tangent) for the tangent-linear
+// model.
+template <class T> struct AuxViewT {
+  T *q, *zeta, *z4;              // [V][K]
+  T *div, *ke, *d4;              // [C][K]
+  T *ntr, *lap;                  // [T][C][K]
+  T *F, *G, *Q, *mh, *u2, *d2u, *d2u4; // [E][K]
+};
+using AuxView = AuxViewT<double>;
 
 enum EpiMode {
   EPI_REPLACE = 0,   // tend = x
@@ -86,26 +95,36 @@ enum EpiMode {
   EPI_RK4_LAST = 5,  // out = acc + dtb*x
 };
 
-struct FieldIO {
-  double *tend;      // REPLACE / INCREMENT / LSRK
-  const double *old; // RK4 first & mid: state at the start of the step
-  double *acc;       // RK4: accumulator
-  double *out;       // LSRK: state; RK4: next stage input or final state
+template <class T> struct FieldIOT {
+  T *tend;      // REPLACE / INCREMENT / LSRK
+  const T *old; // RK4 first & mid: state at the start of the step
+  T *acc;       // RK4: accumulator
+  T *out;       // LSRK: state; RK4: next stage input or final state
 };
+using FieldIO = FieldIOT<double>;
 
 struct Epilogue {
   int mode;
   double a, dtb, dta;
 };
 
-struct StageArgs {
-  const double *h, *vn, *tr; // stage input state
-  FieldIO fh, fvn, ftr;
+template <class T> struct StageArgsT {
+  const T *h, *vn, *tr; // stage input state
+  FieldIOT<T> fh, fvn, ftr;
   Epilogue ep;
 };
+using StageArgs = StageArgsT<double>;
 
 void launch_tendency(const MeshView &m, const ModelView &p, const AuxView &a,
                      const StageArgs &s, cudaStream_t st);
+// the same six passes on dual numbers (tangent-linear model)
+void launch_tendency_dual(const MeshView &m, const ModelView &p,
+                          const AuxViewT<Dual> &a, const StageArgsT<Dual> &s,
+                          cudaStream_t st);
+// only the four auxiliary passes (intermediates of the state h, vn, tr)
+void launch_aux(const MeshView &m, const ModelView &p, const AuxView &a,
+                const double *h, const double *vn, const double *tr,
+                cudaStream_t st);
 void launch_axpby(double *y, const double *x, const double *z, double alpha,
                   double beta, long long n, int kind, cudaStream_t st);
 // opt-in per-kernel CUDA-event timing (swg_profile_enable)
@@ -128,6 +147,9 @@ struct swg_mesh_s {
   // host copies of the per-edge scaling (the model scales them)
   std::vector<double> scale2_h, scale4_h, ckq_h, inv_dc_h;
   std::vector<int> ec_h;
+  // host copies of the derived tables (the adjoint builds transposes)
+  std::vector<int> ev_h, cv_h, nbc_h, ce_h, ve_h, eoe_h;
+  std::vector<double> cvr_h, kvh_h, ccd_h, cke_h, ccdh_h, inv_dv_h, woe_h;
 };
 
 struct swg_state_s {

@@ -39,51 +39,57 @@ namespace {
 
 constexpr int TPB = 256;
 
-// Single-instance kernels: one launch per pass over (entity, level).
+// Single-instance kernels: one launch per pass over (entity, level),
+// templated on the value type (double, or Dual for the tangent-linear model).
+template <class T>
 __global__ void __launch_bounds__(TPB)
-    k_vertex(MeshView m, ModelView p, AuxView a, const double *__restrict__ h,
-             const double *__restrict__ vn) {
+    k_vertex(MeshView m, ModelView p, AuxViewT<T> a, const T *__restrict__ h,
+             const T *__restrict__ vn) {
   const unsigned i = blockIdx.x * TPB + threadIdx.x;
   if (i < unsigned(m.nvertices) * unsigned(m.nlayers))
-    pt_vertex(m, p, a, h, vn, i);
+    pt_vertex<T>(m, p, a, h, vn, i);
 }
 
+template <class T>
 __global__ void __launch_bounds__(TPB)
-    k_cell1(MeshView m, ModelView p, AuxView a, const double *__restrict__ h,
-            const double *__restrict__ vn, const double *__restrict__ tr) {
+    k_cell1(MeshView m, ModelView p, AuxViewT<T> a, const T *__restrict__ h,
+            const T *__restrict__ vn, const T *__restrict__ tr) {
   const unsigned i = blockIdx.x * TPB + threadIdx.x;
   if (i < unsigned(m.ncells) * unsigned(m.nlayers))
-    pt_cell1(m, p, a, h, vn, tr, i);
+    pt_cell1<T>(m, p, a, h, vn, tr, i);
 }
 
+template <class T>
 __global__ void __launch_bounds__(TPB)
-    k_edge1(MeshView m, ModelView p, AuxView a, const double *__restrict__ h,
-            const double *__restrict__ vn) {
+    k_edge1(MeshView m, ModelView p, AuxViewT<T> a, const T *__restrict__ h,
+            const T *__restrict__ vn) {
   const unsigned i = blockIdx.x * TPB + threadIdx.x;
   if (i < unsigned(m.nedges) * unsigned(m.nlayers))
-    pt_edge1(m, p, a, h, vn, i);
+    pt_edge1<T>(m, p, a, h, vn, i);
 }
 
+template <class T>
 __global__ void __launch_bounds__(TPB)
-    k_aux2(MeshView m, ModelView p, AuxView a, unsigned base) {
+    k_aux2(MeshView m, ModelView p, AuxViewT<T> a, unsigned base) {
   const unsigned i = base + blockIdx.x * TPB + threadIdx.x;
   if (i < unsigned(m.nvertices + m.ncells) * unsigned(m.nlayers))
-    pt_aux2(m, p, a, i);
+    pt_aux2<T>(m, p, a, i);
 }
 
-template <int NE>
+template <int NE, class T>
 __global__ void __launch_bounds__(TPB)
-    k_edge_final(MeshView m, ModelView p, AuxView a, StageArgs s) {
+    k_edge_final(MeshView m, ModelView p, AuxViewT<T> a, StageArgsT<T> s) {
   const unsigned i = blockIdx.x * TPB + threadIdx.x;
   if (i < unsigned(m.nedges) * unsigned(m.nlayers))
-    pt_edge_final<NE>(m, p, a, s, i);
+    pt_edge_final<NE, T>(m, p, a, s, i);
 }
 
+template <class T>
 __global__ void __launch_bounds__(TPB)
-    k_cell_final(MeshView m, ModelView p, AuxView a, StageArgs s) {
+    k_cell_final(MeshView m, ModelView p, AuxViewT<T> a, StageArgsT<T> s) {
   const unsigned i = blockIdx.x * TPB + threadIdx.x;
   if (i < unsigned(m.ncells) * unsigned(m.nlayers))
-    pt_cell_final(m, p, a, s, i);
+    pt_cell_final<T>(m, p, a, s, i);
 }
 
 // Elementwise helpers for the unfused stepper path (forcing hook set).
@@ -218,40 +224,71 @@ int profile_read(int max_kernels, char *names, double *total_ms,
   return SWG_OK;
 }
 
-void launch_tendency(const MeshView &m, const ModelView &p, const AuxView &a,
-                     const StageArgs &s, cudaStream_t st) {
+namespace {
+
+template <class T>
+void launch_aux_t(const MeshView &m, const ModelView &p, const AuxViewT<T> &a,
+                  const T *h, const T *vn, const T *tr, cudaStream_t st) {
   const long long K = m.nlayers;
   const long long VK = m.nvertices * K, CK = m.ncells * K, EK = m.nedges * K;
   if (p.do_vn) {
     Scope sc("k_vertex", st);
-    k_vertex<<<nblocks(VK), TPB, 0, st>>>(m, p, a, s.h, s.vn);
+    k_vertex<T><<<nblocks(VK), TPB, 0, st>>>(m, p, a, h, vn);
   }
   if ((p.do_vn && (p.vel_del2 || p.vel_del4)) || p.ntracers > 0) {
     Scope sc("k_cell1", st);
-    k_cell1<<<nblocks(CK), TPB, 0, st>>>(m, p, a, s.h, s.vn, s.tr);
+    k_cell1<T><<<nblocks(CK), TPB, 0, st>>>(m, p, a, h, vn, tr);
   }
   if (p.do_vn || p.do_h || p.ntracers > 0) {
     Scope sc("k_edge1", st);
-    k_edge1<<<nblocks(EK), TPB, 0, st>>>(m, p, a, s.h, s.vn);
+    k_edge1<T><<<nblocks(EK), TPB, 0, st>>>(m, p, a, h, vn);
   }
   const bool tr4 = p.ntracers > 0 && p.tr_del4;
   if (p.do_vn || tr4) {
     Scope sc("k_aux2", st);
     // vertex threads only when the velocity del4 curl is needed
     const unsigned base = (p.do_vn && p.vel_del4) ? 0u : unsigned(VK);
-    k_aux2<<<nblocks(VK + CK - base), TPB, 0, st>>>(m, p, a, base);
+    k_aux2<T><<<nblocks(VK + CK - base), TPB, 0, st>>>(m, p, a, base);
   }
+}
+
+template <class T>
+void launch_tendency_t(const MeshView &m, const ModelView &p,
+                       const AuxViewT<T> &a, const StageArgsT<T> &s,
+                       cudaStream_t st) {
+  const long long K = m.nlayers;
+  const long long CK = m.ncells * K, EK = m.nedges * K;
+  launch_aux_t<T>(m, p, a, s.h, s.vn, s.tr, st);
   if (p.do_vn) {
     Scope sc("k_edge_final", st);
     if (m.ne == 8)
-      k_edge_final<8><<<nblocks(EK), TPB, 0, st>>>(m, p, a, s);
+      k_edge_final<8, T><<<nblocks(EK), TPB, 0, st>>>(m, p, a, s);
     else
-      k_edge_final<10><<<nblocks(EK), TPB, 0, st>>>(m, p, a, s);
+      k_edge_final<10, T><<<nblocks(EK), TPB, 0, st>>>(m, p, a, s);
   }
   if (p.do_h || p.ntracers > 0) {
     Scope sc("k_cell_final", st);
-    k_cell_final<<<nblocks(CK), TPB, 0, st>>>(m, p, a, s);
+    k_cell_final<T><<<nblocks(CK), TPB, 0, st>>>(m, p, a, s);
   }
+}
+
+} // namespace
+
+void launch_tendency(const MeshView &m, const ModelView &p, const AuxView &a,
+                     const StageArgs &s, cudaStream_t st) {
+  launch_tendency_t<double>(m, p, a, s, st);
+}
+
+void launch_tendency_dual(const MeshView &m, const ModelView &p,
+                          const AuxViewT<Dual> &a, const StageArgsT<Dual> &s,
+                          cudaStream_t st) {
+  launch_tendency_t<Dual>(m, p, a, s, st);
+}
+
+void launch_aux(const MeshView &m, const ModelView &p, const AuxView &a,
+                const double *h, const double *vn, const double *tr,
+                cudaStream_t st) {
+  launch_aux_t<double>(m, p, a, h, vn, tr, st);
 }
 
 void launch_axpby(double *y, const double *x, const double *z, double alpha,

@@ -394,6 +394,53 @@ class Batch:
             self._h = None
 
 
+class Adjoint:
+    """Tangent-linear and adjoint models of the RK4 step with binomial
+    checkpointing (swg_adjoint_* / swg_tlm_* / swg_adj_* in swgpu.h)."""
+
+    def __init__(self, model: ShallowWaterModel, nsnapshots: int = 32):
+        self.model = model
+        h = C.c_void_p()
+        check(lib().swg_adjoint_create(model.handle, int(nsnapshots),
+                                       C.byref(h)))
+        self._h = h
+
+    def tlm_tendency(self, x, dx, dtend, stream=None):
+        check(lib().swg_tlm_tendency(self._h, x.handle, dx.handle,
+                                     dtend.handle, _s(stream)))
+
+    def adj_tendency(self, x, mu, lam, stream=None):
+        check(lib().swg_adj_tendency(self._h, x.handle, mu.handle, lam.handle,
+                                     _s(stream)))
+
+    def tlm_apply(self, x0, dx, t0, dt, nsteps, stream=None):
+        check(lib().swg_tlm_apply(self._h, x0.handle, dx.handle, float(t0),
+                                  float(dt), int(nsteps), _s(stream)))
+
+    def forward(self, state0, t0, dt, nsteps, final, stream=None):
+        check(lib().swg_adj_forward(self._h, state0.handle, float(t0),
+                                    float(dt), int(nsteps), final.handle,
+                                    _s(stream)))
+
+    def backward(self, lam, stream=None):
+        check(lib().swg_adj_backward(self._h, lam.handle, _s(stream)))
+
+    def info(self):
+        a, b = C.c_longlong(), C.c_longlong()
+        check(lib().swg_adj_info(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _capi._lib is not None:
+            _capi._lib.swg_adjoint_destroy(self._h)
+            self._h = None
+
+
+def checkpoint_cost(nsteps: int, nsnapshots: int) -> int:
+    """Plain forward steps of the optimal binomial checkpointing schedule."""
+    return int(lib().swg_checkpoint_cost(int(nsteps), int(nsnapshots)))
+
+
 def _diag(fn, state, model, stream=None):
     out = C.c_double()
     check(fn(model.handle, state.handle, C.byref(out), _s(stream)))

@@ -114,7 +114,44 @@ WORKLOADS = {
                               5, 100, visc_del2=1e3, visc_del4=1e9,
                               eddy_diff2=1e3, eddy_diff4=1e9,
                               vn_noise_rms=0.05),
+    # checkpointed adjoint: 128x128 cells, 32 levels, 2 tracers, RK4,
+    # 1000 steps, 32 snapshots (the 64x64 workload's physics)
+    "rk4_128x128_adjoint": Workload("rk4_128x128_adjoint", 128, 128, 1e4, 32,
+                                    2, "rk4", 4, 1000, visc_del2=1e3),
 }
+ADJOINT_SNAPSHOTS = 32
+
+
+def region_cells(mesh, seed: int, frac: float = 0.25) -> np.ndarray:
+    """Cells inside a seeded axis-aligned rectangle covering `frac` of each
+    periodic dimension (the loss's target region)."""
+    Lx, Ly = mesh.m_period_x, mesh.m_period_y
+    u = uniform(seed, 2)
+    x0, y0 = u[0] * Lx * (1 - frac), u[1] * Ly * (1 - frac)
+    xc, yc = np.asarray(mesh.m_x_cell), np.asarray(mesh.m_y_cell)
+    inside = ((xc >= x0) & (xc < x0 + frac * Lx) &
+              (yc >= y0) & (yc < y0 + frac * Ly))
+    return np.nonzero(inside)[0]
+
+
+def loss_and_grad(h, vn, tr, region, h_ref: float = 1000.0):
+    """L = sum over region cells and levels of (h - h_ref)^2, plus for every
+    tracer and level the variance over the region of the concentration
+    tr / h.  Returns L and (dL/dh, dL/dvn, dL/dtr)."""
+    hr = h[region]                                   # [R][K]
+    L = float(np.sum((hr - h_ref) ** 2))
+    gh = np.zeros_like(h)
+    gh[region] = 2.0 * (hr - h_ref)
+    gtr = np.zeros_like(tr)
+    R = len(region)
+    for l in range(tr.shape[0]):
+        n = tr[l][region] / hr                       # [R][K]
+        dev = n - n.mean(axis=0, keepdims=True)
+        L += float(np.sum(dev * dev) / R)
+        g = 2.0 * dev / R                            # dL/dn
+        gtr[l][region] = g / hr
+        gh[region] -= g * n / hr
+    return L, (gh, np.zeros_like(vn), gtr)
 
 
 ENSEMBLE_NX = (32, 48, 64, 96, 128, 192)

@@ -79,3 +79,19 @@ def test_null_handles_are_errors_not_crashes():
     assert lib.swg_step(None, None, 0.0, 1.0, 1, 0, None) == 1
     assert lib.swg_compute_tendency(None, None, None, 0.0, 0, None) == 1
     assert lib.swg_mesh_destroy(None) == 0
+
+
+def test_checkpoint_cost_matches_binomial_formula():
+    """Plain advances of the optimal schedule equal Griewank-Walther's
+    t(n, s) = r n - C(s + r, s + 1) with C(s + r - 1, s) < n <= C(s + r, s)
+    (host-only planner, no GPU)."""
+    from math import comb
+    lib = _capi.lib()
+    for n, s in [(1000, 32), (100, 5), (50, 1), (7, 3), (20, 4), (12, 12),
+                 (300, 10)]:
+        r = 0
+        while comb(s + r, s) < n:
+            r += 1
+        t = r * n - comb(s + r, s + 1) if r > 0 else 0
+        assert lib.swg_checkpoint_cost(n, s) == t, (n, s)
+    assert lib.swg_checkpoint_cost(1000, 32) == 2405

@@ -1,0 +1,161 @@
+"""Tangent-linear and adjoint models.
+
+- dot-product tests: <J dx, mu> = <dx, J^T mu> for one tendency evaluation
+  (every term on, and the frozen-flow tracer configuration), and
+  <dx_N, lam_N> = <dx_0, lam_0> over RK4 trajectories whose adjoint runs
+  through the binomial checkpointing schedule (several snapshot budgets);
+  bound 1e-12 relative.  The TLM is the forward kernels on dual numbers, the
+  adjoint is hand-written, so agreement checks the adjoint;
+- central finite differences of the plain forward (16 seeded directions)
+  against the adjoint gradient of the region loss; bound 1e-6 relative."""
+import numpy as np
+import pytest
+
+import omega_playground_gb300 as og
+from omega_playground_gb300.workloads import (WORKLOADS, initial_state,
+                                              loss_and_grad, region_cells,
+                                              uniform)
+
+pytestmark = pytest.mark.gpu
+
+
+def setup(wl, **over):
+    mesh = og.PlanarHexagonalMesh(wl.nx, wl.ny, wl.dc, wl.nlayers)
+    params = wl.params()
+    for k, v in over.items():
+        setattr(params, k, v)
+    model = og.ShallowWaterModel(mesh, params)
+    return mesh, params, model
+
+
+def rand_like(shapes, seed, scale=(1.0, 1.0, 1.0)):
+    out = []
+    for j, (sh, sc) in enumerate(zip(shapes, scale)):
+        n = int(np.prod(sh))
+        u = uniform(seed + 7 * j, 2 * n)
+        g = np.sqrt(-2 * np.log(u[:n] + 1e-300)) * np.cos(2 * np.pi * u[n:])
+        out.append(sc * g.reshape(sh))
+    return out
+
+
+def dot(a, b):
+    return sum(float(np.sum(x * y)) for x, y in zip(a, b))
+
+
+def make_state(mesh, params, arrays):
+    s = og.ShallowWaterState(mesh, params)
+    s.upload(*arrays)
+    return s
+
+
+ALL_TERMS = WORKLOADS["lsrk5_512x512"].scaled(nx=12, ny=10, nlayers=5,
+                                              ntracers=3, stepper="rk4",
+                                              nstages=4)
+
+
+@pytest.mark.parametrize("over", [{}, {"m_disable_h_tendency": True,
+                                       "m_disable_vn_tendency": True},
+                                  {"m_visc_del4": 0.0, "m_eddy_diff4": 0.0}])
+def test_tendency_dot_product(over):
+    mesh, params, model = setup(ALL_TERMS, **over)
+    adj = og.Adjoint(model, 2)
+    x = initial_state(mesh, ALL_TERMS)
+    shapes = [a.shape for a in x]
+    dx = rand_like(shapes, 101, (1.0, 0.01, 10.0))
+    mu = rand_like(shapes, 202)
+    X = make_state(mesh, params, x)
+    DX = make_state(mesh, params, dx)
+    MU = make_state(mesh, params, mu)
+    JT = og.ShallowWaterState(mesh, params)
+    JD = og.ShallowWaterState(mesh, params)
+    adj.tlm_tendency(X, DX, JD)
+    adj.adj_tendency(X, MU, JT)
+    jd, jt = JD.download(), JT.download()
+    lhs, rhs = dot(jd, mu), dot(dx, jt)
+    assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+    # the TLM against a central difference of the forward tendency
+    eps = 1e-6
+    tp = og.ShallowWaterState(mesh, params)
+    tm = og.ShallowWaterState(mesh, params)
+    model.compute_tendency(tp, make_state(mesh, params,
+                                          [a + eps * b for a, b in zip(x, dx)]), 0.0)
+    model.compute_tendency(tm, make_state(mesh, params,
+                                          [a - eps * b for a, b in zip(x, dx)]), 0.0)
+    fd = [(p - q) / (2 * eps) for p, q in zip(tp.download(), tm.download())]
+    for a, b in zip(fd, jd):
+        scale = max(np.max(np.abs(b)), 1e-300)
+        assert np.max(np.abs(a - b)) / scale < 1e-5
+
+
+@pytest.mark.parametrize("nsteps,nsnap", [(1, 1), (7, 1), (7, 3), (20, 4),
+                                          (9, 12)])
+def test_trajectory_dot_product_through_checkpointing(nsteps, nsnap):
+    wl = ALL_TERMS
+    mesh, params, model = setup(wl)
+    adj = og.Adjoint(model, nsnap)
+    x0 = initial_state(mesh, wl)
+    shapes = [a.shape for a in x0]
+    dx0 = rand_like(shapes, 303, (1.0, 0.01, 10.0))
+    lamN = rand_like(shapes, 404)
+    X0 = make_state(mesh, params, x0)
+    XN = og.ShallowWaterState(mesh, params)
+    adj.forward(X0, 0.0, wl.dt, nsteps, XN)
+    LAM = make_state(mesh, params, lamN)
+    adj.backward(LAM)
+    lam0 = LAM.download()
+    plain, taped = adj.info()
+    assert taped == nsteps
+    assert plain == og.checkpoint_cost(nsteps, nsnap)
+    DX = make_state(mesh, params, dx0)
+    adj.tlm_apply(X0, DX, 0.0, wl.dt, nsteps)
+    dxN = DX.download()
+    lhs, rhs = dot(dxN, lamN), dot(dx0, lam0)
+    assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+    # the forward sweep's final state equals a plain RK4 run
+    ref = make_state(mesh, params, x0)
+    og.RK4Stepper(model).step(ref, 0.0, wl.dt, nsteps, use_graph=False)
+    for a, b in zip(XN.download(), ref.download()):
+        np.testing.assert_array_equal(a, b)
+
+
+def _fd_check(wl, nsteps, nsnap, ndir, eps):
+    mesh, params, model = setup(wl)
+    region = region_cells(mesh, wl.seed + 99)
+    assert len(region) > 0
+    x0 = initial_state(mesh, wl)
+    adj = og.Adjoint(model, nsnap)
+    X0 = make_state(mesh, params, x0)
+    XN = og.ShallowWaterState(mesh, params)
+    adj.forward(X0, 0.0, wl.dt, nsteps, XN)
+    L0, g = loss_and_grad(*XN.download(), region)
+    G = make_state(mesh, params, g)
+    adj.backward(G)
+    grad = G.download()
+    stepper = og.RK4Stepper(model)
+    shapes = [a.shape for a in x0]
+    worst = 0.0
+    for j in range(ndir):
+        d = rand_like(shapes, 1000 + 17 * j, (1.0, 0.01, 10.0))
+        vals = []
+        for sgn in (1, -1):
+            s = make_state(mesh, params, [a + sgn * eps * b for a, b in zip(x0, d)])
+            stepper.step(s, 0.0, wl.dt, nsteps)
+            vals.append(loss_and_grad(*s.download(), region)[0])
+        fd = (vals[0] - vals[1]) / (2 * eps)
+        an = dot(grad, d)
+        worst = max(worst, abs(fd - an) / abs(an))
+    return worst
+
+
+def test_finite_differences_reduced():
+    """The adjoint workload's physics on a 32x32x8 mesh, 60 RK4 steps, 6
+    snapshots, 16 seeded directions."""
+    wl = WORKLOADS["rk4_128x128_adjoint"].scaled(nx=32, ny=32, nlayers=8)
+    assert _fd_check(wl, 60, 6, 16, 1e-4) <= 1e-6
+
+
+def test_finite_differences_full_adjoint_workload():
+    """128x128 cells, 32 levels, 2 tracers, RK4, 1000 steps, 32 snapshots,
+    16 seeded directions."""
+    wl = WORKLOADS["rk4_128x128_adjoint"]
+    assert _fd_check(wl, wl.nsteps, 32, 16, 1e-4) <= 1e-6
