@@ -66,8 +66,25 @@ struct AdjWork {
 struct AdjIO {
   const double *h, *vn, *tr;    // state X
   const double *mh_, *mvn, *mtr; // mu (adjoint of the tendency)
-  double *lh, *lvn, *ltr;        // lambda = J^T mu (written)
+  double *lh, *lvn, *ltr;        // lambda = J^T mu (written unless null)
+  // fused RK4 bookkeeping (each may be null): acc += lambda, and the next
+  // stage's mu_next = alpha * lam + beta * lambda
+  double *acc_h, *acc_vn, *acc_tr;
+  double *nmu_h, *nmu_vn, *nmu_tr;
+  const double *lam_h, *lam_vn, *lam_tr;
+  double alpha, beta;
 };
+
+__device__ __forceinline__ void emit(double *out, double *acc, double *nmu,
+                                     const double *lam, double alpha,
+                                     double beta, size_t i, double x) {
+  if (out)
+    out[i] = x;
+  if (acc)
+    acc[i] += x;
+  if (nmu)
+    nmu[i] = fma(alpha, lam[i], beta * x);
+}
 
 // --- pass 1: transposed edge stencils of the velocity tendency (cells and
 // vertices); the first V*K threads take vertices.
@@ -195,7 +212,8 @@ __global__ void __launch_bounds__(ATPB)
       for (int j = 0; j < MAXE; ++j)
         ln = fma(mnb[j], lL[size_t(nb[j]) * K + k], ln);
     }
-    io.ltr[t] = ln * r;
+    emit(io.ltr, io.acc_tr, io.nmu_tr, io.lam_tr, io.alpha, io.beta, t,
+         ln * r);
     hsum = fma(ln, a.ntr[t], hsum);
   }
   w.lhtr[i] = -(r * hsum);
@@ -328,7 +346,7 @@ __global__ void __launch_bounds__(ATPB)
     lh += w.lhs[i];
   if (p.ntracers > 0)
     lh += w.lhtr[i];
-  io.lh[i] = lh;
+  emit(io.lh, io.acc_h, io.nmu_h, io.lam_h, io.alpha, io.beta, i, lh);
   if (p.do_vn && (p.vel_del2 | p.vel_del4))
     w.ldiv[i] = ld;
 }
@@ -352,20 +370,15 @@ __global__ void __launch_bounds__(ATPB)
       l = fma(__ldg(v.ccd_e2 + 2 * e + 1), w.ldiv[size_t(c1) * K + k], l);
     }
   }
-  io.lvn[i] = l;
+  emit(io.lvn, io.acc_vn, io.nmu_vn, io.lam_vn, io.alpha, io.beta, i, l);
 }
 
-// y = alpha x1 + beta x2 (x2 may be null), y += x (axpy), dual pack/unpack
+// y = alpha x1 + beta x2 (x2 may be null); dual pack / unpack
 __global__ void ka_lincomb(double *y, const double *x1, const double *x2,
                            double alpha, double beta, long long n) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i < n)
     y[i] = x2 ? fma(alpha, x1[i], beta * x2[i]) : alpha * x1[i];
-}
-__global__ void ka_add(double *y, const double *x, long long n) {
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i < n)
-    y[i] += x[i];
 }
 __global__ void ka_pack(Dual *y, const double *v, const double *d,
                         long long n) {
@@ -404,7 +417,12 @@ struct swg_adjoint_s {
   swg_stepper stepper = nullptr; // plain advances (graph replay)
   std::vector<swg_state> snaps;
   swg_state cur = nullptr, next = nullptr, X[4] = {}, acc = nullptr,
-            lam = nullptr, lacc = nullptr, mu = nullptr, lX = nullptr;
+            lam = nullptr, lacc = nullptr, mu = nullptr, mu2 = nullptr,
+            lX = nullptr;
+  AuxView taux[4]{};              // intermediates of the taped stages
+  cudaGraphExec_t tape_graph = nullptr;
+  double tape_graph_dt = 0;
+  long long tape_graph_launches = 0;
   // tangent-linear model buffers
   AuxViewT<Dual> daux{};
   Dual *dS = nullptr, *dacc = nullptr, *dP0 = nullptr, *dP1 = nullptr,
@@ -580,24 +598,22 @@ int build_tables(swg_adjoint ad) {
   return SWG_OK;
 }
 
-// aux arrays of the tangent-linear model (same set as the model's)
-int alloc_dual_aux(swg_adjoint ad) {
+// aux arrays of the same set as the model's, of value type T
+template <class T> int alloc_aux_like(swg_adjoint ad, AuxViewT<T> &d) {
   swg_model md = ad->model;
-  const ModelView &pv = md->view;
   const AuxView &a = md->aux;
   const size_t C = md->mesh->ncells, E = md->mesh->nedges,
                V = md->mesh->nvertices, K = md->mesh->nlayers,
-               T = md->params.ntracers;
-  AuxViewT<Dual> &d = ad->daux;
+               T_ = md->params.ntracers;
   auto &A = ad->allocs;
   struct {
     const double *on;
     size_t n;
-    Dual **p;
+    T **p;
   } t[] = {{a.q, V * K, &d.q},       {a.zeta, V * K, &d.zeta},
            {a.z4, V * K, &d.z4},     {a.div, C * K, &d.div},
            {a.ke, C * K, &d.ke},     {a.d4, C * K, &d.d4},
-           {a.ntr, T * C * K, &d.ntr}, {a.lap, T * C * K, &d.lap},
+           {a.ntr, T_ * C * K, &d.ntr}, {a.lap, T_ * C * K, &d.lap},
            {a.F, E * K, &d.F},       {a.G, E * K, &d.G},
            {a.Q, E * K, &d.Q},       {a.mh, E * K, &d.mh},
            {a.u2, E * K, &d.u2},     {a.d2u, E * K, &d.d2u}};
@@ -605,20 +621,17 @@ int alloc_dual_aux(swg_adjoint ad) {
     if (x.on)
       TRY(zal(A, x.n, x.p));
   d.d2u4 = d.d2u;
-  (void)pv;
   return SWG_OK;
 }
 
-void adj_tendency(swg_adjoint ad, const double *h, const double *vn,
-                  const double *tr, swg_state mu, swg_state out,
-                  cudaStream_t st) {
+// lambda = J(X)^T mu with the intermediates of X already in `aux`
+void adj_passes(swg_adjoint ad, const AuxView &aux, const AdjIO &io,
+                cudaStream_t st) {
   swg_model md = ad->model;
   const MeshView &m = md->mesh->view;
   const ModelView &p = md->view;
   const long long K = m.nlayers, CK = m.ncells * K, EK = m.nedges * K,
                   VK = m.nvertices * K;
-  launch_aux(m, p, md->aux, h, vn, tr, st);
-  AdjIO io{h, vn, tr, mu->h, mu->vn, mu->tr, out->h, out->vn, out->tr};
   const AdjView &v = ad->av;
   const AdjWork &w = ad->aw;
   if (p.do_vn) {
@@ -626,17 +639,17 @@ void adj_tendency(swg_adjoint ad, const double *h, const double *vn,
     ++g_launches;
   }
   if (p.ntracers > 0) {
-    ka_tr1<<<nb(CK), ATPB, 0, st>>>(m, p, md->aux, v, w, io);
-    ka_tr2<<<nb(CK), ATPB, 0, st>>>(m, p, md->aux, v, w, io);
+    ka_tr1<<<nb(CK), ATPB, 0, st>>>(m, p, aux, v, w, io);
+    ka_tr2<<<nb(CK), ATPB, 0, st>>>(m, p, aux, v, w, io);
     g_launches += 2;
   }
   if (m.ne == 8)
-    ka_edge<8><<<nb(EK), ATPB, 0, st>>>(m, p, md->aux, v, w, io);
+    ka_edge<8><<<nb(EK), ATPB, 0, st>>>(m, p, aux, v, w, io);
   else
-    ka_edge<10><<<nb(EK), ATPB, 0, st>>>(m, p, md->aux, v, w, io);
+    ka_edge<10><<<nb(EK), ATPB, 0, st>>>(m, p, aux, v, w, io);
   ++g_launches;
   if (p.do_vn) {
-    ka_vertex<<<nb(VK), ATPB, 0, st>>>(m, p, md->aux, v, w, io);
+    ka_vertex<<<nb(VK), ATPB, 0, st>>>(m, p, aux, v, w, io);
     ++g_launches;
   }
   ka_cell<<<nb(CK), ATPB, 0, st>>>(m, p, v, w, io);
@@ -644,14 +657,27 @@ void adj_tendency(swg_adjoint ad, const double *h, const double *vn,
   g_launches += 2;
 }
 
+void adj_tendency(swg_adjoint ad, const double *h, const double *vn,
+                  const double *tr, swg_state mu, swg_state out,
+                  cudaStream_t st) {
+  swg_model md = ad->model;
+  launch_aux(md->mesh->view, md->view, md->aux, h, vn, tr, st);
+  AdjIO io{};
+  io.h = h;
+  io.vn = vn;
+  io.tr = tr;
+  io.mh_ = mu->h;
+  io.mvn = mu->vn;
+  io.mtr = mu->tr;
+  io.lh = out->h;
+  io.lvn = out->vn;
+  io.ltr = out->tr;
+  adj_passes(ad, md->aux, io, st);
+}
+
 void lincomb(swg_state y, swg_state x1, swg_state x2, double a, double b,
              long long n, cudaStream_t st) {
   ka_lincomb<<<nb(n), ATPB, 0, st>>>(y->h, x1->h, x2 ? x2->h : nullptr, a, b, n);
-  ++g_launches;
-}
-
-void addto(swg_state y, swg_state x, long long n, cudaStream_t st) {
-  ka_add<<<nb(n), ATPB, 0, st>>>(y->h, x->h, n);
   ++g_launches;
 }
 
@@ -687,15 +713,21 @@ int tape_step(swg_adjoint ad, double dt, swg_state out, cudaStream_t st) {
     a.ftr = {nullptr, S->tr, ad->acc->tr, o->tr};
     const int mode = s == 0 ? EPI_RK4_FIRST : (s < 3 ? EPI_RK4_MID : EPI_RK4_LAST);
     a.ep = {mode, 0.0, dt * rkb[s], s < 3 ? dt * rka[s] : 0.0};
-    launch_tendency(md->mesh->view, pv, md->aux, a, st);
+    launch_tendency(md->mesh->view, pv, ad->taux[s], a, st);
   }
-  // a disabled field is not written by the stages: keep X_s meaningful
+  if (!out) { // intermediates of the last stage input
+    const double *h, *vn, *tr;
+    stage_ptrs(ad, 3, &h, &vn, &tr);
+    launch_aux(md->mesh->view, pv, ad->taux[3], h, vn, tr, st);
+  }
   ++ad->taped_steps;
   cudaError_t err = cudaGetLastError();
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_adjoint: taped step");
 }
 
-// lam <- adjoint of the taped step applied to lam
+// lam <- adjoint of the taped step applied to lam.  The output passes of
+// stage s accumulate lamX_s into lacc and form mu_{s-1} directly
+// (ping-pong mu buffers: the passes of stage s still read mu_s).
 int adjoint_step(swg_adjoint ad, double dt, cudaStream_t st) {
   static const double rka[3] = {1. / 2, 1. / 2, 1};
   static const double rkb[4] = {1. / 6, 1. / 3, 1. / 3, 1. / 6};
@@ -704,15 +736,29 @@ int adjoint_step(swg_adjoint ad, double dt, cudaStream_t st) {
                                     cudaMemcpyDeviceToDevice, st);
   if (err != cudaSuccess)
     return cuda_fail(err, "swg_adjoint: copy");
+  lincomb(ad->mu, ad->lam, nullptr, dt * rkb[3], 0.0, n, st);
+  swg_state mus[2] = {ad->mu, ad->mu2};
   for (int s = 3; s >= 0; --s) {
-    if (s == 3)
-      lincomb(ad->mu, ad->lam, nullptr, dt * rkb[3], 0.0, n, st);
-    else
-      lincomb(ad->mu, ad->lam, ad->lX, dt * rkb[s], dt * rka[s], n, st);
-    const double *h, *vn, *tr;
-    stage_ptrs(ad, s, &h, &vn, &tr);
-    adj_tendency(ad, h, vn, tr, ad->mu, ad->lX, st);
-    addto(ad->lacc, ad->lX, n, st);
+    swg_state mu = mus[(3 - s) % 2], nmu = mus[(4 - s) % 2];
+    AdjIO io{};
+    stage_ptrs(ad, s, &io.h, &io.vn, &io.tr);
+    io.mh_ = mu->h;
+    io.mvn = mu->vn;
+    io.mtr = mu->tr;
+    io.acc_h = ad->lacc->h;
+    io.acc_vn = ad->lacc->vn;
+    io.acc_tr = ad->lacc->tr;
+    if (s > 0) {
+      io.nmu_h = nmu->h;
+      io.nmu_vn = nmu->vn;
+      io.nmu_tr = nmu->tr;
+      io.lam_h = ad->lam->h;
+      io.lam_vn = ad->lam->vn;
+      io.lam_tr = ad->lam->tr;
+      io.alpha = dt * rkb[s - 1];
+      io.beta = dt * rka[s - 1];
+    }
+    adj_passes(ad, ad->taux[s], io, st);
   }
   err = cudaMemcpyAsync(ad->lam->h, ad->lacc->h, n * 8,
                         cudaMemcpyDeviceToDevice, st);
@@ -792,9 +838,52 @@ int run_action(swg_adjoint ad, const AdjAction &a, cudaStream_t st) {
   case 2:
     return swg_state_copy(ad->cur, ad->snaps[a.a], st);
   default:
-    TRY(tape_step(ad, ad->dt, nullptr, st));
-    return adjoint_step(ad, ad->dt, st);
+    break;
   }
+  // tape + adjoint of one step: the same launches every time (no forcing),
+  // replayed from a CUDA graph captured on first use
+  if (!ad->tape_graph || ad->tape_graph_dt != ad->dt) {
+    if (ad->tape_graph) {
+      cudaGraphExecDestroy(ad->tape_graph);
+      ad->tape_graph = nullptr;
+    }
+    cudaStream_t cs;
+    cudaError_t err = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (err != cudaSuccess)
+      return cuda_fail(err, "swg_adjoint: capture stream");
+    const long long before = g_launches.load();
+    const long long taped = ad->taped_steps;
+    err = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    int rc = SWG_OK;
+    if (err == cudaSuccess && (rc = tape_step(ad, ad->dt, nullptr, cs)) == SWG_OK)
+      rc = adjoint_step(ad, ad->dt, cs);
+    cudaGraph_t g = nullptr;
+    cudaError_t err2 = cudaStreamEndCapture(cs, &g);
+    ad->tape_graph_launches = g_launches.load() - before;
+    g_launches -= ad->tape_graph_launches;
+    ad->taped_steps = taped;
+    cudaStreamDestroy(cs);
+    if (err != cudaSuccess || err2 != cudaSuccess || rc != SWG_OK) {
+      if (g)
+        cudaGraphDestroy(g);
+      (void)cudaGetLastError();
+      TRY(tape_step(ad, ad->dt, nullptr, st)); // direct launches
+      return adjoint_step(ad, ad->dt, st);
+    }
+    err = cudaGraphInstantiate(&ad->tape_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (err != cudaSuccess) {
+      ad->tape_graph = nullptr;
+      return cuda_fail(err, "swg_adjoint: graph instantiate");
+    }
+    ad->tape_graph_dt = ad->dt;
+  }
+  cudaError_t err = cudaGraphLaunch(ad->tape_graph, st);
+  if (err != cudaSuccess)
+    return cuda_fail(err, "swg_adjoint: graph launch");
+  g_launches += ad->tape_graph_launches;
+  ++ad->taped_steps;
+  return SWG_OK;
 }
 
 int check_model(swg_model md) {
@@ -844,7 +933,7 @@ extern "C" int swg_adjoint_create(swg_model md, int nsnapshots,
     ;
   swg_state *st[] = {&ad->cur, &ad->next, &ad->X[0], &ad->X[1], &ad->X[2],
                      &ad->X[3], &ad->acc, &ad->lam, &ad->lacc, &ad->mu,
-                     &ad->lX};
+                     &ad->mu2, &ad->lX};
   for (auto *p : st)
     if (rc == SWG_OK)
       rc = swg_state_create(md->mesh, T, p);
@@ -856,7 +945,11 @@ extern "C" int swg_adjoint_create(swg_model md, int nsnapshots,
   if (rc == SWG_OK)
     rc = swg_stepper_create(md, SWG_STEPPER_RK4, 4, &ad->stepper);
   const size_t n = words(md);
-  if (rc == SWG_OK && ((rc = alloc_dual_aux(ad)) || (rc = zal(A, n, &ad->dS)) ||
+  if (rc == SWG_OK && ((rc = alloc_aux_like(ad, ad->daux)) ||
+                       (rc = alloc_aux_like(ad, ad->taux[0])) ||
+                       (rc = alloc_aux_like(ad, ad->taux[1])) ||
+                       (rc = alloc_aux_like(ad, ad->taux[2])) ||
+                       (rc = alloc_aux_like(ad, ad->taux[3])) || (rc = zal(A, n, &ad->dS)) ||
                        (rc = zal(A, n, &ad->dacc)) || (rc = zal(A, n, &ad->dP0)) ||
                        (rc = zal(A, n, &ad->dP1)) || (rc = zal(A, n, &ad->dT))))
     ;
@@ -872,8 +965,10 @@ extern "C" int swg_adjoint_destroy(swg_adjoint ad) {
   if (!ad)
     return SWG_OK;
   swg_stepper_destroy(ad->stepper);
+  if (ad->tape_graph)
+    cudaGraphExecDestroy(ad->tape_graph);
   swg_state st[] = {ad->cur, ad->next, ad->X[0], ad->X[1], ad->X[2], ad->X[3],
-                    ad->acc, ad->lam, ad->lacc, ad->mu, ad->lX};
+                    ad->acc, ad->lam, ad->lacc, ad->mu, ad->mu2, ad->lX};
   for (auto s : st)
     swg_state_destroy(s);
   for (auto s : ad->snaps)
