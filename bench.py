@@ -59,6 +59,22 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
+def max_over_ranks(ms: float, world: int, device: str = "cpu") -> float:
+    """Slowest rank's time (the whole job ends when the last replica does)."""
+    if world == 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank: int, ms_max: float, world: int) -> float:
+    """Whole-job updates/s of `world` independent replicas (weak scaling)."""
+    return world * units_per_rank / (ms_max / 1e3)
+
+
 def hbm_peak():
     try:
         with open(PEAKS_FILE) as f:
@@ -303,12 +319,9 @@ def run_ours(args, wl):
     ms = e0.elapsed_time(e1)
     launches = og.kernel_launches() - launches0
     clk = clocks.stop()
-    ms_t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(ms_t.item())
+    ms_max = max_over_ranks(ms, world, device="cuda")
     units = wl.ncells * wl.nlayers * wl.nstages * args.steps
-    value = world * units / (ms_max / 1e3)
+    value = replica_throughput(units, ms_max, world)
 
     # per-kernel event timing of one step (direct launches)
     og.profile_enable(True)
