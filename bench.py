@@ -500,10 +500,124 @@ def run_ensemble(args):
     print(json.dumps(line), flush=True)
 
 
+def run_adjoint_ensemble(args):
+    """Batched adjoints: 32 members (nx from {32, 64, 96, 128}, 16-64 levels,
+    2 tracers, RK4, 300 steps, per-cell log-normal viscosity), gradient of
+    the region loss w.r.t. the initial state and the viscosity field, each
+    member with its own checkpoint budget and stream.  Timed against the
+    batched plain forward of the same members and against the members'
+    adjoints run one after another."""
+    import torch
+    import omega_playground_gb300 as og
+    from omega_playground_gb300.workloads import (adjoint_ensemble,
+                                                  initial_state,
+                                                  lognormal_visc,
+                                                  loss_and_grad, region_cells,
+                                                  visc_scaling)
+    torch.cuda.set_device(0)
+    wls = adjoint_ensemble(n=32)
+    mem = []
+    for wl in wls:
+        visc = lognormal_visc(wl.nx * wl.ny, wl.seed + 5)
+        probe = og.PlanarHexagonalMesh(wl.nx, wl.ny, wl.dc, wl.nlayers)
+        mesh = og.PlanarHexagonalMesh(
+            wl.nx, wl.ny, wl.dc, wl.nlayers,
+            mesh_scaling_del2=visc_scaling(probe, visc, wl.visc_del2))
+        params = wl.params()
+        model = og.ShallowWaterModel(mesh, params)
+        x0 = initial_state(mesh, wl)
+        # checkpoint budget per member: 32 snapshots, 16 for the largest
+        nsnap = 16 if wl.nx >= 128 else 32
+        mem.append(dict(wl=wl, mesh=mesh, params=params, model=model, x0=x0,
+                        region=region_cells(mesh, wl.seed + 99), nsnap=nsnap))
+    dt, nsteps = wls[0].dt, wls[0].nsteps
+    units = sum(w.ncells * w.nlayers * 4 for w in wls) * nsteps
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    cur = torch.cuda.current_stream()
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        ev[0].record(cur)
+        fn()
+        torch.cuda.synchronize()
+        ev[1].record(cur)
+        torch.cuda.synchronize()
+        return ev[0].elapsed_time(ev[1])
+
+    # plain batched forward of the members
+    states = []
+    for m in mem:
+        st = og.ShallowWaterState(m["mesh"], m["params"])
+        st.upload(*m["x0"])
+        states.append(st)
+    batch = og.Batch([m["model"] for m in mem], states, "rk4", 4)
+    best_cfg, _ = batch.autotune(dt, 2)
+    batch.step(0.0, dt, 2)
+    for st, m in zip(states, mem):
+        st.upload(*m["x0"])
+    fwd_ms = timed(lambda: batch.step(0.0, dt, nsteps))
+    # batched adjoint: forward sweep, loss gradients, backward sweep
+    adjs = [og.Adjoint(m["model"], m["nsnap"]) for m in mem]
+    X0 = []
+    XN = []
+    for m in mem:
+        a = og.ShallowWaterState(m["mesh"], m["params"])
+        a.upload(*m["x0"])
+        X0.append(a)
+        XN.append(og.ShallowWaterState(m["mesh"], m["params"]))
+    streams = [torch.cuda.Stream() for _ in mem]
+    sh = [s.cuda_stream for s in streams]
+    f_ms = timed(lambda: og.adjoint_batch_forward(adjs, X0, 0.0, dt, nsteps,
+                                                  XN, sh))
+    Gs, loss = [], 0.0
+    for m, xn in zip(mem, XN):
+        L, g = loss_and_grad(*xn.download(), m["region"])
+        loss += L
+        G = og.ShallowWaterState(m["mesh"], m["params"])
+        G.upload(*g)
+        Gs.append(G)
+    b_ms = timed(lambda: og.adjoint_batch_backward(adjs, Gs, sh))
+    gvisc = [a.grad_visc()[1] for a in adjs]
+    # the same adjoints one member at a time (default stream)
+    seq_ms = 0.0
+    for m in mem:
+        a = og.Adjoint(m["model"], m["nsnap"])
+        x = og.ShallowWaterState(m["mesh"], m["params"])
+        x.upload(*m["x0"])
+        xn = og.ShallowWaterState(m["mesh"], m["params"])
+        seq_ms += timed(lambda: a.forward(x, 0.0, dt, nsteps, xn))
+        g = og.ShallowWaterState(m["mesh"], m["params"])
+        g.upload(*loss_and_grad(*xn.download(), m["region"])[1])
+        seq_ms += timed(lambda: a.backward(g))
+    line = {"metric": METRIC, "value": (f_ms + b_ms) / fwd_ms,
+            "unit": "adjoint/forward time ratio", "n_gpus": 1,
+            "steps": nsteps, "warmup": 2, "ms_per_step": (f_ms + b_ms) / nsteps,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": "adjoint_ensemble32", "members": len(wls),
+                       "nx": sorted({w.nx for w in wls}),
+                       "levels": [min(w.nlayers for w in wls),
+                                  max(w.nlayers for w in wls)],
+                       "tracers": 2, "stepper": "rk4",
+                       "snapshots": sorted({m["nsnap"] for m in mem})},
+            "batched_forward_ms": fwd_ms, "batch_config": best_cfg,
+            "adjoint_forward_sweep_ms": f_ms,
+            "adjoint_backward_sweep_ms": b_ms,
+            "sequential_member_adjoints_ms": seq_ms,
+            "batched_over_sequential_speedup": seq_ms / (f_ms + b_ms),
+            "forward_updates_per_s": units / (fwd_ms / 1e3), "loss": loss,
+            "grad_visc_norm": float(np.sqrt(sum(float(np.sum(g * g))
+                                                for g in gvisc)))}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "ensemble64":
         run_ensemble(args)
+        return
+    if args.workload == "adjoint_ensemble32":
+        run_adjoint_ensemble(args)
         return
     from omega_playground_gb300.workloads import WORKLOADS
     wl = WORKLOADS[args.workload]

@@ -259,9 +259,29 @@ int swg_tlm_apply(swg_adjoint adj, swg_state x0, swg_state dx, double t0,
 int swg_adj_forward(swg_adjoint adj, swg_state state0, double t0, double dt,
                     int nsteps, swg_state final_out, void *stream);
 int swg_adj_backward(swg_adjoint adj, swg_state lambda, void *stream);
+/* Batched ensemble adjoints: members with uneven sizes, each with its own
+ * adjoint object (so its own checkpoint budget and schedule), advanced
+ * together: the schedules are interleaved one action at a time and member m
+ * runs on streams[m] (NULL array: the legacy stream), so the GPU executes the
+ * members concurrently.  Results equal per-member swg_adj_forward/backward. */
+int swg_adj_batch_forward(int n, const swg_adjoint *adjs,
+                          const swg_state *states0, double t0, double dt,
+                          int nsteps, const swg_state *finals,
+                          void *const *streams);
+int swg_adj_batch_backward(int n, const swg_adjoint *adjs,
+                           const swg_state *lambdas, void *const *streams);
 /* plain (re-)advanced and taped steps of the last forward/backward pair */
 int swg_adj_info(swg_adjoint adj, long long *plain_steps,
                  long long *taped_steps);
+/* Gradient of the loss whose dL/dx_N was given to the last swg_adj_backward
+ * with respect to the del2 viscosity, host arrays (either may be NULL):
+ * per edge, d L / d(visc_del2 * mesh_scaling_del2[e]); per cell, for a
+ * per-cell field mapped to edges as visc_e = (visc_c0 + visc_c1) / 2
+ * (realised through mesh_scaling_del2, vel_diff_edge.hpp:83-84).  Only the
+ * momentum term is differentiated: with eddy_diff2 > 0 the same scaling
+ * also enters tracer diffusion, which this gradient leaves out. */
+int swg_adj_grad_visc(swg_adjoint adj, double *grad_edge, double *grad_cell,
+                      void *stream);
 /* plain advances of the optimal binomial schedule (host only) */
 long long swg_checkpoint_cost(int nsteps, int nsnapshots);
 

@@ -7,7 +7,8 @@ in include/swgpu.h.  This package is the Python mirror of the reference's
 C++ classes (see shallow_water.py); the C++ mirror is cxx/omega_gpu.hpp.
 """
 from .shallow_water import (AddMode, Adjoint, Batch, LSRKStepper,  # noqa: F401
-                            MPASMesh, checkpoint_cost,
+                            MPASMesh, adjoint_batch_backward,
+                            adjoint_batch_forward, checkpoint_cost,
                             PlanarHexagonalMesh, RK4Stepper,
                             ShallowWaterModel, ShallowWaterParams,
                             ShallowWaterState, TimeStepper,
@@ -17,7 +18,8 @@ from .shallow_water import (AddMode, Adjoint, Batch, LSRKStepper,  # noqa: F401
 from ._capi import SwgError, exported_symbols  # noqa: F401
 from . import workloads  # noqa: F401
 
-__all__ = ["AddMode", "Adjoint", "Batch", "checkpoint_cost", "LSRKStepper", "MPASMesh", "PlanarHexagonalMesh",
+__all__ = ["AddMode", "Adjoint", "Batch", "checkpoint_cost",
+           "adjoint_batch_forward", "adjoint_batch_backward", "LSRKStepper", "MPASMesh", "PlanarHexagonalMesh",
            "RK4Stepper", "ShallowWaterModel", "ShallowWaterParams",
            "ShallowWaterState", "TimeStepper", "circulation_integral",
            "energy_integral", "mass_integral", "sync", "kernel_launches",

@@ -61,6 +61,7 @@ struct AdjWork {
   double *lke, *ld4, *lhs, *lhtr, *ldiv; // [C][K]
   double *lz4, *lzeta, *lhv;            // [V][K]
   double *lQ, *lmh, *lvnp, *ld2u;       // [E][K]
+  double *gc2e; // [E][K] accumulated dL/d(visc_del2 * mesh_scaling_del2), or null
 };
 
 struct AdjIO {
@@ -259,6 +260,8 @@ __global__ void __launch_bounds__(ATPB)
     if (p.vel_del2 | p.vel_del4) {
       const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
       double d = p.vel_del2 ? __ldg(p.c2e + e) * mu : 0.0;
+      if (p.vel_del2 && w.gc2e) // parameter gradient of the del2 coefficient
+        w.gc2e[i] = fma(mu, a.d2u[i], w.gc2e[i]);
       if (p.vel_del4) {
         d = fma(__ldg(v.cvr_e2 + 2 * e), w.lz4[size_t(v0) * K + k], d);
         d = fma(__ldg(v.cvr_e2 + 2 * e + 1), w.lz4[size_t(v1) * K + k], d);
@@ -379,6 +382,15 @@ __global__ void ka_lincomb(double *y, const double *x1, const double *x2,
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i < n)
     y[i] = x2 ? fma(alpha, x1[i], beta * x2[i]) : alpha * x1[i];
+}
+__global__ void ka_sum_levels(const double *x, double *out, int n, int K) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  double s = 0;
+  for (int k = 0; k < K; ++k)
+    s += x[size_t(i) * K + k];
+  out[i] = s;
 }
 __global__ void ka_pack(Dual *y, const double *v, const double *d,
                         long long n) {
@@ -929,7 +941,8 @@ extern "C" int swg_adjoint_create(swg_model md, int nsnapshots,
        (rc = zal(A, C * K, &w.ldiv)) || (rc = zal(A, V * K, &w.lz4)) ||
        (rc = zal(A, V * K, &w.lzeta)) || (rc = zal(A, V * K, &w.lhv)) ||
        (rc = zal(A, E * K, &w.lQ)) || (rc = zal(A, E * K, &w.lmh)) ||
-       (rc = zal(A, E * K, &w.lvnp)) || (rc = zal(A, E * K, &w.ld2u))))
+       (rc = zal(A, E * K, &w.lvnp)) || (rc = zal(A, E * K, &w.ld2u)) ||
+       (md->view.vel_del2 && (rc = zal(A, E * K, &w.gc2e)))))
     ;
   swg_state *st[] = {&ad->cur, &ad->next, &ad->X[0], &ad->X[1], &ad->X[2],
                      &ad->X[3], &ad->acc, &ad->lam, &ad->lacc, &ad->mu,
@@ -1064,13 +1077,12 @@ extern "C" int swg_tlm_apply(swg_adjoint ad, swg_state x0, swg_state dx,
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_tlm_apply");
 }
 
-extern "C" int swg_adj_forward(swg_adjoint ad, swg_state state0, double t0,
-                               double dt, int nsteps, swg_state final_out,
-                               void *stream) {
-  if (!ad || !same_layout(ad, state0) || !same_layout(ad, final_out) ||
-      nsteps < 1)
-    return fail(SWG_ERR_ARG, "swg_adj_forward: bad argument");
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
+namespace {
+
+// Resumable sweeps: one schedule action per call, so several members'
+// schedules can be interleaved on their own streams.
+int fwd_begin(swg_adjoint ad, swg_state state0, double t0, double dt,
+              int nsteps, cudaStream_t st) {
   ad->t0 = t0;
   ad->dt = dt;
   ad->nsteps = nsteps;
@@ -1079,17 +1091,66 @@ extern "C" int swg_adj_forward(swg_adjoint ad, swg_state state0, double t0,
   Planner pl(nsteps, ad->nsnap - 1);
   ad->actions.push_back({1, 0, 0});
   pl.gen(ad->actions, 0, nsteps, ad->nsnap - 1, 0, true);
-  TRY(swg_state_copy(ad->cur, state0, st));
-  // execute up to the first tape+adjoint action: that is step nsteps-1
-  size_t i = 0;
-  for (; i < ad->actions.size() && ad->actions[i].type != 3; ++i)
-    TRY(run_action(ad, ad->actions[i], st));
-  if (i == ad->actions.size() || ad->actions[i].a != nsteps - 1)
+  ad->pos = 0;
+  ad->state = 0;
+  return swg_state_copy(ad->cur, state0, st);
+}
+
+// the forward sweep runs the schedule up to its first tape+adjoint action
+// (step nsteps-1), then tapes that step, producing x_N
+int fwd_next(swg_adjoint ad, swg_state final_out, cudaStream_t st, bool *done) {
+  const AdjAction &a = ad->actions[ad->pos];
+  if (a.type != 3) {
+    ++ad->pos;
+    *done = false;
+    return run_action(ad, a, st);
+  }
+  if (a.a != ad->nsteps - 1)
     return fail(SWG_ERR_STATE, "swg_adj_forward: unexpected schedule");
-  TRY(tape_step(ad, dt, ad->next, st));
+  TRY(tape_step(ad, ad->dt, ad->next, st));
   TRY(swg_state_copy(final_out, ad->next, st));
-  ad->pos = i;
   ad->state = 1;
+  *done = true;
+  return SWG_OK;
+}
+
+int bwd_begin(swg_adjoint ad, swg_state lambda, cudaStream_t st) {
+  TRY(swg_state_copy(ad->lam, lambda, st));
+  if (ad->aw.gc2e) {
+    cudaError_t err = cudaMemsetAsync(
+        ad->aw.gc2e, 0,
+        sizeof(double) * ad->model->mesh->nedges * ad->model->mesh->nlayers, st);
+    if (err != cudaSuccess)
+      return cuda_fail(err, "swg_adj_backward: reset parameter gradient");
+  }
+  TRY(adjoint_step(ad, ad->dt, st)); // the last step is already taped
+  ++ad->pos;
+  return SWG_OK;
+}
+
+int bwd_next(swg_adjoint ad, swg_state lambda, cudaStream_t st, bool *done) {
+  if (ad->pos < ad->actions.size()) {
+    *done = false;
+    return run_action(ad, ad->actions[ad->pos++], st);
+  }
+  TRY(swg_state_copy(lambda, ad->lam, st));
+  ad->state = 0;
+  *done = true;
+  return SWG_OK;
+}
+
+} // namespace
+
+extern "C" int swg_adj_forward(swg_adjoint ad, swg_state state0, double t0,
+                               double dt, int nsteps, swg_state final_out,
+                               void *stream) {
+  if (!ad || !same_layout(ad, state0) || !same_layout(ad, final_out) ||
+      nsteps < 1)
+    return fail(SWG_ERR_ARG, "swg_adj_forward: bad argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  TRY(fwd_begin(ad, state0, t0, dt, nsteps, st));
+  for (bool done = false; !done;)
+    TRY(fwd_next(ad, final_out, st, &done));
   return SWG_OK;
 }
 
@@ -1100,13 +1161,68 @@ extern "C" int swg_adj_backward(swg_adjoint ad, swg_state lambda,
   if (ad->state != 1)
     return fail(SWG_ERR_STATE, "swg_adj_backward: call swg_adj_forward first");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  TRY(swg_state_copy(ad->lam, lambda, st));
-  // the last step is already taped
-  TRY(adjoint_step(ad, ad->dt, st));
-  for (size_t i = ad->pos + 1; i < ad->actions.size(); ++i)
-    TRY(run_action(ad, ad->actions[i], st));
-  TRY(swg_state_copy(lambda, ad->lam, st));
-  ad->state = 0;
+  TRY(bwd_begin(ad, lambda, st));
+  for (bool done = false; !done;)
+    TRY(bwd_next(ad, lambda, st, &done));
+  return SWG_OK;
+}
+
+extern "C" int swg_adj_batch_forward(int n, const swg_adjoint *adjs,
+                                     const swg_state *states0, double t0,
+                                     double dt, int nsteps,
+                                     const swg_state *finals,
+                                     void *const *streams) {
+  if (n < 1 || !adjs || !states0 || !finals || nsteps < 1)
+    return fail(SWG_ERR_ARG, "swg_adj_batch_forward: bad argument");
+  for (int m = 0; m < n; ++m)
+    if (!adjs[m] || !same_layout(adjs[m], states0[m]) ||
+        !same_layout(adjs[m], finals[m]))
+      return fail(SWG_ERR_ARG, "swg_adj_batch_forward: member mismatch");
+  auto S = [&](int m) {
+    return streams ? static_cast<cudaStream_t>(streams[m]) : cudaStream_t(0);
+  };
+  for (int m = 0; m < n; ++m)
+    TRY(fwd_begin(adjs[m], states0[m], t0, dt, nsteps, S(m)));
+  std::vector<char> done(n, 0);
+  for (int left = n; left > 0;)
+    for (int m = 0; m < n; ++m) {
+      if (done[m])
+        continue;
+      bool d = false;
+      TRY(fwd_next(adjs[m], finals[m], S(m), &d));
+      if (d) {
+        done[m] = 1;
+        --left;
+      }
+    }
+  return SWG_OK;
+}
+
+extern "C" int swg_adj_batch_backward(int n, const swg_adjoint *adjs,
+                                      const swg_state *lambdas,
+                                      void *const *streams) {
+  if (n < 1 || !adjs || !lambdas)
+    return fail(SWG_ERR_ARG, "swg_adj_batch_backward: bad argument");
+  for (int m = 0; m < n; ++m)
+    if (!adjs[m] || !same_layout(adjs[m], lambdas[m]) || adjs[m]->state != 1)
+      return fail(SWG_ERR_ARG, "swg_adj_batch_backward: member not ready");
+  auto S = [&](int m) {
+    return streams ? static_cast<cudaStream_t>(streams[m]) : cudaStream_t(0);
+  };
+  for (int m = 0; m < n; ++m)
+    TRY(bwd_begin(adjs[m], lambdas[m], S(m)));
+  std::vector<char> done(n, 0);
+  for (int left = n; left > 0;)
+    for (int m = 0; m < n; ++m) {
+      if (done[m])
+        continue;
+      bool d = false;
+      TRY(bwd_next(adjs[m], lambdas[m], S(m), &d));
+      if (d) {
+        done[m] = 1;
+        --left;
+      }
+    }
   return SWG_OK;
 }
 
@@ -1118,6 +1234,40 @@ extern "C" int swg_adj_info(swg_adjoint ad, long long *plain_steps,
     *plain_steps = ad->plain_steps;
   if (taped_steps)
     *taped_steps = ad->taped_steps;
+  return SWG_OK;
+}
+
+extern "C" int swg_adj_grad_visc(swg_adjoint ad, double *grad_edge,
+                                 double *grad_cell, void *stream) {
+  if (!ad)
+    return fail(SWG_ERR_ARG, "swg_adj_grad_visc: NULL");
+  if (!ad->aw.gc2e)
+    return fail(SWG_ERR_STATE, "swg_adj_grad_visc: the model has no del2 "
+                               "viscosity term");
+  swg_mesh me = ad->model->mesh;
+  const int E = me->nedges, C = me->ncells, K = me->nlayers;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // reuse the edge work array lQ as the per-edge sum
+  ka_sum_levels<<<(E + 255) / 256, 256, 0, st>>>(ad->aw.gc2e, ad->aw.lQ, E, K);
+  ++g_launches;
+  std::vector<double> ge(E);
+  cudaError_t err = cudaMemcpyAsync(ge.data(), ad->aw.lQ, E * sizeof(double),
+                                    cudaMemcpyDeviceToHost, st);
+  if (err == cudaSuccess)
+    err = cudaStreamSynchronize(st);
+  if (err != cudaSuccess)
+    return cuda_fail(err, "swg_adj_grad_visc");
+  // dL/d visc_edge = dL/dc2e (c2e = visc_del2 * scale2 = visc_edge); a
+  // per-cell field maps to edges as visc_e = (visc_c0 + visc_c1) / 2
+  if (grad_edge)
+    std::memcpy(grad_edge, ge.data(), E * sizeof(double));
+  if (grad_cell) {
+    std::fill(grad_cell, grad_cell + C, 0.0);
+    for (int e = 0; e < E; ++e) {
+      grad_cell[me->ce_h[2 * e]] += 0.5 * ge[e];
+      grad_cell[me->ce_h[2 * e + 1]] += 0.5 * ge[e];
+    }
+  }
   return SWG_OK;
 }
 

@@ -405,6 +405,10 @@ class Adjoint:
                                        C.byref(h)))
         self._h = h
 
+    @property
+    def handle(self):
+        return self._h
+
     def tlm_tendency(self, x, dx, dtend, stream=None):
         check(lib().swg_tlm_tendency(self._h, x.handle, dx.handle,
                                      dtend.handle, _s(stream)))
@@ -425,6 +429,14 @@ class Adjoint:
     def backward(self, lam, stream=None):
         check(lib().swg_adj_backward(self._h, lam.handle, _s(stream)))
 
+    def grad_visc(self, stream=None):
+        """(dL/dvisc per edge, dL/dvisc per cell) of the last backward."""
+        me = self.model.m_mesh
+        ge = np.empty(me.m_nedges)
+        gc = np.empty(me.m_ncells)
+        check(lib().swg_adj_grad_visc(self._h, _d(ge), _d(gc), _s(stream)))
+        return ge, gc
+
     def info(self):
         a, b = C.c_longlong(), C.c_longlong()
         check(lib().swg_adj_info(self._h, C.byref(a), C.byref(b)))
@@ -434,6 +446,32 @@ class Adjoint:
         if getattr(self, "_h", None) and _capi._lib is not None:
             _capi._lib.swg_adjoint_destroy(self._h)
             self._h = None
+
+
+def _handles(objs):
+    return (C.c_void_p * len(objs))(*[o.handle.value for o in objs])
+
+
+def _streams(streams, n):
+    if streams is None:
+        return None
+    return (C.c_void_p * n)(*[int(s) if s else None for s in streams])
+
+
+def adjoint_batch_forward(adjs, states0, t0, dt, nsteps, finals,
+                          streams=None):
+    """Forward sweeps of several members' adjoints, interleaved, member m on
+    streams[m] (raw cudaStream_t ints)."""
+    n = len(adjs)
+    check(lib().swg_adj_batch_forward(n, _handles(adjs), _handles(states0),
+                                      float(t0), float(dt), int(nsteps),
+                                      _handles(finals), _streams(streams, n)))
+
+
+def adjoint_batch_backward(adjs, lambdas, streams=None):
+    n = len(adjs)
+    check(lib().swg_adj_batch_backward(n, _handles(adjs), _handles(lambdas),
+                                       _streams(streams, n)))
 
 
 def checkpoint_cost(nsteps: int, nsnapshots: int) -> int:

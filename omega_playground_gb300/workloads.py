@@ -154,6 +154,44 @@ def loss_and_grad(h, vn, tr, region, h_ref: float = 1000.0):
     return L, (gh, np.zeros_like(vn), gtr)
 
 
+def lognormal_visc(ncells: int, seed: int, median: float = 1e3,
+                   sigma: float = 0.5) -> np.ndarray:
+    """Per-cell del2 viscosity, log-normal around `median` (Box-Muller on
+    SplitMix64 uniforms)."""
+    u = uniform(seed, 2 * ncells)
+    z = np.sqrt(-2.0 * np.log(u[:ncells] + 2.0**-60)) * \
+        np.cos(2 * np.pi * u[ncells:])
+    return median * np.exp(sigma * z)
+
+
+def visc_scaling(mesh, visc_cell: np.ndarray, visc_del2: float) -> np.ndarray:
+    """mesh_scaling_del2 realising a per-cell viscosity on edges:
+    visc_e = (visc_c0 + visc_c1) / 2 = visc_del2 * scale_e."""
+    coe = np.asarray(mesh.m_cells_on_edge if hasattr(mesh, "m_cells_on_edge")
+                     else mesh.tables["cells_on_edge"])
+    return 0.5 * (visc_cell[coe[:, 0]] + visc_cell[coe[:, 1]]) / visc_del2
+
+
+ADJOINT_ENSEMBLE_NX = (32, 64, 96, 128)
+
+
+def adjoint_ensemble(n: int = 32, seed: int = 20240603,
+                     nx_choices=ADJOINT_ENSEMBLE_NX, levels=(16, 64),
+                     nsteps: int = 300):
+    """Members of the batched adjoint: nx from `nx_choices`, levels uniform in
+    `levels`, 2 tracers, RK4, `nsteps` steps, del2 viscosity realised as a
+    per-cell log-normal field (see lognormal_visc)."""
+    r = uniform(seed, 2 * n).reshape(n, 2)
+    base = WORKLOADS["rk4_128x128_adjoint"]
+    out = []
+    for i in range(n):
+        nx = nx_choices[int(r[i, 0] * len(nx_choices))]
+        K = levels[0] + int(r[i, 1] * (levels[1] - levels[0] + 1))
+        out.append(base.scaled(name=f"adjmember{i}", nx=nx, ny=nx, nlayers=K,
+                               nsteps=nsteps, seed=seed + 1000 * i))
+    return out
+
+
 ENSEMBLE_NX = (32, 48, 64, 96, 128, 192)
 
 
