@@ -84,6 +84,10 @@ typedef struct swg_mesh_desc {
   const double *mesh_scaling_del2;   /* [E] or NULL */
   const double *mesh_scaling_del4;   /* [E] or NULL */
   const double *edge_mask;           /* [E][K] or NULL */
+  /* levels per column summed by the diagnostics
+   * (shallow_water_diagnostics.cpp:23,52,76); NULL = nlayers everywhere */
+  const int *max_level_cell;         /* [C] in [0, K] or NULL */
+  const int *max_level_vertex_bot;   /* [V] in [0, K] or NULL */
 } swg_mesh_desc;
 
 /* Host tables of the doubly periodic planar hexagonal mesh, identical to

@@ -37,7 +37,8 @@ class MeshDesc(C.Structure):
                 ("dc_edge", _dp), ("dv_edge", _dp), ("weights_on_edge", _dp),
                 ("area_triangle", _dp), ("kiteareas_on_vertex", _dp),
                 ("edge_sign_on_vertex", _dp), ("mesh_scaling_del2", _dp),
-                ("mesh_scaling_del4", _dp), ("edge_mask", _dp)]
+                ("mesh_scaling_del4", _dp), ("edge_mask", _dp),
+                ("max_level_cell", _ip), ("max_level_vertex_bot", _ip)]
 
 
 HEX_INT = ["nedges_on_cell", "edges_on_cell", "cells_on_cell",

@@ -77,6 +77,14 @@ bool in_range(const int *a, size_t n, int lo, int hi) {
   return true;
 }
 
+// true when a is NULL or every entry equals x
+bool all_equal(const int *a, size_t n, int x) {
+  for (size_t i = 0; a && i < n; ++i)
+    if (a[i] != x)
+      return false;
+  return true;
+}
+
 cudaStream_t as_stream(void *s) { return static_cast<cudaStream_t>(s); }
 
 int check_launch(const char *what) {
@@ -140,6 +148,10 @@ extern "C" int swg_mesh_create(const swg_mesh_desc *d, swg_mesh *out) {
   for (long long v = 0; v < V; ++v)
     if (!(d->area_triangle[v] > 0))
       return fail(SWG_ERR_ARG, "swg_mesh_create: area_triangle must be > 0");
+  if ((d->max_level_cell && !in_range(d->max_level_cell, C, 0, int(K) + 1)) ||
+      (d->max_level_vertex_bot &&
+       !in_range(d->max_level_vertex_bot, V, 0, int(K) + 1)))
+    return fail(SWG_ERR_ARG, "swg_mesh_create: max level out of [0, nlayers]");
 
   swg_mesh m = new (std::nothrow) swg_mesh_s();
   if (!m)
@@ -276,7 +288,11 @@ extern "C" int swg_mesh_create(const swg_mesh_desc *d, swg_mesh *out) {
       (rc = upload(A, m->scale4_h.data(), E, &mv.scale4)) ||
       (rc = upload(A, d->area_cell, C, &mv.area_cell_d)) ||
       (rc = upload(A, d->area_triangle, V, &mv.area_tri_d)) ||
-      (!mask_ones && (rc = upload(A, d->edge_mask, E * K, &mv.mask)))) {
+      (!mask_ones && (rc = upload(A, d->edge_mask, E * K, &mv.mask))) ||
+      (!all_equal(d->max_level_cell, C, int(K)) &&
+       (rc = upload(A, d->max_level_cell, C, &mv.maxlev_c))) ||
+      (!all_equal(d->max_level_vertex_bot, V, int(K)) &&
+       (rc = upload(A, d->max_level_vertex_bot, V, &mv.maxlev_v)))) {
     swg_mesh_destroy(m);
     return rc;
   }

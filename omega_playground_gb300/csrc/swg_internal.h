@@ -53,6 +53,8 @@ struct MeshView {
   const double *area_cell_d; // [C]
   const double *area_tri_d;  // [V]
   const double *dcs_v;       // [V][3] dc * edge_sign_on_vertex
+  const int *maxlev_c;       // [C] levels summed per cell, nullptr = nlayers
+  const int *maxlev_v;       // [V] levels summed per vertex, nullptr = nlayers
 };
 
 // Parameters and parameter-scaled coefficient tables of one model.
@@ -83,6 +85,9 @@ template <class T> struct AuxViewT {
   T *div, *ke, *d4;              // [C][K]
   T *ntr, *lap;                  // [T][C][K]
   T *F, *G, *Q, *mh, *u2, *d2u, *d2u4; // [E][K]
+  // written only when set (the adjoint's tape): 1/h_vertex [V][K], 1/h
+  // [C][K] and the PV-flux sum S1 = sum_j w_j F_j [E][K]
+  T *rhv, *rh, *S1;
 };
 using AuxView = AuxViewT<double>;
 

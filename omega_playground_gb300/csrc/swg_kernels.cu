@@ -120,6 +120,9 @@ __global__ void __launch_bounds__(TPB)
   for (long long i = blockIdx.x * (long long)TPB + threadIdx.x; i < n;
        i += (long long)gridDim.x * TPB) {
     const int ent = int(i / K), k = int(i - (long long)ent * K);
+    const int *maxlev = WHICH == 2 ? m.maxlev_v : m.maxlev_c;
+    if (maxlev && k >= maxlev[ent])
+      continue;
     if (WHICH == 0) { // mass: area_cell h
       s += m.area_cell_d[ent] * h[i];
     } else if (WHICH == 1) { // energy: area (g h^2/2 + h ke)

@@ -132,6 +132,8 @@ struct MPASMesh {
   std::vector<Int> m_edges_on_vertex, m_cells_on_vertex;
   std::vector<Real> m_area_triangle, m_x_vertex, m_y_vertex,
       m_kiteareas_on_vertex, m_edge_sign_on_vertex;
+  // levels per column for the diagnostics; empty = m_nlayers everywhere
+  std::vector<Int> m_max_level_cell, m_max_level_vertex_bot;
 
   // device copies of the geometry user kernels typically read
   DeviceArray<Real> d_x_cell, d_y_cell, d_x_edge, d_y_edge, d_angle_edge;
@@ -172,6 +174,10 @@ struct MPASMesh {
     d.mesh_scaling_del4 =
         m_mesh_scaling_del4.empty() ? nullptr : m_mesh_scaling_del4.data();
     d.edge_mask = m_edge_mask.empty() ? nullptr : m_edge_mask.data();
+    d.max_level_cell =
+        m_max_level_cell.empty() ? nullptr : m_max_level_cell.data();
+    d.max_level_vertex_bot =
+        m_max_level_vertex_bot.empty() ? nullptr : m_max_level_vertex_bot.data();
     swg_mesh_destroy(m_handle);
     m_handle = nullptr;
     swg_check(swg_mesh_create(&d, &m_handle));

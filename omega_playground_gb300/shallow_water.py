@@ -69,8 +69,29 @@ class MPASMesh:
         self.tables = {}
         self._h = None
 
+    @classmethod
+    def from_tables(cls, tables: dict, nlayers: int, **finalize_kw):
+        """A mesh from arbitrary MPAS tables (numpy arrays named like the
+        reference's members without ``m_``: nedges_on_cell [C], edges_on_cell
+        [C][6], nedges_on_edge [E], edges_on_edge [E][12], cells_on_edge,
+        vertices_on_edge [E][2], edges_on_vertex, cells_on_vertex [V][3],
+        area_cell, edge_sign_on_cell, dc_edge, dv_edge, weights_on_edge,
+        area_triangle, kiteareas_on_vertex, edge_sign_on_vertex)."""
+        m = cls.__new__(cls)
+        MPASMesh.__init__(m)
+        for k, v in tables.items():
+            dt = np.int32 if np.asarray(v).dtype.kind in "iu" else np.float64
+            m.tables[k] = np.ascontiguousarray(v, dt)
+        m.m_ncells = len(m.tables["nedges_on_cell"])
+        m.m_nedges = len(m.tables["nedges_on_edge"])
+        m.m_nvertices = len(m.tables["area_triangle"])
+        m.m_nlayers = int(nlayers)
+        m.finalize(**finalize_kw)
+        return m
+
     def finalize(self, mesh_scaling_del2=None, mesh_scaling_del4=None,
-                 edge_mask=None):
+                 edge_mask=None, max_level_cell=None,
+                 max_level_vertex_bot=None):
         t = self.tables
         d = _capi.MeshDesc()
         d.ncells, d.nedges, d.nvertices = self.m_ncells, self.m_nedges, \
@@ -90,6 +111,11 @@ class MPASMesh:
         d.mesh_scaling_del2 = _d(self._keep[0])
         d.mesh_scaling_del4 = _d(self._keep[1])
         d.edge_mask = _d(self._keep[2])
+        self._keep_i = [np.ascontiguousarray(x, np.int32) if x is not None
+                        else None for x in (max_level_cell,
+                                            max_level_vertex_bot)]
+        d.max_level_cell = _i(self._keep_i[0])
+        d.max_level_vertex_bot = _i(self._keep_i[1])
         h = C.c_void_p()
         check(lib().swg_mesh_create(C.byref(d), C.byref(h)))
         self._h = h

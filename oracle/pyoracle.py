@@ -51,7 +51,8 @@ class _Mesh(C.Structure):
                  ("nlayers", C.c_int), ("dc", C.c_double),
                  ("period_x", C.c_double), ("period_y", C.c_double)]
                 + [(n, _ip) for n, _, _ in _MESH_INT]
-                + [(n, _dp) for n, _, _ in _MESH_DBL])
+                + [(n, _dp) for n, _, _ in _MESH_DBL]
+                + [("max_level_cell", _ip), ("max_level_vertex_bot", _ip)])
 
 
 class _Params(C.Structure):
@@ -143,6 +144,17 @@ class OracleMesh:
             setattr(self._s, name, _ptr(self.tables[name], C.c_double))
         lib().or_planar_hex_build(C.byref(self._s), nx, ny, self.dc, nlayers)
         self.period_x, self.period_y = self._s.period_x, self._s.period_y
+
+    def set_max_levels(self, max_level_cell=None, max_level_vertex_bot=None):
+        """Per-column level counts for the diagnostics (None = nlayers)."""
+        for name, a in (("max_level_cell", max_level_cell),
+                        ("max_level_vertex_bot", max_level_vertex_bot)):
+            if a is None:
+                self.tables.pop(name, None)
+                setattr(self._s, name, None)
+            else:
+                self.tables[name] = np.ascontiguousarray(a, np.int32)
+                setattr(self._s, name, _ptr(self.tables[name], C.c_int))
 
     def __getattr__(self, name):
         t = self.__dict__.get("tables")

@@ -786,7 +786,7 @@ double or_energy_integral(or_model *md, const double *h, const double *vn) {
   const int K = m->nlayers;
   double total = 0;
   for (int c = 0; c < m->ncells; ++c)
-    for (int k = 0; k < K; ++k) {
+    for (int k = 0; k < (m->max_level_cell ? m->max_level_cell[c] : K); ++k) {
       double KE = 0;
       for (int j = 0; j < m->nedges_on_cell[c]; ++j) {
         const int je = m->edges_on_cell[6 * c + j];
@@ -807,7 +807,7 @@ double or_mass_integral(or_model *md, const double *h) {
   const int K = m->nlayers;
   double total = 0;
   for (int c = 0; c < m->ncells; ++c)
-    for (int k = 0; k < K; ++k)
+    for (int k = 0; k < (m->max_level_cell ? m->max_level_cell[c] : K); ++k)
       total += m->area_cell[c] * h[(size_t)c * K + k];
   return total;
 }
@@ -818,7 +818,8 @@ double or_circulation_integral(or_model *md, const double *vn) {
   const int K = m->nlayers;
   double total = 0;
   for (int v = 0; v < m->nvertices; ++v)
-    for (int k = 0; k < K; ++k) {
+    for (int k = 0;
+         k < (m->max_level_vertex_bot ? m->max_level_vertex_bot[v] : K); ++k) {
       double cir = -0.0;
       for (int j = 0; j < 3; ++j) {
         const int je = m->edges_on_vertex[3 * v + j];

@@ -46,6 +46,9 @@ typedef struct or_mesh {
   double *area_triangle, *x_vertex, *y_vertex;
   double *kiteareas_on_vertex; /* [V][3] */
   double *edge_sign_on_vertex; /* [V][3] */
+  /* levels per column summed by the diagnostics; NULL = nlayers */
+  int *max_level_cell;         /* [C] */
+  int *max_level_vertex_bot;   /* [V] */
 } or_mesh;
 
 /* ShallowWaterParams (src/model/shallow_water_params.hpp:7-18). */

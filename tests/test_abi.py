@@ -71,6 +71,20 @@ def test_mesh_create_rejects_bad_sizes_and_nulls():
     assert _capi.lib().swg_mesh_create(C.byref(d), C.byref(out)) == 1
 
 
+def test_mesh_create_rejects_max_levels_out_of_range():
+    d, t = _desc_for(4, 4, 2)
+    ml = np.full(16, 2, np.int32)
+    ml[7] = 3  # > nlayers
+    d.max_level_cell = ml.ctypes.data_as(C.POINTER(C.c_int))
+    out = C.c_void_p()
+    assert _capi.lib().swg_mesh_create(C.byref(d), C.byref(out)) == 1
+    assert b"max level" in _capi.lib().swg_last_error()
+    d, t = _desc_for(4, 4, 2)
+    mv = np.full(32, -1, np.int32)
+    d.max_level_vertex_bot = mv.ctypes.data_as(C.POINTER(C.c_int))
+    assert _capi.lib().swg_mesh_create(C.byref(d), C.byref(out)) == 1
+
+
 def test_null_handles_are_errors_not_crashes():
     lib = _capi.lib()
     assert lib.swg_state_create(None, 0, C.byref(C.c_void_p())) == 1
