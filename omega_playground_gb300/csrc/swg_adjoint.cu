@@ -46,8 +46,10 @@ struct AdjView {
   const double *keadj, *d4adj, *hsadj, *divadj;    // transposed edge terms
   const int *cvtx;                                 // vertices of the cell
   const double *ckvh;                              // their kite weight for c
+  const double *hm_c;                              // 0.5 on edges, 0 on padding
   // edges [E][2]: coefficients of cells (c0, c1) / vertices (v0, v1) for e
   const double *ccd_e2, *ccdh_e2, *cke_e2, *ckq_e2, *kd2_e2, *cvr_e2;
+  const double *ccdh2_e2, *cke2_e2;                // 2 ccdh_e2, 2 cke_e2
   // transposed edges-on-edge [E][nt] with weights / 4
   const int *eoeT;
   const double *woeT;
@@ -61,6 +63,7 @@ struct AdjWork {
   double *lke, *ld4, *lhs, *lhtr, *ldiv; // [C][K]
   double *lz4, *lzeta, *lhv;            // [V][K]
   double *lQ, *lmh, *lvnp, *ld2u;       // [E][K]
+  double *Qmu;                          // [E][K] Q mu_vn of the stage
   double *gc2e; // [E][K] accumulated dL/d(visc_del2 * mesh_scaling_del2), or null
 };
 
@@ -88,12 +91,20 @@ __device__ __forceinline__ void emit(double *out, double *acc, double *nmu,
 }
 
 // --- pass 1: transposed edge stencils of the velocity tendency (cells and
-// vertices); the first V*K threads take vertices.
+// vertices), and Q mu_vn per edge for the transposed PV flux; the first V*K
+// threads take vertices, the next C*K cells, the last E*K edges.
 __global__ void __launch_bounds__(ATPB)
-    ka_vel(MeshView m, ModelView p, AdjView v, AdjWork w, AdjIO io) {
+    ka_vel(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
+           AdjIO io) {
   const int K = m.nlayers;
   unsigned i = blockIdx.x * ATPB + threadIdx.x;
   const unsigned VK = unsigned(m.nvertices) * K, CK = unsigned(m.ncells) * K;
+  if (i >= VK + CK) {
+    i -= VK + CK;
+    if (i < unsigned(m.nedges) * K)
+      w.Qmu[i] = a.Q[i] * io.mvn[i];
+    return;
+  }
   if (i < VK) {
     if (!p.vel_del4)
       return;
@@ -106,8 +117,6 @@ __global__ void __launch_bounds__(ATPB)
     return;
   }
   i -= VK;
-  if (i >= CK)
-    return;
   const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
   double ke = 0, d4 = 0, hs = 0;
   for (int j = 0; j < MAXE; ++j) {
@@ -123,11 +132,24 @@ __global__ void __launch_bounds__(ATPB)
     w.ld4[i] = d4;
 }
 
-__device__ __forceinline__ double mean_h(const MeshView &m, const double *h,
-                                         int e, int k) {
+// mean thickness of edge e (the forward's value: taped, or recomputed)
+__device__ __forceinline__ double mean_h(const MeshView &m, const AuxView &a,
+                                         const double *h, int e, int k) {
   const int K = m.nlayers;
+  if (a.mh)
+    return a.mh[size_t(e) * K + k];
   return 0.5 * (h[size_t(__ldg(m.ce + 2 * e)) * K + k] +
                 h[size_t(__ldg(m.ce + 2 * e + 1)) * K + k]);
+}
+
+// the forward's Newton reciprocal of x
+__device__ __forceinline__ double fwd_rcp(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
 }
 
 // --- pass 2: tracer tendency transposed to the normalised tracers (partial)
@@ -150,7 +172,7 @@ __global__ void __launch_bounds__(ATPB)
     double x = __ldg(v.ccdh_nb + 6 * c + j) * F;
     double own = __ldg(m.ccdh + 6 * c + j) * F;
     if (p.tr_del2) {
-      const double mh = mean_h(m, io.h, e, k);
+      const double mh = mean_h(m, a, io.h, e, k);
       x = fma(__ldg(v.kd2_nb + 6 * c + j), mh, x);
       own = fma(-__ldg(p.kd2 + 6 * c + j), mh, own);
     }
@@ -188,21 +210,13 @@ __global__ void __launch_bounds__(ATPB)
   if (p.tr_del4)
     for (int j = 0; j < MAXE; ++j) {
       const int e = __ldg(m.ec + 6 * c + j);
-      const double mh = mean_h(m, io.h, e, k);
+      const double mh = mean_h(m, a, io.h, e, k);
       nb[j] = __ldg(m.nbc + 6 * c + j);
       mnb[j] = __ldg(v.ckq_nb + 6 * c + j) * mh;
       M = fma(__ldg(m.ckq + 6 * c + j), mh, M);
     }
-  // 1/h: the forward's own reciprocal
-  double r;
-  {
-    double x = io.h[i];
-    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
-    double e = fma(-x, r, 1.0);
-    r = fma(r, e, r);
-    e = fma(-x, r, 1.0);
-    r = fma(r, e, r);
-  }
+  // 1/h: the forward's own reciprocal (taped, or recomputed)
+  const double r = a.rh ? a.rh[i] : fwd_rcp(io.h[i]);
   double hsum = 0;
   for (int l = 0; l < p.ntracers; ++l) {
     const size_t t = size_t(l) * CK + i;
@@ -240,23 +254,27 @@ __global__ void __launch_bounds__(ATPB)
     // PV flux: t_e = Q_e S1_e + S2_e, S1 = sum w F_j, S2 = sum w G_j
     double lG = 0, lFq = 0;
     for (int t = 0; t < v.nt; ++t) {
-      const int es = __ldg(v.eoeT + v.nt * e + t);
+      const size_t is = size_t(__ldg(v.eoeT + v.nt * e + t)) * K + k;
       const double ws = __ldg(v.woeT + v.nt * e + t);
-      const double mus = io.mvn[size_t(es) * K + k];
-      lG = fma(ws, mus, lG);
-      lFq = fma(ws, a.Q[size_t(es) * K + k] * mus, lFq);
+      lG = fma(ws, io.mvn[is], lG);
+      lFq = fma(ws, w.Qmu[is], lFq);
     }
-    double S1 = 0;
-    for (int j = 0; j < NE; ++j)
-      S1 = fma(__ldg(m.woe + NE * e + j),
-               a.F[size_t(__ldg(m.eoe + NE * e + j)) * K + k], S1);
+    double S1;
+    if (a.S1) {
+      S1 = a.S1[i];
+    } else {
+      S1 = 0;
+      for (int j = 0; j < NE; ++j)
+        S1 = fma(__ldg(m.woe + NE * e + j),
+                 a.F[size_t(__ldg(m.eoe + NE * e + j)) * K + k], S1);
+    }
     const double Q = a.Q[i], mu = io.mvn[i];
     w.lQ[i] = fma(S1, mu, F * lG);
     lF = fma(Q, lG, lFq);
-    // kinetic energy from vn^2
-    const double lu2 = fma(__ldg(v.cke_e2 + 2 * e), w.lke[i0],
-                           __ldg(v.cke_e2 + 2 * e + 1) * w.lke[i1]);
-    w.lvnp[i] = 2.0 * u * lu2; // mean-h term added below
+    // kinetic energy from vn^2 (the factor 2 of d(vn^2) is in cke2_e2)
+    const double lu2 = fma(__ldg(v.cke2_e2 + 2 * e), w.lke[i0],
+                           __ldg(v.cke2_e2 + 2 * e + 1) * w.lke[i1]);
+    w.lvnp[i] = u * lu2; // mean-h term added below
     if (p.vel_del2 | p.vel_del4) {
       const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
       double d = p.vel_del2 ? __ldg(p.c2e + e) * mu : 0.0;
@@ -275,7 +293,8 @@ __global__ void __launch_bounds__(ATPB)
   }
   const double g0 = __ldg(v.ccdh_e2 + 2 * e), g1 = __ldg(v.ccdh_e2 + 2 * e + 1);
   if (p.do_h)
-    lF = fma(2.0 * g0, io.mh_[i0], fma(2.0 * g1, io.mh_[i1], lF));
+    lF = fma(__ldg(v.ccdh2_e2 + 2 * e), io.mh_[i0],
+             fma(__ldg(v.ccdh2_e2 + 2 * e + 1), io.mh_[i1], lF));
   if (p.ntracers > 0) {
     const double k20 = __ldg(v.kd2_e2 + 2 * e), k21 = __ldg(v.kd2_e2 + 2 * e + 1);
     const double q0 = __ldg(v.ckq_e2 + 2 * e), q1 = __ldg(v.ckq_e2 + 2 * e + 1);
@@ -291,7 +310,7 @@ __global__ void __launch_bounds__(ATPB)
         lmh = fma(dn, fma(q0, w.lL[b + i0], -(q1 * w.lL[b + i1])), lmh);
     }
   }
-  const double mh = mean_h(m, io.h, e, k);
+  const double mh = mean_h(m, a, io.h, e, k);
   lmh = fma(u, lF, lmh);
   w.lmh[i] = lmh;
   w.lvnp[i] = fma(mh, lF, w.lvnp[i]);
@@ -306,21 +325,26 @@ __global__ void __launch_bounds__(ATPB)
   if (i >= unsigned(m.nvertices) * K)
     return;
   const int vx = int(i / unsigned(K)), k = int(i - unsigned(vx) * K);
-  double lq = 0, hv = 0, lz = 0;
-  for (int j = 0; j < 3; ++j) {
-    const int e = __ldg(m.ev + 3 * vx + j);
-    lq += w.lQ[size_t(e) * K + k];
-    hv = fma(__ldg(m.kvh + 3 * vx + j),
-             io.h[size_t(__ldg(m.cv + 3 * vx + j)) * K + k], hv);
-    if (p.vel_del2 | p.vel_del4)
-      lz = fma(__ldg(v.zetaadj + 3 * vx + j), w.ld2u[size_t(e) * K + k], lz);
+  const int e0 = __ldg(m.ev + 3 * vx), e1 = __ldg(m.ev + 3 * vx + 1),
+            e2 = __ldg(m.ev + 3 * vx + 2);
+  const double lq = w.lQ[size_t(e0) * K + k] + w.lQ[size_t(e1) * K + k] +
+                    w.lQ[size_t(e2) * K + k];
+  double lz = 0;
+  if (p.vel_del2 | p.vel_del4) {
+    lz = __ldg(v.zetaadj + 3 * vx) * w.ld2u[size_t(e0) * K + k];
+    lz = fma(__ldg(v.zetaadj + 3 * vx + 1), w.ld2u[size_t(e1) * K + k], lz);
+    lz = fma(__ldg(v.zetaadj + 3 * vx + 2), w.ld2u[size_t(e2) * K + k], lz);
   }
-  double r;
-  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(hv));
-  double er = fma(-hv, r, 1.0);
-  r = fma(r, er, r);
-  er = fma(-hv, r, 1.0);
-  r = fma(r, er, r);
+  double r; // 1/h_vertex: the forward's value (taped, or recomputed)
+  if (a.rhv) {
+    r = a.rhv[i];
+  } else {
+    double hv = __ldg(m.kvh + 3 * vx) * io.h[size_t(__ldg(m.cv + 3 * vx)) * K + k];
+    for (int j = 1; j < 3; ++j)
+      hv = fma(__ldg(m.kvh + 3 * vx + j),
+               io.h[size_t(__ldg(m.cv + 3 * vx + j)) * K + k], hv);
+    r = fwd_rcp(hv);
+  }
   w.lzeta[i] = fma(r, lq, lz);
   w.lhv[i] = -(a.q[i] * r * lq);
 }
@@ -333,10 +357,10 @@ __global__ void __launch_bounds__(ATPB)
   if (i >= unsigned(m.ncells) * K)
     return;
   const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
-  double lh = 0, ld = 0, smh = 0;
+  double lh = 0, ld = 0;
   for (int j = 0; j < MAXE; ++j) {
     const int e = __ldg(m.ec + 6 * c + j);
-    smh += w.lmh[size_t(e) * K + k] * (__ldg(m.ccd + 6 * c + j) != 0.0);
+    lh = fma(__ldg(v.hm_c + 6 * c + j), w.lmh[size_t(e) * K + k], lh);
     if (p.do_vn) {
       lh = fma(__ldg(v.ckvh + 6 * c + j),
                w.lhv[size_t(__ldg(v.cvtx + 6 * c + j)) * K + k], lh);
@@ -344,7 +368,6 @@ __global__ void __launch_bounds__(ATPB)
         ld = fma(__ldg(v.divadj + 6 * c + j), w.ld2u[size_t(e) * K + k], ld);
     }
   }
-  lh = fma(0.5, smh, lh);
   if (p.do_vn)
     lh += w.lhs[i];
   if (p.ntracers > 0)
@@ -506,7 +529,8 @@ int build_tables(swg_adjoint ad) {
       divadj(6 * C, 0), ckvh(6 * C, 0);
   std::vector<int> cvtx(6 * C, 0);
   std::vector<double> ccd_e2(2 * E), ccdh_e2(2 * E), cke_e2(2 * E),
-      ckq_e2(2 * E), kd2_e2(2 * E), cvr_e2(2 * E), z4adj(3 * V), zetaadj(3 * V);
+      ckq_e2(2 * E), kd2_e2(2 * E), cvr_e2(2 * E), z4adj(3 * V), zetaadj(3 * V),
+      ccdh2_e2(2 * E), cke2_e2(2 * E), hm_c(6 * C, 0);
   auto kd2 = [&](int c, int j) {
     return P.eddy_diff2 * me->scale2_h[me->ec_h[6 * c + j]] * me->ckq_h[6 * c + j];
   };
@@ -515,6 +539,8 @@ int build_tables(swg_adjoint ad) {
   };
   for (int c = 0; c < C; ++c)
     for (int j = 0; j < MAXE; ++j) {
+      if (me->ccd_h[6 * c + j] != 0.0)
+        hm_c[6 * c + j] = 0.5;
       if (me->ccd_h[6 * c + j] == 0.0 && me->ckq_h[6 * c + j] == 0.0)
         continue; // padding slot
       const int e = me->ec_h[6 * c + j], n = me->nbc_h[6 * c + j];
@@ -555,6 +581,8 @@ int build_tables(swg_adjoint ad) {
       ccd_e2[2 * e + s] = me->ccd_h[6 * c + j];
       ccdh_e2[2 * e + s] = me->ccdh_h[6 * c + j];
       cke_e2[2 * e + s] = me->cke_h[6 * c + j];
+      cke2_e2[2 * e + s] = 2.0 * me->cke_h[6 * c + j];
+      ccdh2_e2[2 * e + s] = 2.0 * me->ccdh_h[6 * c + j];
       ckq_e2[2 * e + s] = me->ckq_h[6 * c + j];
       kd2_e2[2 * e + s] = kd2(c, j);
       cvr_e2[2 * e + s] = me->cvr_h[3 * v + jv];
@@ -604,7 +632,9 @@ int build_tables(swg_adjoint ad) {
       (rc = up(A, cke_e2, &a.cke_e2)) || (rc = up(A, ckq_e2, &a.ckq_e2)) ||
       (rc = up(A, kd2_e2, &a.kd2_e2)) || (rc = up(A, cvr_e2, &a.cvr_e2)) ||
       (rc = up(A, eoeT, &a.eoeT)) || (rc = up(A, woeT, &a.woeT)) ||
-      (rc = up(A, z4adj, &a.z4adj)) || (rc = up(A, zetaadj, &a.zetaadj)))
+      (rc = up(A, z4adj, &a.z4adj)) || (rc = up(A, zetaadj, &a.zetaadj)) ||
+      (rc = up(A, hm_c, &a.hm_c)) || (rc = up(A, ccdh2_e2, &a.ccdh2_e2)) ||
+      (rc = up(A, cke2_e2, &a.cke2_e2)))
     return rc;
   a.nt = nt;
   return SWG_OK;
@@ -636,6 +666,28 @@ template <class T> int alloc_aux_like(swg_adjoint ad, AuxViewT<T> &d) {
   return SWG_OK;
 }
 
+// tape of stage s: the model's intermediates plus what the adjoint passes
+// would otherwise recompute (1/h_vertex, 1/h, mean thickness, and for the
+// stages whose final passes run in the taped step, the PV sum S1)
+int alloc_tape(swg_adjoint ad, int s) {
+  swg_model md = ad->model;
+  const size_t C = md->mesh->ncells, E = md->mesh->nedges,
+               V = md->mesh->nvertices, K = md->mesh->nlayers;
+  AuxView &t = ad->taux[s];
+  auto &A = ad->allocs;
+  TRY(alloc_aux_like(ad, t));
+  if (md->view.do_vn) {
+    TRY(zal(A, V * K, &t.rhv));
+    if (s < 3)
+      TRY(zal(A, E * K, &t.S1));
+  }
+  if (md->params.ntracers > 0)
+    TRY(zal(A, C * K, &t.rh));
+  if (!t.mh)
+    TRY(zal(A, E * K, &t.mh));
+  return SWG_OK;
+}
+
 // lambda = J(X)^T mu with the intermediates of X already in `aux`
 void adj_passes(swg_adjoint ad, const AuxView &aux, const AdjIO &io,
                 cudaStream_t st) {
@@ -647,7 +699,7 @@ void adj_passes(swg_adjoint ad, const AuxView &aux, const AdjIO &io,
   const AdjView &v = ad->av;
   const AdjWork &w = ad->aw;
   if (p.do_vn) {
-    ka_vel<<<nb(VK + CK), ATPB, 0, st>>>(m, p, v, w, io);
+    ka_vel<<<nb(VK + CK + EK), ATPB, 0, st>>>(m, p, aux, v, w, io);
     ++g_launches;
   }
   if (p.ntracers > 0) {
@@ -942,6 +994,7 @@ extern "C" int swg_adjoint_create(swg_model md, int nsnapshots,
        (rc = zal(A, V * K, &w.lzeta)) || (rc = zal(A, V * K, &w.lhv)) ||
        (rc = zal(A, E * K, &w.lQ)) || (rc = zal(A, E * K, &w.lmh)) ||
        (rc = zal(A, E * K, &w.lvnp)) || (rc = zal(A, E * K, &w.ld2u)) ||
+       (rc = zal(A, E * K, &w.Qmu)) ||
        (md->view.vel_del2 && (rc = zal(A, E * K, &w.gc2e)))))
     ;
   swg_state *st[] = {&ad->cur, &ad->next, &ad->X[0], &ad->X[1], &ad->X[2],
@@ -959,10 +1012,9 @@ extern "C" int swg_adjoint_create(swg_model md, int nsnapshots,
     rc = swg_stepper_create(md, SWG_STEPPER_RK4, 4, &ad->stepper);
   const size_t n = words(md);
   if (rc == SWG_OK && ((rc = alloc_aux_like(ad, ad->daux)) ||
-                       (rc = alloc_aux_like(ad, ad->taux[0])) ||
-                       (rc = alloc_aux_like(ad, ad->taux[1])) ||
-                       (rc = alloc_aux_like(ad, ad->taux[2])) ||
-                       (rc = alloc_aux_like(ad, ad->taux[3])) || (rc = zal(A, n, &ad->dS)) ||
+                       (rc = alloc_tape(ad, 0)) || (rc = alloc_tape(ad, 1)) ||
+                       (rc = alloc_tape(ad, 2)) || (rc = alloc_tape(ad, 3)) ||
+                       (rc = zal(A, n, &ad->dS)) ||
                        (rc = zal(A, n, &ad->dacc)) || (rc = zal(A, n, &ad->dP0)) ||
                        (rc = zal(A, n, &ad->dP1)) || (rc = zal(A, n, &ad->dT))))
     ;

@@ -97,7 +97,10 @@ pt_vertex(const MeshView &m, const ModelView &p, const AuxViewT<T> &a,
     z = fma(__ldg(m.cvr + 3 * v + j), vn[size_t(e) * K + k], z);
     hv = fma(__ldg(m.kvh + 3 * v + j), h[size_t(c) * K + k], hv);
   }
-  a.q[i] = (z + __ldg(p.f_vertex + v)) * rcp_nr(hv);
+  const T r = rcp_nr(hv);
+  a.q[i] = (z + __ldg(p.f_vertex + v)) * r;
+  if (a.rhv)
+    a.rhv[i] = r;
   if (p.vel_del2 | p.vel_del4)
     a.zeta[i] = z;
 }
@@ -122,6 +125,8 @@ pt_cell1(const MeshView &m, const ModelView &p, const AuxViewT<T> &a,
   }
   if (p.ntracers > 0) {
     const T r = rcp_nr(h[i]);
+    if (a.rh)
+      a.rh[i] = r;
     for (int l = 0; l < p.ntracers; ++l) {
       const size_t t = size_t(l) * CK + i;
       a.ntr[t] = tr[t] * r;
@@ -142,7 +147,7 @@ pt_edge1(const MeshView &m, const ModelView &p, const AuxViewT<T> &a,
   const T u = vn[i];
   const T F = mh * u;
   a.F[i] = F;
-  if (p.ntracers > 0 && (p.tr_del2 | p.tr_del4))
+  if (a.mh) // allocated for tracer diffusion, and in the adjoint's tape
     a.mh[i] = mh;
   if (p.do_vn) {
     const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
@@ -254,6 +259,8 @@ __device__ __forceinline__ void pt_edge_final(const MeshView &m,
     S1 = fma(w, a.F[size_t(je) * K + k], S1);
     S2 = fma(w, a.G[size_t(je) * K + k], S2);
   }
+  if (a.S1)
+    a.S1[i] = S1;
   T t = fma(a.Q[i], S1, S2);
   const int c0 = __ldg(m.ce + 2 * e), c1 = __ldg(m.ce + 2 * e + 1);
   const double idc = __ldg(m.inv_dc + e);
