@@ -51,6 +51,10 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--nx", type=int, default=0,
                     help="override nx = ny (small profiling cases)")
+    ap.add_argument("--adjoint-steps", type=int, default=0,
+                    help="rk4_128x128_adjoint: override the 1000 steps")
+    ap.add_argument("--snapshots", type=int, default=0,
+                    help="rk4_128x128_adjoint: override the 32 snapshots")
     return ap.parse_args()
 
 
@@ -212,18 +216,22 @@ def run_reference(args, wl):
 
 # ---------------------------------------------------------- GPU arm -------
 
-def adjoint_ratio(stream):
+def adjoint_ratio(stream, nsteps=0, nsnap=0):
     """Checkpointed adjoint of the 128x128x32, 2-tracer RK4 workload (1000
     steps, 32 snapshots): device time of the forward sweep (checkpoints +
     taped last step) plus the backward sweep, over a plain 1000-step forward
     on the same GPU.  The region loss and its gradient (host) are outside
-    both timings."""
+    both timings.  nsteps / nsnap override the step and snapshot counts
+    (small profiling cases)."""
     import torch
     import omega_playground_gb300 as og
     from omega_playground_gb300.workloads import (ADJOINT_SNAPSHOTS, WORKLOADS,
                                                   initial_state, loss_and_grad,
                                                   region_cells)
     wl = WORKLOADS["rk4_128x128_adjoint"]
+    if nsteps:
+        wl = wl.scaled(nsteps=nsteps)
+    nsnap = nsnap or ADJOINT_SNAPSHOTS
     mesh = og.PlanarHexagonalMesh(wl.nx, wl.ny, wl.dc, wl.nlayers)
     params = wl.params()
     model = og.ShallowWaterModel(mesh, params)
@@ -242,7 +250,7 @@ def adjoint_ratio(stream):
     ev[1].record(stream)
     torch.cuda.synchronize()
     fwd_ms = ev[0].elapsed_time(ev[1])
-    adj = og.Adjoint(model, ADJOINT_SNAPSHOTS)
+    adj = og.Adjoint(model, nsnap)
     X0 = og.ShallowWaterState(mesh, params)
     X0.upload(*x0)
     XN = og.ShallowWaterState(mesh, params)
@@ -266,7 +274,7 @@ def adjoint_ratio(stream):
     plain, taped = adj.info()
     grad = G.download(stream=sh)
     return {"workload": wl.name, "steps": wl.nsteps,
-            "snapshots": ADJOINT_SNAPSHOTS, "plain_forward_ms": fwd_ms,
+            "snapshots": nsnap, "plain_forward_ms": fwd_ms,
             "checkpointed_forward_ms": f_ms, "backward_ms": b_ms,
             "ratio": (f_ms + b_ms) / fwd_ms, "plain_advances": plain,
             "taped_steps": taped, "loss": L,
@@ -611,6 +619,25 @@ def run_adjoint_ensemble(args):
     print(json.dumps(line), flush=True)
 
 
+def run_adjoint(args):
+    """The checkpointed adjoint alone: the time ratio as the line's value."""
+    import torch
+    torch.cuda.set_device(0)
+    a = adjoint_ratio(torch.cuda.current_stream(), args.adjoint_steps,
+                      args.snapshots)
+    line = {"metric": METRIC, "value": a["ratio"],
+            "unit": "adjoint/forward time ratio", "n_gpus": 1,
+            "steps": a["steps"], "warmup": 3,
+            "ms_per_step": (a["checkpointed_forward_ms"] + a["backward_ms"])
+            / a["steps"], "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": "rk4_128x128_adjoint", "nx": 128, "ny": 128,
+                       "nlayers": 32, "ntracers": 2, "stepper": "rk4",
+                       "snapshots": a["snapshots"]},
+            "adjoint": a}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "ensemble64":
@@ -618,6 +645,9 @@ def main():
         return
     if args.workload == "adjoint_ensemble32":
         run_adjoint_ensemble(args)
+        return
+    if args.workload == "rk4_128x128_adjoint":
+        run_adjoint(args)
         return
     from omega_playground_gb300.workloads import WORKLOADS
     wl = WORKLOADS[args.workload]

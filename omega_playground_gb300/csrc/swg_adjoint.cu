@@ -170,14 +170,13 @@ __global__ void __launch_bounds__(ATPB)
     nb[j] = __ldg(m.nbc + 6 * c + j);
     const double F = a.F[size_t(e) * K + k];
     double x = __ldg(v.ccdh_nb + 6 * c + j) * F;
-    double own = __ldg(m.ccdh + 6 * c + j) * F;
+    wc = fma(__ldg(m.ccdh + 6 * c + j), F, wc);
     if (p.tr_del2) {
       const double mh = mean_h(m, a, io.h, e, k);
       x = fma(__ldg(v.kd2_nb + 6 * c + j), mh, x);
-      own = fma(-__ldg(p.kd2 + 6 * c + j), mh, own);
+      wc = fma(-__ldg(p.kd2 + 6 * c + j), mh, wc);
     }
     wnb[j] = x;
-    wc += own;
   }
   for (int l = 0; l < p.ntracers; ++l) {
     const double *mu = io.mtr + size_t(l) * CK;
@@ -235,8 +234,10 @@ __global__ void __launch_bounds__(ATPB)
 }
 
 // --- pass 4: edges: PV flux (transposed edges-on-edge), thickness flux,
-// mean thickness, kinetic energy, edge Laplacian.
-template <int NE>
+// mean thickness, kinetic energy, edge Laplacian.  TRD: tracer diffusion
+// on (a compile-time switch: with a runtime flag the compiler evaluated the
+// diffusion products speculatively, 9 wasted FP64 instructions per edge).
+template <int NE, bool TRD>
 __global__ void __launch_bounds__(ATPB)
     ka_edge(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
             AdjIO io) {
@@ -295,19 +296,19 @@ __global__ void __launch_bounds__(ATPB)
   if (p.do_h)
     lF = fma(__ldg(v.ccdh2_e2 + 2 * e), io.mh_[i0],
              fma(__ldg(v.ccdh2_e2 + 2 * e + 1), io.mh_[i1], lF));
-  if (p.ntracers > 0) {
-    const double k20 = __ldg(v.kd2_e2 + 2 * e), k21 = __ldg(v.kd2_e2 + 2 * e + 1);
-    const double q0 = __ldg(v.ckq_e2 + 2 * e), q1 = __ldg(v.ckq_e2 + 2 * e + 1);
-    for (int l = 0; l < p.ntracers; ++l) {
-      const size_t b = size_t(l) * CK;
-      const double n0 = a.ntr[b + i0], n1 = a.ntr[b + i1];
-      const double m0 = io.mtr[b + i0], m1 = io.mtr[b + i1];
-      lF = fma(n0 + n1, fma(g0, m0, g1 * m1), lF);
+  for (int l = 0; l < p.ntracers; ++l) {
+    const size_t b = size_t(l) * CK;
+    const double n0 = a.ntr[b + i0], n1 = a.ntr[b + i1];
+    const double m0 = io.mtr[b + i0], m1 = io.mtr[b + i1];
+    lF = fma(n0 + n1, fma(g0, m0, g1 * m1), lF);
+    if (TRD) {
       const double dn = n1 - n0;
       if (p.tr_del2)
-        lmh = fma(dn, fma(k20, m0, -(k21 * m1)), lmh);
+        lmh = fma(dn, fma(__ldg(v.kd2_e2 + 2 * e), m0,
+                          -(__ldg(v.kd2_e2 + 2 * e + 1) * m1)), lmh);
       if (p.tr_del4)
-        lmh = fma(dn, fma(q0, w.lL[b + i0], -(q1 * w.lL[b + i1])), lmh);
+        lmh = fma(dn, fma(__ldg(v.ckq_e2 + 2 * e), w.lL[b + i0],
+                          -(__ldg(v.ckq_e2 + 2 * e + 1) * w.lL[b + i1])), lmh);
     }
   }
   const double mh = mean_h(m, a, io.h, e, k);
@@ -707,10 +708,15 @@ void adj_passes(swg_adjoint ad, const AuxView &aux, const AdjIO &io,
     ka_tr2<<<nb(CK), ATPB, 0, st>>>(m, p, aux, v, w, io);
     g_launches += 2;
   }
-  if (m.ne == 8)
-    ka_edge<8><<<nb(EK), ATPB, 0, st>>>(m, p, aux, v, w, io);
+  const bool trd = p.ntracers > 0 && (p.tr_del2 | p.tr_del4);
+  if (m.ne == 8 && !trd)
+    ka_edge<8, false><<<nb(EK), ATPB, 0, st>>>(m, p, aux, v, w, io);
+  else if (m.ne == 8)
+    ka_edge<8, true><<<nb(EK), ATPB, 0, st>>>(m, p, aux, v, w, io);
+  else if (!trd)
+    ka_edge<10, false><<<nb(EK), ATPB, 0, st>>>(m, p, aux, v, w, io);
   else
-    ka_edge<10><<<nb(EK), ATPB, 0, st>>>(m, p, aux, v, w, io);
+    ka_edge<10, true><<<nb(EK), ATPB, 0, st>>>(m, p, aux, v, w, io);
   ++g_launches;
   if (p.do_vn) {
     ka_vertex<<<nb(VK), ATPB, 0, st>>>(m, p, aux, v, w, io);
