@@ -148,6 +148,33 @@ typedef struct swg_params {
 int swg_model_create(swg_mesh mesh, const swg_params *params, swg_model *out);
 int swg_model_destroy(swg_model model);
 
+/* Model variants beside the reference's live model.  Both come from its
+ * un-built hierarchical source (shallow_water_hierarchical.cpp):
+ *   linear:     LinearShallowWaterModel (:676-775), the shallow-water
+ *               equations linearised about a resting layer of thickness h0:
+ *               h_t = -h0 div(vn), vn_t = f0 sum_j w_j vn_j - g grad h.
+ *               Dissipation coefficients are ignored; ntracers must be 0.
+ *   apply_drag: bottom drag -drag_coeff sqrt(ke_c0 + ke_c1) vn / mean_h on
+ *               the lowest level of every edge (the term commented out at
+ *               :479-486).  The reference's live model declares drag_coeff
+ *               (shallow_water_params.hpp:10) but never applies it, which is
+ *               what swg_model_create reproduces; the drag is opt-in. */
+typedef struct swg_model_options {
+  int linear;
+  double h0;
+  int apply_drag;
+} swg_model_options;
+/* swg_model_create with options (NULL = swg_model_create).  Linear models and
+ * models with drag are not differentiated (swg_adjoint_create rejects them);
+ * linear models are not batched. */
+int swg_model_create_ex(swg_mesh mesh, const swg_params *params,
+                        const swg_model_options *opts, swg_model *out);
+/* replaces LinearShallowWaterModel::LinearShallowWaterModel(mesh, params)
+ * (shallow_water_hierarchical.cpp:676-678; h0 = LinearShallowWaterParams::
+ * m_h0) */
+int swg_linear_model_create(swg_mesh mesh, const swg_params *params, double h0,
+                            swg_model *out);
+
 /* replaces the virtual ShallowWaterModel::additional_tendency hook
  * (shallow_water_model.hpp:42-44).  Called on the host after the built-in
  * terms of every tendency evaluation with device pointers and the stream the

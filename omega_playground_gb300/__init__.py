@@ -14,11 +14,13 @@ from .shallow_water import (AddMode, Adjoint, Batch, LSRKStepper,  # noqa: F401
                             ShallowWaterState, TimeStepper,
                             circulation_integral, energy_integral,
                             kernel_launches, mass_integral,
+                            LinearShallowWaterModel, LinearShallowWaterParams,
                             profile_enable, profile_read, sync)
 from ._capi import SwgError, exported_symbols  # noqa: F401
 from . import workloads  # noqa: F401
 
 __all__ = ["AddMode", "Adjoint", "Batch", "checkpoint_cost",
+           "LinearShallowWaterModel", "LinearShallowWaterParams",
            "adjoint_batch_forward", "adjoint_batch_backward", "LSRKStepper", "MPASMesh", "PlanarHexagonalMesh",
            "RK4Stepper", "ShallowWaterModel", "ShallowWaterParams",
            "ShallowWaterState", "TimeStepper", "circulation_integral",

@@ -78,6 +78,11 @@ class Params(C.Structure):
                 ("disable_vn_tendency", C.c_int)]
 
 
+class ModelOptions(C.Structure):
+    _fields_ = [("linear", C.c_int), ("h0", C.c_double),
+                ("apply_drag", C.c_int)]
+
+
 FORCING_FN = C.CFUNCTYPE(None, _vp, _dp, _dp, _dp, _dp, C.c_double, _vp)
 
 # name -> (restype, argtypes)
@@ -98,6 +103,11 @@ _SIGS = {
     "swg_state_copy": (C.c_int, [_vp, _vp, _vp]),
     "swg_state_fill": (C.c_int, [_vp, C.c_double, _vp]),
     "swg_model_create": (C.c_int, [_vp, C.POINTER(Params), C.POINTER(_vp)]),
+    "swg_model_create_ex": (C.c_int, [_vp, C.POINTER(Params),
+                                      C.POINTER(ModelOptions),
+                                      C.POINTER(_vp)]),
+    "swg_linear_model_create": (C.c_int, [_vp, C.POINTER(Params), C.c_double,
+                                          C.POINTER(_vp)]),
     "swg_model_destroy": (C.c_int, [_vp]),
     "swg_model_set_forcing": (C.c_int, [_vp, FORCING_FN, _vp]),
     "swg_compute_tendency": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int,

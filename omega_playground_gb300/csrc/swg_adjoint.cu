@@ -965,6 +965,9 @@ int check_model(swg_model md) {
   if (md->mesh->view.mask)
     return fail(SWG_ERR_ARG, "swg_adjoint: edge_mask other than ones is not "
                              "supported");
+  if (md->view.linear || md->view.drag)
+    return fail(SWG_ERR_ARG, "swg_adjoint: the linear model and the bottom "
+                             "drag are not differentiated");
   if (md->mesh->view.dv4_differs)
     return fail(SWG_ERR_ARG, "swg_adjoint: meshes with dv < dc/4 are not "
                              "supported");

@@ -424,9 +424,29 @@ extern "C" int swg_state_fill(swg_state s, double value, void *stream) {
 
 extern "C" int swg_model_create(swg_mesh mesh, const swg_params *p,
                                 swg_model *out) {
+  return swg_model_create_ex(mesh, p, nullptr, out);
+}
+
+extern "C" int swg_linear_model_create(swg_mesh mesh, const swg_params *p,
+                                       double h0, swg_model *out) {
+  swg_model_options o{};
+  o.linear = 1;
+  o.h0 = h0;
+  return swg_model_create_ex(mesh, p, &o, out);
+}
+
+extern "C" int swg_model_create_ex(swg_mesh mesh, const swg_params *p,
+                                   const swg_model_options *opts,
+                                   swg_model *out) {
   if (!mesh || !p || !out || p->ntracers < 0)
     return fail(SWG_ERR_ARG, "swg_model_create: bad argument");
   *out = nullptr;
+  const swg_model_options o = opts ? *opts : swg_model_options{};
+  if (o.linear && (p->ntracers != 0 || !std::isfinite(o.h0)))
+    return fail(SWG_ERR_ARG, "swg_model_create: the linear model takes no "
+                             "tracers and a finite h0");
+  if (o.apply_drag && !(p->drag_coeff >= 0))
+    return fail(SWG_ERR_ARG, "swg_model_create: drag_coeff must be >= 0");
   swg_model md = new (std::nothrow) swg_model_s();
   if (!md)
     return fail(SWG_ERR_OOM, "swg_model_create: host allocation");
@@ -447,6 +467,14 @@ extern "C" int swg_model_create(swg_mesh mesh, const swg_params *p,
   pv.tr_del4 = p->eddy_diff4 > 0;
   pv.do_h = !p->disable_h_tendency;
   pv.do_vn = !p->disable_vn_tendency;
+  if (o.linear) { // shallow_water_hierarchical.cpp:676-740: no dissipation
+    pv.linear = 1;
+    pv.h0 = o.h0;
+    pv.f4 = 4.0 * p->f0;
+    pv.vel_del2 = pv.vel_del4 = pv.tr_del2 = pv.tr_del4 = 0;
+  }
+  pv.drag = !o.linear && o.apply_drag && p->drag_coeff > 0 && pv.do_vn;
+  pv.drag_coeff = p->drag_coeff;
 
   std::vector<double> f(V, p->f0), c2(E), c4(E), kd2(6 * C), r4(6 * C),
       r4s(C), gidc(E);
@@ -499,7 +527,7 @@ extern "C" int swg_model_create(swg_mesh mesh, const swg_params *p,
       {v4 && mesh->view.dv4_differs, E * K, &a.d2u4},
   };
   for (auto &nd : need)
-    if (nd.on && (rc = dalloc(A, nd.n, nd.p))) {
+    if (!pv.linear && nd.on && (rc = dalloc(A, nd.n, nd.p))) {
       swg_model_destroy(md);
       return rc;
     }

@@ -359,6 +359,9 @@ extern "C" int swg_batch_create(int nmembers, const swg_model *models,
     if (md->forcing)
       return fail(SWG_ERR_ARG, "swg_batch_create: members cannot have an "
                                "additional_tendency hook");
+    if (md->view.linear)
+      return fail(SWG_ERR_ARG, "swg_batch_create: linear models are not "
+                               "batched");
     if (ne && md->mesh->view.ne != ne)
       return fail(SWG_ERR_ARG, "swg_batch_create: members must share the "
                                "edges-on-edge width (8 or 10)");

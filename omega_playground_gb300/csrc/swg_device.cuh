@@ -47,6 +47,11 @@ __device__ __forceinline__ Dual rcp_nr(Dual x) {
   const double r = rcp_nr(x.v);
   return {r, -(r * r) * x.d};
 }
+using ::sqrt;
+__device__ __forceinline__ Dual sqrt(Dual x) {
+  const double s = ::sqrt(x.v);
+  return {s, x.d * (0.5 / s)};
+}
 
 template <class T>
 __device__ __forceinline__ void epilogue(const Epilogue &ep,
@@ -63,6 +68,9 @@ __device__ __forceinline__ void epilogue(const Epilogue &ep,
     f.tend[i] = t;
     f.out[i] = fma(ep.dtb, t, f.out[i]);
   } break;
+  case EPI_LSRK_TEND:
+    f.tend[i] = fma(ep.a, f.tend[i], x);
+    break;
   case EPI_RK4_FIRST: {
     const T s = f.old[i];
     f.acc[i] = fma(ep.dtb, x, s);
@@ -269,6 +277,13 @@ __device__ __forceinline__ void pt_edge_final(const MeshView &m,
   t = fma(-idc, a.ke[size_t(c1) * K + k] - a.ke[size_t(c0) * K + k], t);
   t = fma(-__ldg(p.gidc + e), s.h[size_t(c1) * K + k] - s.h[size_t(c0) * K + k],
           t);
+  if (p.drag && k == K - 1) {
+    // bottom drag -c_d sqrt(ke_0 + ke_1) vn / mean_h on the lowest level
+    // (the term commented out at shallow_water_hierarchical.cpp:479-486)
+    const T hm = 0.5 * (s.h[size_t(c0) * K + k] + s.h[size_t(c1) * K + k]);
+    const T ks = a.ke[size_t(c0) * K + k] + a.ke[size_t(c1) * K + k];
+    t = t + (-p.drag_coeff * sqrt(ks)) * s.vn[i] * rcp_nr(hm);
+  }
   const double mk = m.mask ? m.mask[i] : 1.0;
   if (p.vel_del2)
     t = fma(m.mask ? __ldg(p.c2e + e) * mk : __ldg(p.c2e + e), a.d2u[i], t);
@@ -350,5 +365,42 @@ __device__ __forceinline__ void pt_cell_final(const MeshView &m,
 // Pass domain sizes (threads) of pass `pass` for one instance.
 enum Pass { P_VERTEX = 0, P_CELL1, P_EDGE1, P_AUX2, P_EDGE_FINAL,
             P_CELL_FINAL, NPASS };
+
+// LinearShallowWaterModel (shallow_water_hierarchical.cpp:680-740):
+// vn_t = f sum_j w_j vn_j - g (h_1 - h_0) / dc and h_t = -h0 div(vn), each
+// with its stage update.
+template <int NE, class T>
+__device__ __forceinline__ void pt_lin_edge(const MeshView &m,
+                                            const ModelView &p,
+                                            const StageArgsT<T> &s,
+                                            unsigned i) {
+  const int K = m.nlayers;
+  const int e = int(i / unsigned(K)), k = int(i - unsigned(e) * unsigned(K));
+  T vt = __ldg(m.woe + NE * e) * s.vn[size_t(__ldg(m.eoe + NE * e)) * K + k];
+#pragma unroll
+  for (int j = 1; j < NE; ++j)
+    vt = fma(__ldg(m.woe + NE * e + j),
+             s.vn[size_t(__ldg(m.eoe + NE * e + j)) * K + k], vt);
+  const int c0 = __ldg(m.ce + 2 * e), c1 = __ldg(m.ce + 2 * e + 1);
+  const T t = fma(-__ldg(p.gidc + e),
+                  s.h[size_t(c1) * K + k] - s.h[size_t(c0) * K + k],
+                  p.f4 * vt);
+  epilogue(s.ep, s.fvn, i, t);
+}
+
+template <class T>
+__device__ __forceinline__ void pt_lin_cell(const MeshView &m,
+                                            const ModelView &p,
+                                            const StageArgsT<T> &s,
+                                            unsigned i) {
+  const int K = m.nlayers;
+  const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * unsigned(K));
+  T d = __ldg(m.ccd + 6 * c) * s.vn[size_t(__ldg(m.ec + 6 * c)) * K + k];
+#pragma unroll
+  for (int j = 1; j < MAXE; ++j)
+    d = fma(__ldg(m.ccd + 6 * c + j),
+            s.vn[size_t(__ldg(m.ec + 6 * c + j)) * K + k], d);
+  epilogue(s.ep, s.fh, i, -p.h0 * d);
+}
 
 } // namespace swg

@@ -69,6 +69,10 @@ struct ModelView {
   const double *r4sum;    // [C] sum of r4
   int ntracers;
   int vel_del2, vel_del4, tr_del2, tr_del4, do_h, do_vn;
+  // LinearShallowWaterModel (mean thickness h0; f4 = 4 f0, the Coriolis
+  // factor for the weights/4 table), and the optional bottom drag
+  int linear, drag;
+  double h0, f4, drag_coeff;
 };
 
 // Forward-mode dual number (value, tangent) of the tangent-linear model;
@@ -98,6 +102,7 @@ enum EpiMode {
   EPI_RK4_FIRST = 3, // acc = old + dtb*x; out = old + dta*x
   EPI_RK4_MID = 4,   // acc += dtb*x;      out = old + dta*x
   EPI_RK4_LAST = 5,  // out = acc + dtb*x
+  EPI_LSRK_TEND = 6, // t = a*tend + x; tend = t (state updated afterwards)
 };
 
 template <class T> struct FieldIOT {

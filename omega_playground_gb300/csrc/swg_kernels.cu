@@ -32,6 +32,7 @@
 #include "swg_device.cuh"
 
 #include <algorithm>
+#include <type_traits>
 #include <cstring>
 
 namespace swg {
@@ -92,6 +93,22 @@ __global__ void __launch_bounds__(TPB)
     pt_cell_final<T>(m, p, a, s, i);
 }
 
+template <int NE, class T>
+__global__ void __launch_bounds__(TPB)
+    k_lin_edge(MeshView m, ModelView p, StageArgsT<T> s) {
+  const unsigned i = blockIdx.x * TPB + threadIdx.x;
+  if (i < unsigned(m.nedges) * unsigned(m.nlayers))
+    pt_lin_edge<NE, T>(m, p, s, i);
+}
+
+template <class T>
+__global__ void __launch_bounds__(TPB)
+    k_lin_cell(MeshView m, ModelView p, StageArgsT<T> s) {
+  const unsigned i = blockIdx.x * TPB + threadIdx.x;
+  if (i < unsigned(m.ncells) * unsigned(m.nlayers))
+    pt_lin_cell<T>(m, p, s, i);
+}
+
 // Elementwise helpers for the unfused stepper path (forcing hook set).
 __global__ void k_axpby(double *__restrict__ y, const double *__restrict__ x,
                         const double *__restrict__ z, double alpha,
@@ -132,7 +149,10 @@ __global__ void __launch_bounds__(TPB)
         ke += m.cke[6 * ent + j] * u * u;
       }
       const double hc = h[i];
-      s += m.area_cell_d[ent] * (p.grav * hc * hc / 2 + hc * ke);
+      // the linear model's kinetic energy is weighted by h0
+      // (shallow_water_hierarchical.cpp:743-771)
+      s += m.area_cell_d[ent] *
+           (p.grav * hc * hc / 2 + (p.linear ? p.h0 : hc) * ke);
     } else { // circulation: sum_j dc s vn + f area_triangle
       double cir = 0.0;
       for (int j = 0; j < 3; ++j)
@@ -234,6 +254,8 @@ void launch_aux_t(const MeshView &m, const ModelView &p, const AuxViewT<T> &a,
                   const T *h, const T *vn, const T *tr, cudaStream_t st) {
   const long long K = m.nlayers;
   const long long VK = m.nvertices * K, CK = m.ncells * K, EK = m.nedges * K;
+  if (p.linear) // the linear model has no intermediates
+    return;
   if (p.do_vn) {
     Scope sc("k_vertex", st);
     k_vertex<T><<<nblocks(VK), TPB, 0, st>>>(m, p, a, h, vn);
@@ -261,6 +283,39 @@ void launch_tendency_t(const MeshView &m, const ModelView &p,
                        cudaStream_t st) {
   const long long K = m.nlayers;
   const long long CK = m.ncells * K, EK = m.nedges * K;
+  if (p.linear) {
+    // The linear passes read neighbouring h and vn of the stage input
+    // directly, so an in-place (LSRK) stage first forms the tendency and
+    // then updates the state.
+    StageArgsT<T> ls = s;
+    const bool in_place = s.ep.mode == EPI_LSRK;
+    if (in_place)
+      ls.ep.mode = EPI_LSRK_TEND;
+    if (p.do_vn) {
+      Scope sc("k_lin_edge", st);
+      if (m.ne == 8)
+        k_lin_edge<8, T><<<nblocks(EK), TPB, 0, st>>>(m, p, ls);
+      else
+        k_lin_edge<10, T><<<nblocks(EK), TPB, 0, st>>>(m, p, ls);
+    }
+    if (p.do_h) {
+      Scope sc("k_lin_cell", st);
+      k_lin_cell<T><<<nblocks(CK), TPB, 0, st>>>(m, p, ls);
+    }
+    if constexpr (std::is_same<T, double>::value) {
+      if (in_place && p.do_vn) {
+        Scope sc("k_axpby", st);
+        k_axpby<<<nblocks(EK), TPB, 0, st>>>(s.fvn.out, s.fvn.tend, nullptr,
+                                             s.ep.dtb, 0.0, EK, 1);
+      }
+      if (in_place && p.do_h) {
+        Scope sc("k_axpby", st);
+        k_axpby<<<nblocks(CK), TPB, 0, st>>>(s.fh.out, s.fh.tend, nullptr,
+                                             s.ep.dtb, 0.0, CK, 1);
+      }
+    }
+    return;
+  }
   launch_aux_t<T>(m, p, a, s.h, s.vn, s.tr, st);
   if (p.do_vn) {
     Scope sc("k_edge_final", st);

@@ -11,6 +11,8 @@
 //   TimeStepper, LSRKStepper, RK4Stepper
 //                                      src/time_integration/time_stepper.hpp:8-38
 //   energy/mass/circulation_integral   src/model/shallow_water_diagnostics.hpp:7-12
+//   LinearShallowWaterModel/Params     src/shallow_water_hierarchical.cpp:676-775
+//                                      (never built in the reference)
 //
 // Differences a reference user sees:
 //  - Real1d/Real2d/Real3d are DeviceView (a device pointer plus extents,
@@ -333,14 +335,18 @@ struct ShallowWaterModel {
   MPASMesh *m_mesh;
   swg_model m_handle = nullptr;
 
-  ShallowWaterModel(MPASMesh *mesh, const ShallowWaterParams &params)
+  // `options`: the linear variant or the opt-in bottom drag
+  // (swg_model_options in swgpu.h); the default is the reference's model,
+  // which ignores m_drag_coeff.
+  ShallowWaterModel(MPASMesh *mesh, const ShallowWaterParams &params,
+                    const swg_model_options &options = swg_model_options{})
       : m_params(params), m_mesh(mesh) {
     swg_params p{params.m_f0,         params.m_grav,       params.m_drag_coeff,
                  params.m_visc_del2,  params.m_visc_del4,  params.m_eddy_diff2,
                  params.m_eddy_diff4, params.m_ntracers,
                  params.m_disable_h_tendency ? 1 : 0,
                  params.m_disable_vn_tendency ? 1 : 0};
-    swg_check(swg_model_create(mesh->m_handle, &p, &m_handle));
+    swg_check(swg_model_create_ex(mesh->m_handle, &p, &options, &m_handle));
     // The hook stays registered until the base no-op runs once; then the
     // steppers switch to the fused kernels (models that override
     // additional_tendency keep the unfused, hooked sequence).
@@ -388,6 +394,20 @@ private:
     if (self->m_default_hook)
       swg_model_set_forcing(self->m_handle, nullptr, nullptr);
   }
+};
+
+// LinearShallowWaterModel and its parameters
+// (shallow_water_hierarchical.cpp:676-775): h_t = -h0 div(vn),
+// vn_t = f0 sum_j w_j vn_j - g grad h; no tracers, no dissipation.
+struct LinearShallowWaterParams : ShallowWaterParams {
+  Real m_h0 = 1000;
+};
+
+struct LinearShallowWaterModel : ShallowWaterModel {
+  LinearShallowWaterModel(MPASMesh *mesh, const LinearShallowWaterParams &params)
+      : ShallowWaterModel(mesh, params, swg_model_options{1, params.m_h0, 0}),
+        m_h0(params.m_h0) {}
+  Real m_h0;
 };
 
 // --------------------------------------------------------------- steppers --

@@ -250,13 +250,24 @@ class ShallowWaterState:
 
 class ShallowWaterModel:
     """shallow_water_model.hpp:14-51.  Override ``additional_tendency`` to
-    add forcing (it receives device pointers and the CUDA stream)."""
+    add forcing (it receives device pointers and the CUDA stream).
 
-    def __init__(self, mesh: MPASMesh, params: ShallowWaterParams):
+    ``apply_drag`` turns on the bottom drag with ``params.m_drag_coeff``
+    (the term commented out at shallow_water_hierarchical.cpp:479-486); the
+    reference's live model ignores the coefficient, and so does this one by
+    default."""
+
+    _linear_h0 = None
+
+    def __init__(self, mesh: MPASMesh, params: ShallowWaterParams,
+                 apply_drag: bool = False):
         self.m_mesh, self.m_params = mesh, params
         p = params._c()
+        o = _capi.ModelOptions(int(self._linear_h0 is not None),
+                               float(self._linear_h0 or 0.0), int(apply_drag))
         h = C.c_void_p()
-        check(lib().swg_model_create(mesh.handle, C.byref(p), C.byref(h)))
+        check(lib().swg_model_create_ex(mesh.handle, C.byref(p), C.byref(o),
+                                        C.byref(h)))
         self._h = h
         self._cb = None
         if type(self).additional_tendency is not \
@@ -314,6 +325,24 @@ def _cudart():
         _cudart_lib.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t,
                                            C.c_int]
     return _cudart_lib
+
+
+@dataclasses.dataclass
+class LinearShallowWaterParams(ShallowWaterParams):
+    """ShallowWaterParams plus the resting thickness m_h0 of the linear
+    model (shallow_water_hierarchical.cpp:676-678)."""
+    m_h0: float = 1000.0
+
+
+class LinearShallowWaterModel(ShallowWaterModel):
+    """LinearShallowWaterModel (shallow_water_hierarchical.cpp:676-775):
+    h_t = -h0 div(vn), vn_t = f0 sum_j w_j vn_j - g grad h; no tracers, no
+    dissipation.  Same state, steppers and diagnostics as the nonlinear
+    model; its energy integral weights the kinetic energy by h0."""
+
+    def __init__(self, mesh: MPASMesh, params: LinearShallowWaterParams):
+        self._linear_h0 = float(params.m_h0)
+        super().__init__(mesh, params)
 
 
 class TimeStepper:

@@ -89,6 +89,9 @@ def lib():
                                           C.c_double, C.c_int]
         L.or_model_create.argtypes = [C.POINTER(_Mesh), C.POINTER(_Params)]
         L.or_model_create.restype = C.c_void_p
+        L.or_model_create_ex.argtypes = [C.POINTER(_Mesh), C.POINTER(_Params),
+                                         C.c_int, C.c_double, C.c_int]
+        L.or_model_create_ex.restype = C.c_void_p
         L.or_model_destroy.argtypes = [C.c_void_p]
         L.or_model_aux.argtypes = [C.c_void_p, C.c_char_p,
                                    C.POINTER(C.c_size_t)]
@@ -168,13 +171,18 @@ class OracleModel:
 
     def __init__(self, mesh: OracleMesh, *, f0=0.0, grav=9.81, visc_del2=0.0,
                  visc_del4=0.0, eddy_diff2=0.0, eddy_diff4=0.0, ntracers=0,
-                 disable_h_tendency=False, disable_vn_tendency=False):
+                 disable_h_tendency=False, disable_vn_tendency=False,
+                 drag_coeff=0.0, apply_drag=False, linear_h0=None):
+        """linear_h0: the linear model with that resting thickness;
+        apply_drag: the opt-in bottom drag with drag_coeff."""
         self.mesh = mesh
         self.ntracers = ntracers
-        self._p = _Params(f0, grav, 0.0, visc_del2, visc_del4, eddy_diff2,
-                          eddy_diff4, ntracers, int(disable_h_tendency),
-                          int(disable_vn_tendency))
-        self._h = lib().or_model_create(C.byref(mesh._s), C.byref(self._p))
+        self._p = _Params(f0, grav, drag_coeff, visc_del2, visc_del4,
+                          eddy_diff2, eddy_diff4, ntracers,
+                          int(disable_h_tendency), int(disable_vn_tendency))
+        self._h = lib().or_model_create_ex(
+            C.byref(mesh._s), C.byref(self._p), int(linear_h0 is not None),
+            float(linear_h0 or 0.0), int(apply_drag))
 
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:

@@ -239,6 +239,10 @@ struct or_model {
   or_mesh m;
   or_params p;
   int en_vel_diff, en_vel_hyperdiff, en_tr_diff, en_tr_hyperdiff;
+  /* variants from shallow_water_hierarchical.cpp: LinearShallowWaterModel
+   * (h0) and the bottom drag that its nonlinear model leaves commented out */
+  int linear, apply_drag;
+  double h0;
   double *f_vertex;
   /* auxiliary state (shallow_water_auxstate.hpp:9-21) */
   double *rvort_vertex, *norm_rvort_vertex, *norm_pvort_vertex;
@@ -255,9 +259,17 @@ struct or_model {
 static double *zalloc(size_t n) { return (double *)calloc(n ? n : 1, 8); }
 
 or_model *or_model_create(const or_mesh *m, const or_params *p) {
+  return or_model_create_ex(m, p, 0, 0.0, 0);
+}
+
+or_model *or_model_create_ex(const or_mesh *m, const or_params *p, int linear,
+                             double h0, int apply_drag) {
   or_model *md = (or_model *)calloc(1, sizeof(or_model));
   md->m = *m;
   md->p = *p;
+  md->linear = linear;
+  md->h0 = h0;
+  md->apply_drag = apply_drag && !linear;
   /* shallow_water_model.cpp:17-35 */
   md->en_vel_diff = p->visc_del2 > 0;
   md->en_vel_hyperdiff = p->visc_del4 > 0;
@@ -526,6 +538,16 @@ static void vn_tendency(or_model *md, double *vn_tend, const double *h,
       /* SSHGradOnEdge (ssh_grad_edge.hpp:281-294) */
       vn_tend[i] -= p->grav *
                     (h[(size_t)c1 * K + k] - h[(size_t)c0 * K + k]) * inv_dc;
+      /* bottom drag, opt-in: the term commented out at
+       * shallow_water_hierarchical.cpp:479-486 with h_drag_edge = h_mean
+       * (:258-276) on the lowest level (max_level_edge_top = nlayers) */
+      if (md->apply_drag && p->drag_coeff > 0 && k == K - 1) {
+        const double inv_h_drag_edge = 1. / md->mean_h_edge[i];
+        vn_tend[i] += -p->drag_coeff *
+                      sqrt(md->ke_cell[(size_t)c0 * K + k] +
+                           md->ke_cell[(size_t)c1 * K + k]) *
+                      vn[i] * inv_h_drag_edge;
+      }
       /* VelocityDiffusionOnEdge (vel_diff_edge.hpp:61-86) */
       if (md->en_vel_diff) {
         const double del2u =
@@ -650,10 +672,58 @@ static void tr_tendency(or_model *md, double *tr_tend, const double *vn,
     }
 }
 
+/* LinearShallowWaterModel::compute_h_tendency / compute_vn_tendency
+ * (shallow_water_hierarchical.cpp:680-740); f_edge = f0 (:15) */
+static void linear_tendency(or_model *md, double *h_tend, double *vn_tend,
+                            const double *h, const double *vn, int add_mode) {
+  const or_mesh *m = &md->m;
+  const int K = m->nlayers;
+  if (!md->p.disable_h_tendency) {
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < m->ncells; ++c)
+      for (int k = 0; k < K; ++k) {
+        double accum = -0.0;
+        for (int j = 0; j < m->nedges_on_cell[c]; ++j) {
+          const int je = m->edges_on_cell[6 * c + j];
+          accum += m->dv_edge[je] * m->edge_sign_on_cell[6 * c + j] *
+                   vn[(size_t)je * K + k];
+        }
+        const double x = -md->h0 * accum / m->area_cell[c];
+        if (add_mode == 1)
+          h_tend[(size_t)c * K + k] += x;
+        else
+          h_tend[(size_t)c * K + k] = x;
+      }
+  }
+  if (!md->p.disable_vn_tendency) {
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < m->nedges; ++e)
+      for (int k = 0; k < K; ++k) {
+        double vt = -0.0;
+        for (int j = 0; j < m->nedges_on_edge[e]; ++j) {
+          const int je = m->edges_on_edge[12 * e + j];
+          vt += m->weights_on_edge[12 * e + j] * vn[(size_t)je * K + k];
+        }
+        const int c0 = m->cells_on_edge[2 * e], c1 = m->cells_on_edge[2 * e + 1];
+        const double grad_h =
+            (h[(size_t)c1 * K + k] - h[(size_t)c0 * K + k]) / m->dc_edge[e];
+        const double x = md->p.f0 * vt - md->p.grav * grad_h;
+        if (add_mode == 1)
+          vn_tend[(size_t)e * K + k] += x;
+        else
+          vn_tend[(size_t)e * K + k] = x;
+      }
+  }
+}
+
 void or_compute_tendency(or_model *md, double *h_tend, double *vn_tend,
                          double *tr_tend, const double *h, const double *vn,
                          const double *tr, double t, int add_mode) {
   (void)t; /* only the additional_tendency hook (not modelled) reads t */
+  if (md->linear) {
+    linear_tendency(md, h_tend, vn_tend, h, vn, add_mode);
+    return;
+  }
   aux_compute(md, h, vn, tr);
   if (!md->p.disable_h_tendency)
     h_tendency(md, h_tend, vn, add_mode);
@@ -796,7 +866,10 @@ double or_energy_integral(or_model *md, const double *h, const double *vn) {
       }
       KE /= m->area_cell[c];
       const double hc = h[(size_t)c * K + k];
-      total += m->area_cell[c] * (md->p.grav * hc * hc / 2 + hc * KE);
+      /* the linear model weights KE by h0
+       * (shallow_water_hierarchical.cpp:743-771) */
+      total += m->area_cell[c] *
+               (md->p.grav * hc * hc / 2 + (md->linear ? md->h0 : hc) * KE);
     }
   return total;
 }

@@ -67,6 +67,12 @@ void or_planar_hex_sizes(int nx, int ny, int *ncells, int *nedges,
 void or_planar_hex_build(or_mesh *m, int nx, int ny, double dc, int nlayers);
 
 or_model *or_model_create(const or_mesh *m, const or_params *p);
+/* linear != 0: LinearShallowWaterModel with resting thickness h0
+ * (shallow_water_hierarchical.cpp:676-775; no tracers, no dissipation).
+ * apply_drag != 0: the nonlinear model plus the bottom drag that
+ * shallow_water_hierarchical.cpp:479-486 leaves commented out. */
+or_model *or_model_create_ex(const or_mesh *m, const or_params *p, int linear,
+                             double h0, int apply_drag);
 void or_model_destroy(or_model *md);
 /* Pointer to a named auxiliary array of the model (NULL if unknown); *n gets
  * its element count.  Names follow the reference's member names. */
