@@ -470,6 +470,11 @@ struct swg_adjoint_s {
   double t0 = 0, dt = 0;
   long long plain_steps = 0, taped_steps = 0;
   int state = 0; // 0 idle, 1 forward done (first step taped)
+  // backward sweep: restores, stores and plain advances run on `adv`,
+  // concurrently with the caller's stream, which tapes and reverses each
+  // step; `ready` = x_i is in cur, `freed` = cur was copied to the tape
+  cudaStream_t adv = nullptr;
+  cudaEvent_t go = nullptr, ready = nullptr, freed = nullptr;
 };
 
 namespace {
@@ -699,25 +704,45 @@ void adj_passes(swg_adjoint ad, const AuxView &aux, const AdjIO &io,
                   VK = m.nvertices * K;
   const AdjView &v = ad->av;
   const AdjWork &w = ad->aw;
-  if (p.do_vn) {
-    ka_vel<<<nb(VK + CK + EK), ATPB, 0, st>>>(m, p, aux, v, w, io);
-    ++g_launches;
-  }
-  if (p.ntracers > 0) {
-    ka_tr1<<<nb(CK), ATPB, 0, st>>>(m, p, aux, v, w, io);
-    ka_tr2<<<nb(CK), ATPB, 0, st>>>(m, p, aux, v, w, io);
-    g_launches += 2;
-  }
+  const Fork *fk = &md->fork;
   const bool trd = p.ntracers > 0 && (p.tr_del2 | p.tr_del4);
-  if (m.ne == 8 && !trd)
-    ka_edge<8, false><<<nb(EK), ATPB, 0, st>>>(m, p, aux, v, w, io);
-  else if (m.ne == 8)
-    ka_edge<8, true><<<nb(EK), ATPB, 0, st>>>(m, p, aux, v, w, io);
-  else if (!trd)
-    ka_edge<10, false><<<nb(EK), ATPB, 0, st>>>(m, p, aux, v, w, io);
-  else
-    ka_edge<10, true><<<nb(EK), ATPB, 0, st>>>(m, p, aux, v, w, io);
-  ++g_launches;
+  auto vel = [&](cudaStream_t q) {
+    ka_vel<<<nb(VK + CK + EK), ATPB, 0, q>>>(m, p, aux, v, w, io);
+    ++g_launches;
+  };
+  auto tr1 = [&](cudaStream_t q) {
+    ka_tr1<<<nb(CK), ATPB, 0, q>>>(m, p, aux, v, w, io);
+    ++g_launches;
+  };
+  auto tr2 = [&](cudaStream_t q) {
+    ka_tr2<<<nb(CK), ATPB, 0, q>>>(m, p, aux, v, w, io);
+    ++g_launches;
+  };
+  auto edge = [&](cudaStream_t q) {
+    if (m.ne == 8 && !trd)
+      ka_edge<8, false><<<nb(EK), ATPB, 0, q>>>(m, p, aux, v, w, io);
+    else if (m.ne == 8)
+      ka_edge<8, true><<<nb(EK), ATPB, 0, q>>>(m, p, aux, v, w, io);
+    else if (!trd)
+      ka_edge<10, false><<<nb(EK), ATPB, 0, q>>>(m, p, aux, v, w, io);
+    else
+      ka_edge<10, true><<<nb(EK), ATPB, 0, q>>>(m, p, aux, v, w, io);
+    ++g_launches;
+  };
+  // ka_vel and ka_tr1 are independent, and so are ka_edge and ka_tr2 (the
+  // tracer pass writes only the tracer adjoint and the h part of tr / h)
+  if (p.do_vn && p.ntracers > 0) {
+    fork_join(fk, st, vel, tr1);
+    fork_join(fk, st, edge, tr2);
+  } else {
+    if (p.do_vn)
+      vel(st);
+    if (p.ntracers > 0) {
+      tr1(st);
+      tr2(st);
+    }
+    edge(st);
+  }
   if (p.do_vn) {
     ka_vertex<<<nb(VK), ATPB, 0, st>>>(m, p, aux, v, w, io);
     ++g_launches;
@@ -731,7 +756,7 @@ void adj_tendency(swg_adjoint ad, const double *h, const double *vn,
                   const double *tr, swg_state mu, swg_state out,
                   cudaStream_t st) {
   swg_model md = ad->model;
-  launch_aux(md->mesh->view, md->view, md->aux, h, vn, tr, st);
+  launch_aux(md->mesh->view, md->view, md->aux, h, vn, tr, st, &md->fork);
   AdjIO io{};
   io.h = h;
   io.vn = vn;
@@ -760,14 +785,13 @@ void stage_ptrs(swg_adjoint ad, int s, const double **h, const double **vn,
   *tr = ad->X[s]->tr;
 }
 
-// Taped RK4 step from `cur`: X0 = cur, X1..X3 the stage inputs, and (when
-// `out` is given) the step's result.
+// Taped RK4 step from X0 (the caller copies the step's start state there):
+// X1..X3 the stage inputs, and (when `out` is given) the step's result.
 int tape_step(swg_adjoint ad, double dt, swg_state out, cudaStream_t st) {
   swg_model md = ad->model;
   const ModelView &pv = md->view;
   static const double rka[3] = {1. / 2, 1. / 2, 1};
   static const double rkb[4] = {1. / 6, 1. / 3, 1. / 3, 1. / 6};
-  TRY(swg_state_copy(ad->X[0], ad->cur, st));
   swg_state S = ad->X[0];
   const int last = out ? 3 : 2;
   for (int s = 0; s <= last; ++s) {
@@ -783,12 +807,12 @@ int tape_step(swg_adjoint ad, double dt, swg_state out, cudaStream_t st) {
     a.ftr = {nullptr, S->tr, ad->acc->tr, o->tr};
     const int mode = s == 0 ? EPI_RK4_FIRST : (s < 3 ? EPI_RK4_MID : EPI_RK4_LAST);
     a.ep = {mode, 0.0, dt * rkb[s], s < 3 ? dt * rka[s] : 0.0};
-    launch_tendency(md->mesh->view, pv, ad->taux[s], a, st);
+    launch_tendency(md->mesh->view, pv, ad->taux[s], a, st, &md->fork);
   }
   if (!out) { // intermediates of the last stage input
     const double *h, *vn, *tr;
     stage_ptrs(ad, 3, &h, &vn, &tr);
-    launch_aux(md->mesh->view, pv, ad->taux[3], h, vn, tr, st);
+    launch_aux(md->mesh->view, pv, ad->taux[3], h, vn, tr, st, &md->fork);
   }
   ++ad->taped_steps;
   cudaError_t err = cudaGetLastError();
@@ -897,19 +921,31 @@ struct Planner {
   }
 };
 
-int run_action(swg_adjoint ad, const AdjAction &a, cudaStream_t st) {
+// One schedule action on stream st.  With `two` (backward sweep) the
+// restores, stores and advances go to ad->adv instead, and a tape+adjoint
+// action hands x_i over from it through the ready / freed events.
+int run_action(swg_adjoint ad, const AdjAction &a, cudaStream_t st, bool two) {
+  cudaStream_t q = two ? ad->adv : st;
   switch (a.type) {
   case 0:
     ad->plain_steps += a.b;
     return swg_step(ad->stepper, ad->cur, ad->t0 + a.a * ad->dt, ad->dt, a.b,
-                    1, st);
+                    1, q);
   case 1:
-    return swg_state_copy(ad->snaps[a.a], ad->cur, st);
+    return swg_state_copy(ad->snaps[a.a], ad->cur, q);
   case 2:
-    return swg_state_copy(ad->cur, ad->snaps[a.a], st);
+    return swg_state_copy(ad->cur, ad->snaps[a.a], q);
   default:
     break;
   }
+  cudaError_t e = cudaSuccess;
+  if (two && ((e = cudaEventRecord(ad->ready, ad->adv)) != cudaSuccess ||
+              (e = cudaStreamWaitEvent(st, ad->ready, 0)) != cudaSuccess))
+    return cuda_fail(e, "swg_adjoint: stream handshake");
+  TRY(swg_state_copy(ad->X[0], ad->cur, st));
+  if (two && ((e = cudaEventRecord(ad->freed, st)) != cudaSuccess ||
+              (e = cudaStreamWaitEvent(ad->adv, ad->freed, 0)) != cudaSuccess))
+    return cuda_fail(e, "swg_adjoint: stream handshake");
   // tape + adjoint of one step: the same launches every time (no forcing),
   // replayed from a CUDA graph captured on first use
   if (!ad->tape_graph || ad->tape_graph_dt != ad->dt) {
@@ -1019,6 +1055,14 @@ extern "C" int swg_adjoint_create(swg_model md, int nsnapshots,
   }
   if (rc == SWG_OK)
     rc = swg_stepper_create(md, SWG_STEPPER_RK4, 4, &ad->stepper);
+  if (rc == SWG_OK) {
+    cudaError_t e = cudaStreamCreateWithFlags(&ad->adv, cudaStreamNonBlocking);
+    for (cudaEvent_t *ev : {&ad->go, &ad->ready, &ad->freed})
+      if (e == cudaSuccess)
+        e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    if (e != cudaSuccess)
+      rc = cuda_fail(e, "swg_adjoint_create: advance stream");
+  }
   const size_t n = words(md);
   if (rc == SWG_OK && ((rc = alloc_aux_like(ad, ad->daux)) ||
                        (rc = alloc_tape(ad, 0)) || (rc = alloc_tape(ad, 1)) ||
@@ -1041,6 +1085,11 @@ extern "C" int swg_adjoint_destroy(swg_adjoint ad) {
   swg_stepper_destroy(ad->stepper);
   if (ad->tape_graph)
     cudaGraphExecDestroy(ad->tape_graph);
+  for (cudaEvent_t e : {ad->go, ad->ready, ad->freed})
+    if (e)
+      cudaEventDestroy(e);
+  if (ad->adv)
+    cudaStreamDestroy(ad->adv);
   swg_state st[] = {ad->cur, ad->next, ad->X[0], ad->X[1], ad->X[2], ad->X[3],
                     ad->acc, ad->lam, ad->lacc, ad->mu, ad->mu2, ad->lX};
   for (auto s : st)
@@ -1164,10 +1213,11 @@ int fwd_next(swg_adjoint ad, swg_state final_out, cudaStream_t st, bool *done) {
   if (a.type != 3) {
     ++ad->pos;
     *done = false;
-    return run_action(ad, a, st);
+    return run_action(ad, a, st, false);
   }
   if (a.a != ad->nsteps - 1)
     return fail(SWG_ERR_STATE, "swg_adj_forward: unexpected schedule");
+  TRY(swg_state_copy(ad->X[0], ad->cur, st));
   TRY(tape_step(ad, ad->dt, ad->next, st));
   TRY(swg_state_copy(final_out, ad->next, st));
   ad->state = 1;
@@ -1176,6 +1226,12 @@ int fwd_next(swg_adjoint ad, swg_state final_out, cudaStream_t st, bool *done) {
 }
 
 int bwd_begin(swg_adjoint ad, swg_state lambda, cudaStream_t st) {
+  // the advance stream starts after everything already queued on st
+  cudaError_t e = cudaEventRecord(ad->go, st);
+  if (e == cudaSuccess)
+    e = cudaStreamWaitEvent(ad->adv, ad->go, 0);
+  if (e != cudaSuccess)
+    return cuda_fail(e, "swg_adj_backward: stream handshake");
   TRY(swg_state_copy(ad->lam, lambda, st));
   if (ad->aw.gc2e) {
     cudaError_t err = cudaMemsetAsync(
@@ -1192,8 +1248,13 @@ int bwd_begin(swg_adjoint ad, swg_state lambda, cudaStream_t st) {
 int bwd_next(swg_adjoint ad, swg_state lambda, cudaStream_t st, bool *done) {
   if (ad->pos < ad->actions.size()) {
     *done = false;
-    return run_action(ad, ad->actions[ad->pos++], st);
+    return run_action(ad, ad->actions[ad->pos++], st, true);
   }
+  cudaError_t e = cudaEventRecord(ad->ready, ad->adv);
+  if (e == cudaSuccess)
+    e = cudaStreamWaitEvent(st, ad->ready, 0);
+  if (e != cudaSuccess)
+    return cuda_fail(e, "swg_adj_backward: stream handshake");
   TRY(swg_state_copy(lambda, ad->lam, st));
   ad->state = 0;
   *done = true;

@@ -533,7 +533,7 @@ extern "C" int swg_model_create_ex(swg_mesh mesh, const swg_params *p,
     }
   if (!a.d2u4)
     a.d2u4 = a.d2u;
-  if ((rc = dalloc(A, 1024, &md->partials))) {
+  if ((rc = dalloc(A, 1024, &md->partials)) || (rc = fork_create(md->fork))) {
     swg_model_destroy(md);
     return rc;
   }
@@ -544,6 +544,7 @@ extern "C" int swg_model_create_ex(swg_mesh mesh, const swg_params *p,
 extern "C" int swg_model_destroy(swg_model md) {
   if (!md)
     return SWG_OK;
+  fork_destroy(md->fork);
   free_all(md->allocs);
   delete md;
   return SWG_OK;
@@ -618,7 +619,7 @@ StageArgs tendency_args(swg_state tend, swg_state state, int mode) {
 int run_tendency(swg_model md, const StageArgs &s, swg_state tend_for_hook,
                  const double *h, const double *vn, double t,
                  cudaStream_t st) {
-  launch_tendency(md->mesh->view, md->view, md->aux, s, st);
+  launch_tendency(md->mesh->view, md->view, md->aux, s, st, &md->fork);
   TRY(check_launch("tendency kernels"));
   if (md->forcing && tend_for_hook) {
     md->forcing(md->forcing_user, tend_for_hook->h, tend_for_hook->vn, h, vn,
@@ -734,7 +735,7 @@ int fused_step(swg_stepper sp, swg_state S, double dt, cudaStream_t st) {
       a.fvn = {sp->tend->vn, nullptr, nullptr, S->vn};
       a.ftr = {sp->tend->tr, nullptr, nullptr, S->tr};
       a.ep = {EPI_LSRK, sp->rka[stage], dt * sp->rkb[stage], 0.0};
-      launch_tendency(md->mesh->view, pv, md->aux, a, st);
+      launch_tendency(md->mesh->view, pv, md->aux, a, st, &md->fork);
     }
     return check_launch("LSRK step");
   }
@@ -755,7 +756,7 @@ int fused_step(swg_stepper sp, swg_state S, double dt, cudaStream_t st) {
         stage == 0 ? EPI_RK4_FIRST : (stage < 3 ? EPI_RK4_MID : EPI_RK4_LAST);
     a.ep = {mode, 0.0, dt * sp->rkb[stage],
             stage < 3 ? dt * sp->rka[stage] : 0.0};
-    launch_tendency(md->mesh->view, pv, md->aux, a, st);
+    launch_tendency(md->mesh->view, pv, md->aux, a, st, &md->fork);
     in = outp;
   }
   return check_launch("RK4 step");

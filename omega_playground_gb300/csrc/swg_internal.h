@@ -125,8 +125,36 @@ template <class T> struct StageArgsT {
 };
 using StageArgs = StageArgsT<double>;
 
+// A second stream and two events owned by a model: independent passes of
+// one evaluation run as a fork/join pair on it (inside captured graphs they
+// become parallel branches), so that one pass fills the other's last wave.
+struct Fork {
+  cudaStream_t side = nullptr;
+  cudaEvent_t go = nullptr, done = nullptr;
+};
+int fork_create(Fork &f);
+void fork_destroy(Fork &f);
+// runs main_fn on st and side_fn on the fork's stream concurrently (in that
+// order on st when fk is null)
+template <class A, class B>
+void fork_join(const Fork *fk, cudaStream_t st, A main_fn, B side_fn) {
+  if (!fk || !fk->side) {
+    main_fn(st);
+    side_fn(st);
+    return;
+  }
+  cudaEventRecord(fk->go, st);
+  cudaStreamWaitEvent(fk->side, fk->go, 0);
+  side_fn(fk->side);
+  cudaEventRecord(fk->done, fk->side);
+  main_fn(st);
+  cudaStreamWaitEvent(st, fk->done, 0);
+}
+
+// fk (optional): run the independent passes concurrently
 void launch_tendency(const MeshView &m, const ModelView &p, const AuxView &a,
-                     const StageArgs &s, cudaStream_t st);
+                     const StageArgs &s, cudaStream_t st,
+                     const Fork *fk = nullptr);
 // the same six passes on dual numbers (tangent-linear model)
 void launch_tendency_dual(const MeshView &m, const ModelView &p,
                           const AuxViewT<Dual> &a, const StageArgsT<Dual> &s,
@@ -134,7 +162,7 @@ void launch_tendency_dual(const MeshView &m, const ModelView &p,
 // only the four auxiliary passes (intermediates of the state h, vn, tr)
 void launch_aux(const MeshView &m, const ModelView &p, const AuxView &a,
                 const double *h, const double *vn, const double *tr,
-                cudaStream_t st);
+                cudaStream_t st, const Fork *fk = nullptr);
 void launch_axpby(double *y, const double *x, const double *z, double alpha,
                   double beta, long long n, int kind, cudaStream_t st);
 // opt-in per-kernel CUDA-event timing (swg_profile_enable)
@@ -178,6 +206,7 @@ struct swg_model_s {
   double *partials; // diagnostic partial sums
   swg_forcing_fn forcing;
   void *forcing_user;
+  swg::Fork fork;
 };
 
 struct swg_stepper_s {

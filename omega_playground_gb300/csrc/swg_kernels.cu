@@ -251,19 +251,29 @@ namespace {
 
 template <class T>
 void launch_aux_t(const MeshView &m, const ModelView &p, const AuxViewT<T> &a,
-                  const T *h, const T *vn, const T *tr, cudaStream_t st) {
+                  const T *h, const T *vn, const T *tr, cudaStream_t st,
+                  const Fork *fk) {
   const long long K = m.nlayers;
   const long long VK = m.nvertices * K, CK = m.ncells * K, EK = m.nedges * K;
   if (p.linear) // the linear model has no intermediates
     return;
-  if (p.do_vn) {
-    Scope sc("k_vertex", st);
-    k_vertex<T><<<nblocks(VK), TPB, 0, st>>>(m, p, a, h, vn);
-  }
-  if ((p.do_vn && (p.vel_del2 || p.vel_del4)) || p.ntracers > 0) {
-    Scope sc("k_cell1", st);
-    k_cell1<T><<<nblocks(CK), TPB, 0, st>>>(m, p, a, h, vn, tr);
-  }
+  // vertex and cell passes read only the state: independent
+  const bool vert = p.do_vn;
+  const bool cell1 = (p.do_vn && (p.vel_del2 || p.vel_del4)) || p.ntracers > 0;
+  auto run_vertex = [&](cudaStream_t s) {
+    Scope sc("k_vertex", s);
+    k_vertex<T><<<nblocks(VK), TPB, 0, s>>>(m, p, a, h, vn);
+  };
+  auto run_cell1 = [&](cudaStream_t s) {
+    Scope sc("k_cell1", s);
+    k_cell1<T><<<nblocks(CK), TPB, 0, s>>>(m, p, a, h, vn, tr);
+  };
+  if (vert && cell1)
+    fork_join(fk, st, run_vertex, run_cell1);
+  else if (vert)
+    run_vertex(st);
+  else if (cell1)
+    run_cell1(st);
   if (p.do_vn || p.do_h || p.ntracers > 0) {
     Scope sc("k_edge1", st);
     k_edge1<T><<<nblocks(EK), TPB, 0, st>>>(m, p, a, h, vn);
@@ -280,7 +290,7 @@ void launch_aux_t(const MeshView &m, const ModelView &p, const AuxViewT<T> &a,
 template <class T>
 void launch_tendency_t(const MeshView &m, const ModelView &p,
                        const AuxViewT<T> &a, const StageArgsT<T> &s,
-                       cudaStream_t st) {
+                       cudaStream_t st, const Fork *fk) {
   const long long K = m.nlayers;
   const long long CK = m.ncells * K, EK = m.nedges * K;
   if (p.linear) {
@@ -316,37 +326,70 @@ void launch_tendency_t(const MeshView &m, const ModelView &p,
     }
     return;
   }
-  launch_aux_t<T>(m, p, a, s.h, s.vn, s.tr, st);
-  if (p.do_vn) {
-    Scope sc("k_edge_final", st);
+  launch_aux_t<T>(m, p, a, s.h, s.vn, s.tr, st, fk);
+  const bool edge = p.do_vn, cell = p.do_h || p.ntracers > 0;
+  auto run_edge = [&](cudaStream_t q) {
+    Scope sc("k_edge_final", q);
     if (m.ne == 8)
-      k_edge_final<8, T><<<nblocks(EK), TPB, 0, st>>>(m, p, a, s);
+      k_edge_final<8, T><<<nblocks(EK), TPB, 0, q>>>(m, p, a, s);
     else
-      k_edge_final<10, T><<<nblocks(EK), TPB, 0, st>>>(m, p, a, s);
-  }
-  if (p.do_h || p.ntracers > 0) {
-    Scope sc("k_cell_final", st);
-    k_cell_final<T><<<nblocks(CK), TPB, 0, st>>>(m, p, a, s);
-  }
+      k_edge_final<10, T><<<nblocks(EK), TPB, 0, q>>>(m, p, a, s);
+  };
+  auto run_cell = [&](cudaStream_t q) {
+    Scope sc("k_cell_final", q);
+    k_cell_final<T><<<nblocks(CK), TPB, 0, q>>>(m, p, a, s);
+  };
+  // The final passes are independent unless the stage updates the state in
+  // place (LSRK): there the edge pass reads h, which the cell pass rewrites,
+  // so the edge pass goes first.
+  if (edge && cell)
+    fork_join(s.ep.mode == EPI_LSRK ? nullptr : fk, st, run_edge, run_cell);
+  else if (edge)
+    run_edge(st);
+  else if (cell)
+    run_cell(st);
 }
 
 } // namespace
 
 void launch_tendency(const MeshView &m, const ModelView &p, const AuxView &a,
-                     const StageArgs &s, cudaStream_t st) {
-  launch_tendency_t<double>(m, p, a, s, st);
+                     const StageArgs &s, cudaStream_t st, const Fork *fk) {
+  launch_tendency_t<double>(m, p, a, s, st, fk);
 }
 
 void launch_tendency_dual(const MeshView &m, const ModelView &p,
                           const AuxViewT<Dual> &a, const StageArgsT<Dual> &s,
                           cudaStream_t st) {
-  launch_tendency_t<Dual>(m, p, a, s, st);
+  launch_tendency_t<Dual>(m, p, a, s, st, nullptr);
 }
 
 void launch_aux(const MeshView &m, const ModelView &p, const AuxView &a,
                 const double *h, const double *vn, const double *tr,
-                cudaStream_t st) {
-  launch_aux_t<double>(m, p, a, h, vn, tr, st);
+                cudaStream_t st, const Fork *fk) {
+  launch_aux_t<double>(m, p, a, h, vn, tr, st, fk);
+}
+
+int fork_create(Fork &f) {
+  cudaError_t err = cudaStreamCreateWithFlags(&f.side, cudaStreamNonBlocking);
+  if (err == cudaSuccess)
+    err = cudaEventCreateWithFlags(&f.go, cudaEventDisableTiming);
+  if (err == cudaSuccess)
+    err = cudaEventCreateWithFlags(&f.done, cudaEventDisableTiming);
+  if (err != cudaSuccess) {
+    fork_destroy(f);
+    return cuda_fail(err, "fork stream");
+  }
+  return SWG_OK;
+}
+
+void fork_destroy(Fork &f) {
+  if (f.go)
+    cudaEventDestroy(f.go);
+  if (f.done)
+    cudaEventDestroy(f.done);
+  if (f.side)
+    cudaStreamDestroy(f.side);
+  f = Fork{};
 }
 
 void launch_axpby(double *y, const double *x, const double *z, double alpha,
