@@ -287,6 +287,9 @@ int swg_adj_tendency(swg_adjoint adj, swg_state x, swg_state mu,
                      swg_state lambda_out, void *stream);
 int swg_tlm_apply(swg_adjoint adj, swg_state x0, swg_state dx, double t0,
                   double dt, int nsteps, void *stream);
+/* nsteps <= 10000 (SWG_ERR_ARG above: the schedule planner's limit);
+ * SWG_ERR_BUDGET when nsnapshots is so small that the schedule would re-run
+ * more than 32 plain steps per step (swg_checkpoint_cost > 32 nsteps). */
 int swg_adj_forward(swg_adjoint adj, swg_state state0, double t0, double dt,
                     int nsteps, swg_state final_out, void *stream);
 int swg_adj_backward(swg_adjoint adj, swg_state lambda, void *stream);
@@ -313,7 +316,8 @@ int swg_adj_info(swg_adjoint adj, long long *plain_steps,
  * also enters tracer diffusion, which this gradient leaves out. */
 int swg_adj_grad_visc(swg_adjoint adj, double *grad_edge, double *grad_cell,
                       void *stream);
-/* plain advances of the optimal binomial schedule (host only) */
+/* plain advances of the optimal binomial schedule (host only; -1 for
+ * nsteps outside [1, 10000] or nsnapshots < 1) */
 long long swg_checkpoint_cost(int nsteps, int nsnapshots);
 
 /* ------------------------------------------------------- diagnostics -----

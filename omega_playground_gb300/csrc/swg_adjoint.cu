@@ -862,6 +862,12 @@ int adjoint_step(swg_adjoint ad, double dt, cudaStream_t st) {
 }
 
 // ---- binomial schedule
+// The planner's dynamic program costs O(nsteps^2 * snapshots) host work
+// (about a second at the step limit); a schedule that re-runs more than
+// kMaxReadvance plain steps per step is refused as a too small budget.
+constexpr int kMaxAdjointSteps = 10000;
+constexpr long long kMaxReadvance = 32;
+
 struct Planner {
   int N, S;
   std::vector<long long> cost; // (n, s) -> plain advances; n in [0,N], s in [0,S]
@@ -1193,12 +1199,20 @@ namespace {
 // schedules can be interleaved on their own streams.
 int fwd_begin(swg_adjoint ad, swg_state state0, double t0, double dt,
               int nsteps, cudaStream_t st) {
+  if (nsteps > kMaxAdjointSteps)
+    return fail(SWG_ERR_ARG, "swg_adj_forward: more steps than the schedule "
+                             "planner takes (10000); split the trajectory");
+  Planner pl(nsteps, ad->nsnap - 1);
+  if (pl.C(nsteps, ad->nsnap - 1) > kMaxReadvance * (long long)nsteps)
+    return fail(SWG_ERR_BUDGET, "swg_adj_forward: too few snapshots: the "
+                                "schedule would re-run more than 32 plain "
+                                "steps per step; give the adjoint more "
+                                "snapshots");
   ad->t0 = t0;
   ad->dt = dt;
   ad->nsteps = nsteps;
   ad->plain_steps = ad->taped_steps = 0;
   ad->actions.clear();
-  Planner pl(nsteps, ad->nsnap - 1);
   ad->actions.push_back({1, 0, 0});
   pl.gen(ad->actions, 0, nsteps, ad->nsnap - 1, 0, true);
   ad->pos = 0;
@@ -1270,6 +1284,7 @@ extern "C" int swg_adj_forward(swg_adjoint ad, swg_state state0, double t0,
       nsteps < 1)
     return fail(SWG_ERR_ARG, "swg_adj_forward: bad argument");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  NvtxRange range("adjoint_forward_sweep");
   TRY(fwd_begin(ad, state0, t0, dt, nsteps, st));
   for (bool done = false; !done;)
     TRY(fwd_next(ad, final_out, st, &done));
@@ -1283,6 +1298,7 @@ extern "C" int swg_adj_backward(swg_adjoint ad, swg_state lambda,
   if (ad->state != 1)
     return fail(SWG_ERR_STATE, "swg_adj_backward: call swg_adj_forward first");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  NvtxRange range("adjoint_backward_sweep");
   TRY(bwd_begin(ad, lambda, st));
   for (bool done = false; !done;)
     TRY(bwd_next(ad, lambda, st, &done));
@@ -1394,7 +1410,7 @@ extern "C" int swg_adj_grad_visc(swg_adjoint ad, double *grad_edge,
 }
 
 extern "C" long long swg_checkpoint_cost(int nsteps, int nsnapshots) {
-  if (nsteps < 1 || nsnapshots < 1)
+  if (nsteps < 1 || nsnapshots < 1 || nsteps > kMaxAdjointSteps)
     return -1;
   Planner pl(nsteps, nsnapshots - 1);
   return pl.C(nsteps, nsnapshots - 1);

@@ -810,6 +810,7 @@ extern "C" int swg_step(swg_stepper sp, swg_state S, double t0, double dt,
                         int nsteps, int use_graph, void *stream) {
   if (!sp || !compatible(sp->model, S) || nsteps < 0)
     return fail(SWG_ERR_ARG, "swg_step: bad argument");
+  NvtxRange range("time_integration");
   cudaStream_t st = as_stream(stream);
   if (sp->model->forcing) {
     for (int s = 0; s < nsteps; ++s)

@@ -477,6 +477,7 @@ extern "C" int swg_batch_step(swg_batch b, double t0, double dt, int nsteps,
   (void)t0; // stage times only matter to forcing hooks, which batches exclude
   if (!b || nsteps < 0)
     return fail(SWG_ERR_ARG, "swg_batch_step: bad argument");
+  NvtxRange range("time_integration");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   TRY(upload_members(b, dt));
   if (!use_graph) {

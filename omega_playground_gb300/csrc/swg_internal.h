@@ -4,6 +4,7 @@
 #include "../../include/swgpu.h"
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 #include <string>
@@ -124,6 +125,17 @@ template <class T> struct StageArgsT {
   Epilogue ep;
 };
 using StageArgs = StageArgsT<double>;
+
+// NVTX range (header-only NVTX3; no cost without a tool attached), named
+// after the reference's Caliper regions (shallow_water_model.cpp:317-346:
+// auxstate, tendencies, h_tendency, vn_tendency, tr_tendency;
+// benchmark.cpp:154,166: time_integration) so timelines read alike.
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // A second stream and two events owned by a model: independent passes of
 // one evaluation run as a fork/join pair on it (inside captured graphs they

@@ -257,6 +257,7 @@ void launch_aux_t(const MeshView &m, const ModelView &p, const AuxViewT<T> &a,
   const long long VK = m.nvertices * K, CK = m.ncells * K, EK = m.nedges * K;
   if (p.linear) // the linear model has no intermediates
     return;
+  NvtxRange range("auxstate");
   // vertex and cell passes read only the state: independent
   const bool vert = p.do_vn;
   const bool cell1 = (p.do_vn && (p.vel_del2 || p.vel_del4)) || p.ntracers > 0;
@@ -293,6 +294,7 @@ void launch_tendency_t(const MeshView &m, const ModelView &p,
                        cudaStream_t st, const Fork *fk) {
   const long long K = m.nlayers;
   const long long CK = m.ncells * K, EK = m.nedges * K;
+  NvtxRange range("tendencies");
   if (p.linear) {
     // The linear passes read neighbouring h and vn of the stage input
     // directly, so an in-place (LSRK) stage first forms the tendency and
@@ -329,6 +331,7 @@ void launch_tendency_t(const MeshView &m, const ModelView &p,
   launch_aux_t<T>(m, p, a, s.h, s.vn, s.tr, st, fk);
   const bool edge = p.do_vn, cell = p.do_h || p.ntracers > 0;
   auto run_edge = [&](cudaStream_t q) {
+    NvtxRange r("vn_tendency");
     Scope sc("k_edge_final", q);
     if (m.ne == 8)
       k_edge_final<8, T><<<nblocks(EK), TPB, 0, q>>>(m, p, a, s);
@@ -336,6 +339,7 @@ void launch_tendency_t(const MeshView &m, const ModelView &p,
       k_edge_final<10, T><<<nblocks(EK), TPB, 0, q>>>(m, p, a, s);
   };
   auto run_cell = [&](cudaStream_t q) {
+    NvtxRange r("h_tendency+tr_tendency");
     Scope sc("k_cell_final", q);
     k_cell_final<T><<<nblocks(CK), TPB, 0, q>>>(m, p, a, s);
   };

@@ -109,3 +109,7 @@ def test_checkpoint_cost_matches_binomial_formula():
         t = r * n - comb(s + r, s + 1) if r > 0 else 0
         assert lib.swg_checkpoint_cost(n, s) == t, (n, s)
     assert lib.swg_checkpoint_cost(1000, 32) == 2405
+    # outside the planner's range
+    assert lib.swg_checkpoint_cost(10001, 32) == -1
+    assert lib.swg_checkpoint_cost(0, 32) == -1
+    assert lib.swg_checkpoint_cost(10, 0) == -1

@@ -159,3 +159,25 @@ def test_finite_differences_full_adjoint_workload():
     16 seeded directions."""
     wl = WORKLOADS["rk4_128x128_adjoint"]
     assert _fd_check(wl, wl.nsteps, 32, 16, 1e-4) <= 1e-6
+
+
+def test_checkpoint_budget_and_step_limit_are_errors():
+    """A budget whose schedule would re-run more than 32 plain steps per step
+    is SWG_ERR_BUDGET (one snapshot for 200 steps: 99.5 per step); more steps
+    than the planner takes is SWG_ERR_ARG; both leave the adjoint usable."""
+    wl = ALL_TERMS
+    mesh, params, model = setup(wl)
+    adj = og.Adjoint(model, 1)
+    x0 = initial_state(mesh, wl)
+    X0 = make_state(mesh, params, x0)
+    XN = og.ShallowWaterState(mesh, params)
+    with pytest.raises(og.SwgError) as e:
+        adj.forward(X0, 0.0, wl.dt, 200, XN)
+    assert e.value.code == 5
+    with pytest.raises(og.SwgError) as e:
+        og.Adjoint(model, 32).forward(X0, 0.0, wl.dt, 10001, XN)
+    assert e.value.code == 1
+    adj.forward(X0, 0.0, wl.dt, 20, XN)   # 190 plain steps: within budget
+    LAM = make_state(mesh, params, rand_like([a.shape for a in x0], 5))
+    adj.backward(LAM)
+    assert adj.info() == (og.checkpoint_cost(20, 1), 20)
