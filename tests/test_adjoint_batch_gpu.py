@@ -70,21 +70,21 @@ def test_viscosity_field_gradient_fd():
         assert abs(fd - an) <= 1e-6 * abs(an), (j, f1, f2, fd, an)
 
 
-def test_batched_adjoint_equals_single_member_adjoints():
+def check_batched_adjoint(wls, budgets):
+    """Batched adjoints (one stream per member) bitwise equal to each
+    member's own adjoint run alone: gradients w.r.t. the initial state and
+    the per-cell viscosity."""
     torch = pytest.importorskip("torch")
-    wls = adjoint_ensemble(n=6, nx_choices=(8, 12, 16), levels=(4, 12),
-                           nsteps=20)
-    budgets = [2, 3, 4, 5, 6, 21]
     members = []
     for i, wl in enumerate(wls):
         visc = lognormal_visc(wl.nx * wl.ny, wl.seed + 5)
         mesh, params, model = build(wl, visc)
         members.append((wl, mesh, params, model, initial_state(mesh, wl),
-                        region_cells(mesh, wl.seed + 99)))
+                        region_cells(mesh, wl.seed + 99), budgets[i]))
 
-    def one(m, batch_objs=None):
-        wl, mesh, params, model, x0, region = m
-        adj = og.Adjoint(model, budgets[members.index(m)])
+    def one(m):
+        wl, mesh, params, model, x0, region, budget = m
+        adj = og.Adjoint(model, budget)
         X0 = og.ShallowWaterState(mesh, params)
         X0.upload(*x0)
         XN = og.ShallowWaterState(mesh, params)
@@ -100,6 +100,7 @@ def test_batched_adjoint_equals_single_member_adjoints():
         G.upload(*g)
         adj.backward(G)
         ref.append((G.download(), adj.grad_visc()[1]))
+        del adj, X0, XN, G
     # all members together, one stream each
     objs = [one(m) for m in members]
     streams = [torch.cuda.Stream() for _ in members]
@@ -120,3 +121,17 @@ def test_batched_adjoint_equals_single_member_adjoints():
         for a, b in zip(G.download(), ref[i][0]):
             np.testing.assert_array_equal(a, b, err_msg=f"member {i}")
         np.testing.assert_array_equal(o[0].grad_visc()[1], ref[i][1])
+
+
+def test_batched_adjoint_equals_single_member_adjoints():
+    """6 uneven members, budgets 2 to 21 snapshots, 20 steps."""
+    wls = adjoint_ensemble(n=6, nx_choices=(8, 12, 16), levels=(4, 12),
+                           nsteps=20)
+    check_batched_adjoint(wls, [2, 3, 4, 5, 6, 21])
+
+
+def test_batched_adjoint_full_ensemble_workload():
+    """The full 32-member ensemble: nx in {32, 64, 96, 128}, 16-64 levels,
+    2 tracers, RK4, 300 steps, 32 snapshots (16 for nx = 128)."""
+    wls = adjoint_ensemble(n=32)
+    check_batched_adjoint(wls, [16 if wl.nx >= 128 else 32 for wl in wls])

@@ -92,6 +92,27 @@ def test_ensemble64_members_match_single_instance():
             np.testing.assert_array_equal(x, y, err_msg=f"member {m}")
 
 
+def test_ensemble64_full_size_workload_matches_single_instance():
+    """The 64-member ensemble workload at full size (nx in {32..192}, 16-96
+    levels, 1-4 tracers; 32.5 M cell-levels), two RK4 steps with the
+    autotuned configuration, every member bitwise equal to its own
+    single-instance run."""
+    wls = ensemble()
+    members = build_members(wls)
+    ref = run_single(members, wls, "rk4", 4, 2)
+    states = [og.ShallowWaterState(m[0], m[1]) for m in members]
+    b = og.Batch([m[2] for m in members], states, "rk4", 4)
+    for st, m in zip(states, members):
+        st.upload(*m[3])
+    b.autotune(wls[0].dt, reps=1)
+    for st, m in zip(states, members):
+        st.upload(*m[3])
+    b.step(0.0, wls[0].dt, 2, use_graph=True)
+    for i, (st, r) in enumerate(zip(states, ref)):
+        for x, y in zip(st.download(), r):
+            np.testing.assert_array_equal(x, y, err_msg=f"member {i}")
+
+
 def test_barrier_wait_limit_reports_timeout_and_context_survives():
     members = build_members(SMALL[:2])
     got, b = run_batch(members, SMALL[:2], "rk4", 4, 1)
