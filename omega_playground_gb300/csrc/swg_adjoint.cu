@@ -1108,6 +1108,15 @@ extern "C" int swg_adjoint_destroy(swg_adjoint ad) {
   return SWG_OK;
 }
 
+// no adjoint or model appears twice (members run concurrently)
+static bool distinct_members(int n, const swg_adjoint *adjs) {
+  for (int a = 0; a < n; ++a)
+    for (int b = a + 1; b < n; ++b)
+      if (adjs[a] == adjs[b] || adjs[a]->model == adjs[b]->model)
+        return false;
+  return true;
+}
+
 static bool same_layout(swg_adjoint ad, swg_state s) {
   return s && s->mesh == ad->model->mesh &&
          s->ntracers == ad->model->params.ntracers;
@@ -1316,6 +1325,10 @@ extern "C" int swg_adj_batch_forward(int n, const swg_adjoint *adjs,
     if (!adjs[m] || !same_layout(adjs[m], states0[m]) ||
         !same_layout(adjs[m], finals[m]))
       return fail(SWG_ERR_ARG, "swg_adj_batch_forward: member mismatch");
+  if (!distinct_members(n, adjs))
+    return fail(SWG_ERR_ARG, "swg_adj_batch_forward: members must have "
+                             "distinct adjoints and models (a shared model's "
+                             "intermediates would be written concurrently)");
   auto S = [&](int m) {
     return streams ? static_cast<cudaStream_t>(streams[m]) : cudaStream_t(0);
   };
@@ -1344,6 +1357,9 @@ extern "C" int swg_adj_batch_backward(int n, const swg_adjoint *adjs,
   for (int m = 0; m < n; ++m)
     if (!adjs[m] || !same_layout(adjs[m], lambdas[m]) || adjs[m]->state != 1)
       return fail(SWG_ERR_ARG, "swg_adj_batch_backward: member not ready");
+  if (!distinct_members(n, adjs))
+    return fail(SWG_ERR_ARG, "swg_adj_batch_backward: members must have "
+                             "distinct adjoints and models");
   auto S = [&](int m) {
     return streams ? static_cast<cudaStream_t>(streams[m]) : cudaStream_t(0);
   };

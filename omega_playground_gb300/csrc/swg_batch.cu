@@ -362,6 +362,11 @@ extern "C" int swg_batch_create(int nmembers, const swg_model *models,
     if (md->view.linear)
       return fail(SWG_ERR_ARG, "swg_batch_create: linear models are not "
                                "batched");
+    for (int j = 0; j < m; ++j)
+      if (models[j] == md || states[j] == states[m])
+        return fail(SWG_ERR_ARG, "swg_batch_create: a model or state appears "
+                                 "in two members (their passes would write "
+                                 "the same arrays concurrently)");
     if (ne && md->mesh->view.ne != ne)
       return fail(SWG_ERR_ARG, "swg_batch_create: members must share the "
                                "edges-on-edge width (8 or 10)");

@@ -135,3 +135,15 @@ def test_batched_adjoint_full_ensemble_workload():
     2 tracers, RK4, 300 steps, 32 snapshots (16 for nx = 128)."""
     wls = adjoint_ensemble(n=32)
     check_batched_adjoint(wls, [16 if wl.nx >= 128 else 32 for wl in wls])
+
+
+def test_batched_adjoint_rejects_members_sharing_a_model():
+    wl = adjoint_ensemble(n=1, nx_choices=(8,), levels=(4, 4), nsteps=4)[0]
+    mesh, params, model = build(wl, lognormal_visc(wl.nx * wl.ny, 3))
+    adjs = [og.Adjoint(model, 2), og.Adjoint(model, 2)]
+    x0 = initial_state(mesh, wl)
+    X = [og.ShallowWaterState(mesh, params) for _ in range(4)]
+    for s in X[:2]:
+        s.upload(*x0)
+    with pytest.raises(og.SwgError):
+        og.adjoint_batch_forward(adjs, X[:2], 0.0, wl.dt, 4, X[2:])

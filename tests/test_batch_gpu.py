@@ -135,3 +135,18 @@ def test_batch_rejects_hooked_members():
     st = og.ShallowWaterState(mesh, params)
     with pytest.raises(og.SwgError):
         og.Batch([Forced(mesh, params)], [st])
+
+
+def test_batch_rejects_shared_models_and_states():
+    """Members run concurrently, so a model (its intermediates) or a state
+    shared by two members would be written by both: refused on the host."""
+    mesh = og.PlanarHexagonalMesh(8, 8, 1e4, 4)
+    params = og.ShallowWaterParams(m_f0=1e-4)
+    model = og.ShallowWaterModel(mesh, params)
+    other = og.ShallowWaterModel(mesh, params)
+    a, b = og.ShallowWaterState(mesh, params), og.ShallowWaterState(mesh, params)
+    with pytest.raises(og.SwgError):
+        og.Batch([model, model], [a, b])
+    with pytest.raises(og.SwgError):
+        og.Batch([model, other], [a, a])
+    og.Batch([model, other], [a, b])  # distinct members are fine
