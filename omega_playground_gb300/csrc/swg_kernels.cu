@@ -269,6 +269,10 @@ void launch_aux_t(const MeshView &m, const ModelView &p, const AuxViewT<T> &a,
     Scope sc("k_cell1", s);
     k_cell1<T><<<nblocks(CK), TPB, 0, s>>>(m, p, a, h, vn, tr);
   };
+  // per-kernel timing (profiling on) runs the passes one after another so
+  // that each event pair times its own kernel alone
+  if (g_profile)
+    fk = nullptr;
   if (vert && cell1)
     fork_join(fk, st, run_vertex, run_cell1);
   else if (vert)
@@ -347,7 +351,8 @@ void launch_tendency_t(const MeshView &m, const ModelView &p,
   // place (LSRK): there the edge pass reads h, which the cell pass rewrites,
   // so the edge pass goes first.
   if (edge && cell)
-    fork_join(s.ep.mode == EPI_LSRK ? nullptr : fk, st, run_edge, run_cell);
+    fork_join(s.ep.mode == EPI_LSRK || g_profile ? nullptr : fk, st, run_edge,
+              run_cell);
   else if (edge)
     run_edge(st);
   else if (cell)
