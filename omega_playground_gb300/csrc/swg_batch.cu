@@ -129,6 +129,38 @@ __global__ void __launch_bounds__(512)
   }
 }
 
+// One pass of one stage for all members (the per-pass launch shape), with
+// the pass fixed at compile time: each pass kernel is compiled on its own,
+// so a light pass does not carry the registers of the heaviest one and
+// keeps the occupancy of the single-instance kernels.
+template <int NE, int ITEMS, int PASS>
+__global__ void __launch_bounds__(512)
+    k_batch_pass(const Member *__restrict__ mem, int nmem,
+                 const unsigned *__restrict__ prefix, int stage) {
+  const unsigned vbsize = blockDim.x * ITEMS;
+  const unsigned *pre = prefix + PASS * (nmem + 1);
+  const unsigned nvb = pre[nmem];
+  for (unsigned vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+    int lo = 0, hi = nmem;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (pre[mid] <= vb)
+        lo = mid;
+      else
+        hi = mid;
+    }
+    const Member &M = mem[lo];
+    const unsigned n = M.units[PASS];
+    const unsigned first = (vb - pre[lo]) * vbsize + threadIdx.x;
+#pragma unroll
+    for (int it = 0; it < ITEMS; ++it) {
+      const unsigned i = first + it * blockDim.x;
+      if (i < n)
+        run_pass<NE>(PASS, M, stage, i);
+    }
+  }
+}
+
 // A wait that nothing releases, for testing the barrier's time limit: every
 // block but block 0 waits at a barrier block 0 never reaches.
 __global__ void k_barrier_selftest(BatchSync *bs, long long limit) {
@@ -254,6 +286,24 @@ void *pick_kernel(int ne, int items) {
   return items == 1 ? kernel_ptr<10, 1>() : kernel_ptr<10, 2>();
 }
 
+template <int NE, int ITEMS> void *pass_kernel_ptr(int pass) {
+  switch (pass) {
+  case P_VERTEX: return reinterpret_cast<void *>(&k_batch_pass<NE, ITEMS, P_VERTEX>);
+  case P_CELL1: return reinterpret_cast<void *>(&k_batch_pass<NE, ITEMS, P_CELL1>);
+  case P_EDGE1: return reinterpret_cast<void *>(&k_batch_pass<NE, ITEMS, P_EDGE1>);
+  case P_AUX2: return reinterpret_cast<void *>(&k_batch_pass<NE, ITEMS, P_AUX2>);
+  case P_EDGE_FINAL:
+    return reinterpret_cast<void *>(&k_batch_pass<NE, ITEMS, P_EDGE_FINAL>);
+  default: return reinterpret_cast<void *>(&k_batch_pass<NE, ITEMS, P_CELL_FINAL>);
+  }
+}
+
+void *pick_pass_kernel(int ne, int items, int pass) {
+  if (ne == 8)
+    return items == 1 ? pass_kernel_ptr<8, 1>(pass) : pass_kernel_ptr<8, 2>(pass);
+  return items == 1 ? pass_kernel_ptr<10, 1>(pass) : pass_kernel_ptr<10, 2>(pass);
+}
+
 // prefix tables for one virtual-block size: [NPASS][nmem+1]
 int upload_prefix(swg_batch b, unsigned vbsize) {
   std::vector<unsigned> pre(size_t(NPASS) * (b->nmem + 1));
@@ -307,9 +357,9 @@ int launch_stage(swg_batch b, int stage, cudaStream_t st) {
     const unsigned nvb = b->prefix_h[pass * (nmem + 1) + nmem];
     if (nvb == 0)
       continue;
-    int p0 = pass, p1 = pass;
-    void *args[] = {&mem, &nmem, &pre, &stage, &p0, &p1, &bs, &limit};
-    cudaError_t err = cudaLaunchKernel(fn, dim3(nvb), dim3(c.block), args, 0, st);
+    void *args[] = {&mem, &nmem, &pre, &stage};
+    cudaError_t err = cudaLaunchKernel(pick_pass_kernel(b->ne, c.items, pass),
+                                       dim3(nvb), dim3(c.block), args, 0, st);
     if (err != cudaSuccess)
       return cuda_fail(err, "swg_batch: pass launch");
     ++g_launches;
