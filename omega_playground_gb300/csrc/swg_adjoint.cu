@@ -153,7 +153,10 @@ __device__ __forceinline__ double fwd_rcp(double x) {
 }
 
 // --- pass 2: tracer tendency transposed to the normalised tracers (partial)
-// and to the tracer Laplacian.
+// and to the tracer Laplacian.  D2, D4: tracer del2 / del4 on, as
+// compile-time switches (with runtime flags the diffusion arrays stayed in
+// registers and lowered the occupancy of the diffusion-free case).
+template <bool D2, bool D4>
 __global__ void __launch_bounds__(ATPB)
     ka_tr1(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
            AdjIO io) {
@@ -171,7 +174,7 @@ __global__ void __launch_bounds__(ATPB)
     const double F = a.F[size_t(e) * K + k];
     double x = __ldg(v.ccdh_nb + 6 * c + j) * F;
     wc = fma(__ldg(m.ccdh + 6 * c + j), F, wc);
-    if (p.tr_del2) {
+    if (D2) {
       const double mh = mean_h(m, a, io.h, e, k);
       x = fma(__ldg(v.kd2_nb + 6 * c + j), mh, x);
       wc = fma(-__ldg(p.kd2 + 6 * c + j), mh, wc);
@@ -184,7 +187,7 @@ __global__ void __launch_bounds__(ATPB)
     for (int j = 0; j < MAXE; ++j)
       acc = fma(wnb[j], mu[size_t(nb[j]) * K + k], acc);
     w.ln[size_t(l) * CK + i] = acc;
-    if (p.tr_del4) {
+    if (D4) {
       double L = -__ldg(p.r4sum + c) * mu[i];
       for (int j = 0; j < MAXE; ++j)
         L = fma(__ldg(v.r4_nb + 6 * c + j), mu[size_t(nb[j]) * K + k], L);
@@ -194,7 +197,8 @@ __global__ void __launch_bounds__(ATPB)
 }
 
 // --- pass 3: through the tracer Laplacian and n = tr / h to the tracers;
-// the h part of n = tr / h is kept for pass 6.
+// the h part of n = tr / h is kept for pass 6.  D4: tracer del4 on.
+template <bool D4>
 __global__ void __launch_bounds__(ATPB)
     ka_tr2(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
            AdjIO io) {
@@ -206,7 +210,7 @@ __global__ void __launch_bounds__(ATPB)
   const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
   double mnb[MAXE], M = 0;
   int nb[MAXE];
-  if (p.tr_del4)
+  if (D4)
     for (int j = 0; j < MAXE; ++j) {
       const int e = __ldg(m.ec + 6 * c + j);
       const double mh = mean_h(m, a, io.h, e, k);
@@ -220,7 +224,7 @@ __global__ void __launch_bounds__(ATPB)
   for (int l = 0; l < p.ntracers; ++l) {
     const size_t t = size_t(l) * CK + i;
     double ln = w.ln[t];
-    if (p.tr_del4) {
+    if (D4) {
       const double *lL = w.lL + size_t(l) * CK;
       ln = fma(-M, lL[i], ln);
       for (int j = 0; j < MAXE; ++j)
@@ -711,11 +715,21 @@ void adj_passes(swg_adjoint ad, const AuxView &aux, const AdjIO &io,
     ++g_launches;
   };
   auto tr1 = [&](cudaStream_t q) {
-    ka_tr1<<<nb(CK), ATPB, 0, q>>>(m, p, aux, v, w, io);
+    if (p.tr_del2 && p.tr_del4)
+      ka_tr1<true, true><<<nb(CK), ATPB, 0, q>>>(m, p, aux, v, w, io);
+    else if (p.tr_del2)
+      ka_tr1<true, false><<<nb(CK), ATPB, 0, q>>>(m, p, aux, v, w, io);
+    else if (p.tr_del4)
+      ka_tr1<false, true><<<nb(CK), ATPB, 0, q>>>(m, p, aux, v, w, io);
+    else
+      ka_tr1<false, false><<<nb(CK), ATPB, 0, q>>>(m, p, aux, v, w, io);
     ++g_launches;
   };
   auto tr2 = [&](cudaStream_t q) {
-    ka_tr2<<<nb(CK), ATPB, 0, q>>>(m, p, aux, v, w, io);
+    if (p.tr_del4)
+      ka_tr2<true><<<nb(CK), ATPB, 0, q>>>(m, p, aux, v, w, io);
+    else
+      ka_tr2<false><<<nb(CK), ATPB, 0, q>>>(m, p, aux, v, w, io);
     ++g_launches;
   };
   auto edge = [&](cudaStream_t q) {
