@@ -373,6 +373,19 @@ struct ShallowWaterModel {
         nullptr));
   }
 
+  // Settles whether additional_tendency is overridden: one tendency
+  // evaluation on a scratch state (h = vn = 1) runs the hook once; the base
+  // no-op then unregisters itself.  The ensemble and adjoint classes call it
+  // because the library refuses models that still carry a hook.
+  void resolve_hook() const {
+    if (m_default_hook)
+      return;
+    ShallowWaterState tend(m_mesh, m_params), state(m_mesh, m_params);
+    swg_check(swg_state_fill(state.handle(), 1.0, nullptr));
+    compute_tendency(tend, state, 0.0);
+    fence();
+  }
+
 private:
   mutable bool m_default_hook = false;
 
@@ -445,6 +458,93 @@ struct RK4Stepper : TimeStepper {
   static constexpr Int nstages = 4;
   explicit RK4Stepper(ShallowWaterModel &shallow_water)
       : TimeStepper(shallow_water, SWG_STEPPER_RK4, 4) {}
+};
+
+// ----------------------------------------------- ensembles and gradients --
+// Beside the plain solver; no counterpart in the reference.
+
+// Many independent members (own mesh size, levels and tracers) advanced
+// together: one persistent kernel, or one launch per pass, per RK stage
+// (swg_batch_*).  Members must have distinct models and states.
+struct EnsembleStepper {
+  swg_batch m_handle = nullptr;
+  EnsembleStepper(const std::vector<ShallowWaterModel *> &models,
+                  const std::vector<const ShallowWaterState *> &states,
+                  bool rk4 = true, Int nstages = 4) {
+    std::vector<swg_model> mh;
+    std::vector<swg_state> sh;
+    for (auto *m : models) {
+      m->resolve_hook();
+      mh.push_back(m->m_handle);
+    }
+    for (auto *s : states)
+      sh.push_back(s->handle());
+    if (mh.size() != sh.size())
+      throw std::runtime_error("EnsembleStepper: models and states differ in number");
+    swg_check(swg_batch_create(int(mh.size()), mh.data(), sh.data(),
+                               rk4 ? SWG_STEPPER_RK4 : SWG_STEPPER_LSRK,
+                               rk4 ? 4 : nstages, &m_handle));
+  }
+  EnsembleStepper(const EnsembleStepper &) = delete;
+  EnsembleStepper &operator=(const EnsembleStepper &) = delete;
+  ~EnsembleStepper() { swg_batch_destroy(m_handle); }
+  // times every launch configuration on these members (advancing them) and
+  // keeps the fastest; returns its index
+  int autotune(Real dt, int reps = 2, double *ms_per_step = nullptr) {
+    int best = 0;
+    double ms = 0;
+    swg_check(swg_batch_autotune(m_handle, dt, reps, nullptr, &best, &ms));
+    if (ms_per_step)
+      *ms_per_step = ms;
+    return best;
+  }
+  void do_steps(Real t0, Real dt, Int nsteps) const {
+    swg_check(swg_batch_step(m_handle, t0, dt, nsteps, 1, nullptr));
+    swg_check(swg_batch_check(m_handle, nullptr));
+  }
+};
+
+// Gradient of a loss of the state after nsteps RK4 steps with respect to the
+// initial state (and the del2 viscosity), by the hand-written adjoint with
+// binomial checkpointing over `nsnapshots` states (swg_adjoint_*):
+//   adj.forward(x0, t0, dt, n, xN);  lambda <- dL/dxN;  adj.backward(lambda);
+//   lambda now holds dL/dx0.
+struct CheckpointedAdjoint {
+  swg_adjoint m_handle = nullptr;
+  explicit CheckpointedAdjoint(ShallowWaterModel &model, Int nsnapshots = 32) {
+    model.resolve_hook();
+    swg_check(swg_adjoint_create(model.m_handle, nsnapshots, &m_handle));
+  }
+  CheckpointedAdjoint(const CheckpointedAdjoint &) = delete;
+  CheckpointedAdjoint &operator=(const CheckpointedAdjoint &) = delete;
+  ~CheckpointedAdjoint() { swg_adjoint_destroy(m_handle); }
+  void forward(const ShallowWaterState &x0, Real t0, Real dt, Int nsteps,
+               const ShallowWaterState &xN) {
+    swg_check(swg_adj_forward(m_handle, x0.handle(), t0, dt, nsteps,
+                              xN.handle(), nullptr));
+  }
+  void backward(const ShallowWaterState &lambda) {
+    swg_check(swg_adj_backward(m_handle, lambda.handle(), nullptr));
+  }
+  // dx <- J dx over nsteps steps from x0 (tangent-linear model)
+  void tlm_apply(const ShallowWaterState &x0, const ShallowWaterState &dx,
+                 Real t0, Real dt, Int nsteps) {
+    swg_check(swg_tlm_apply(m_handle, x0.handle(), dx.handle(), t0, dt,
+                            nsteps, nullptr));
+  }
+  // dL/d(viscosity) of the last backward: per edge and per cell
+  void grad_visc(std::vector<Real> &per_edge, std::vector<Real> &per_cell,
+                 const MPASMesh &mesh) {
+    per_edge.resize(mesh.m_nedges);
+    per_cell.resize(mesh.m_ncells);
+    swg_check(swg_adj_grad_visc(m_handle, per_edge.data(), per_cell.data(),
+                                nullptr));
+  }
+  long long plain_steps() const {
+    long long p = 0, t = 0;
+    swg_check(swg_adj_info(m_handle, &p, &t));
+    return p;
+  }
 };
 
 // ------------------------------------------------------------ diagnostics --

@@ -1,0 +1,161 @@
+// The C++ drop-in's ensemble and gradient classes, used the way a reference
+// user would: (1) a dot-product test of the checkpointed adjoint against the
+// tangent-linear model over 10 RK4 steps with every term on,
+// <J dx0, lamN> = <dx0, J^T lamN> to 1e-12; (2) three members of different
+// sizes advanced by EnsembleStepper equal, bit for bit, the same members
+// advanced one at a time by RK4Stepper.  Exits non-zero on failure.
+#include <omega_gpu.hpp>
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <memory>
+#include <vector>
+
+using namespace omega;
+
+namespace {
+
+struct SplitMix {
+  uint64_t s;
+  double next() { // uniform in [0, 1)
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return double(z >> 11) * 0x1.0p-53;
+  }
+};
+
+struct Fields {
+  std::vector<Real> h, vn, tr;
+};
+
+Fields random_state(const MPASMesh &m, Int ntr, uint64_t seed, Real h0,
+                    Real hs, Real vs, Real ts) {
+  SplitMix r{seed};
+  const size_t C = size_t(m.m_ncells) * m.m_nlayers;
+  const size_t E = size_t(m.m_nedges) * m.m_nlayers;
+  Fields f;
+  for (size_t i = 0; i < C; ++i)
+    f.h.push_back(h0 + hs * (r.next() - 0.5));
+  for (size_t i = 0; i < E; ++i)
+    f.vn.push_back(vs * (r.next() - 0.5));
+  for (Int l = 0; l < ntr; ++l)
+    for (size_t i = 0; i < C; ++i)
+      f.tr.push_back(ts * (h0 > 0 ? f.h[i] * r.next() : r.next() - 0.5));
+  return f;
+}
+
+double dot(const Fields &a, const Fields &b) {
+  double s = 0;
+  for (size_t i = 0; i < a.h.size(); ++i)
+    s += a.h[i] * b.h[i];
+  for (size_t i = 0; i < a.vn.size(); ++i)
+    s += a.vn[i] * b.vn[i];
+  for (size_t i = 0; i < a.tr.size(); ++i)
+    s += a.tr[i] * b.tr[i];
+  return s;
+}
+
+Fields download(const ShallowWaterState &s) {
+  Fields f;
+  s.download(f.h, f.vn, f.tr);
+  return f;
+}
+
+bool dot_product_test() {
+  PlanarHexagonalMesh mesh(12, 10, 1e4, 5);
+  ShallowWaterParams p;
+  p.m_f0 = 1e-4;
+  p.m_visc_del2 = 1e3;
+  p.m_visc_del4 = 1e9;
+  p.m_eddy_diff2 = 1e3;
+  p.m_eddy_diff4 = 1e9;
+  p.m_ntracers = 2;
+  ShallowWaterModel model(&mesh, p);
+  const Real dt = 20, t0 = 0;
+  const Int nsteps = 10;
+  CheckpointedAdjoint adj(model, 4);
+
+  const Fields x0 = random_state(mesh, 2, 11, 1000, 2, 0.2, 1);
+  const Fields dx0 = random_state(mesh, 2, 22, 0, 1, 0.01, 10);
+  const Fields lamN = random_state(mesh, 2, 33, 0, 1, 1, 1);
+  ShallowWaterState X0(&mesh, p), XN(&mesh, p), DX(&mesh, p), LAM(&mesh, p);
+  X0.upload(x0.h, x0.vn, x0.tr);
+  DX.upload(dx0.h, dx0.vn, dx0.tr);
+  LAM.upload(lamN.h, lamN.vn, lamN.tr);
+  adj.forward(X0, t0, dt, nsteps, XN);
+  adj.backward(LAM);
+  adj.tlm_apply(X0, DX, t0, dt, nsteps);
+  const double lhs = dot(download(DX), lamN);
+  const double rhs = dot(dx0, download(LAM));
+  const double rel = std::fabs(lhs - rhs) / std::fmax(std::fabs(lhs), std::fabs(rhs));
+  std::printf("dot_product lhs=%.17e rhs=%.17e rel=%.3e plain_steps=%lld\n",
+              lhs, rhs, rel, adj.plain_steps());
+  return rel <= 1e-12;
+}
+
+bool ensemble_test() {
+  struct Member {
+    std::unique_ptr<PlanarHexagonalMesh> mesh;
+    ShallowWaterParams p;
+    std::unique_ptr<ShallowWaterModel> model;
+    Fields x0;
+  };
+  const Int nx[3] = {8, 12, 16}, K[3] = {3, 7, 5}, T[3] = {1, 0, 3};
+  std::vector<Member> mem(3);
+  for (int m = 0; m < 3; ++m) {
+    mem[m].mesh = std::make_unique<PlanarHexagonalMesh>(nx[m], nx[m], 1e4, K[m]);
+    mem[m].p.m_f0 = 1e-4;
+    mem[m].p.m_visc_del2 = 1e3;
+    mem[m].p.m_ntracers = T[m];
+    mem[m].model = std::make_unique<ShallowWaterModel>(mem[m].mesh.get(), mem[m].p);
+    mem[m].x0 = random_state(*mem[m].mesh, T[m], 100 + m, 1000, 2, 0.2, 1);
+  }
+  const Real dt = 20;
+  // one at a time
+  std::vector<Fields> ref;
+  for (auto &m : mem) {
+    ShallowWaterState s(m.mesh.get(), m.p);
+    s.upload(m.x0.h, m.x0.vn, m.x0.tr);
+    RK4Stepper st(*m.model);
+    st.do_steps(0, dt, s, 3);
+    ref.push_back(download(s));
+  }
+  // together
+  std::vector<std::unique_ptr<ShallowWaterState>> states;
+  std::vector<ShallowWaterModel *> models;
+  std::vector<const ShallowWaterState *> sp;
+  for (auto &m : mem) {
+    states.push_back(std::make_unique<ShallowWaterState>(m.mesh.get(), m.p));
+    models.push_back(m.model.get());
+    sp.push_back(states.back().get());
+  }
+  EnsembleStepper ens(models, sp);
+  ens.autotune(dt, 1);
+  for (int m = 0; m < 3; ++m)
+    states[m]->upload(mem[m].x0.h, mem[m].x0.vn, mem[m].x0.tr);
+  ens.do_steps(0, dt, 3);
+  double worst = 0;
+  for (int m = 0; m < 3; ++m) {
+    const Fields got = download(*states[m]);
+    for (size_t i = 0; i < got.h.size(); ++i)
+      worst = std::fmax(worst, std::fabs(got.h[i] - ref[m].h[i]));
+    for (size_t i = 0; i < got.vn.size(); ++i)
+      worst = std::fmax(worst, std::fabs(got.vn[i] - ref[m].vn[i]));
+    for (size_t i = 0; i < got.tr.size(); ++i)
+      worst = std::fmax(worst, std::fabs(got.tr[i] - ref[m].tr[i]));
+  }
+  std::printf("ensemble max_abs_diff=%.3e\n", worst);
+  return worst == 0.0;
+}
+
+} // namespace
+
+int main() {
+  const bool a = dot_product_test();
+  const bool b = ensemble_test();
+  std::printf("%s\n", a && b ? "PASS" : "FAIL");
+  return a && b ? 0 : 1;
+}

@@ -93,3 +93,14 @@ def test_benchmark_driver_runs():
     out = run("benchmark", "64", "16", "1", "4")
     m = re.search(r"updates_per_s=(\S+)", out)
     assert m and float(m.group(1)) > 0
+
+
+def test_cpp_gradient_and_ensemble_classes():
+    """The C++ drop-in's CheckpointedAdjoint (dot product against the
+    tangent-linear model, 10 RK4 steps, every term on, <= 1e-12) and
+    EnsembleStepper (three uneven members bitwise equal to RK4Stepper)."""
+    out = run("gradients_and_ensembles")
+    assert "PASS" in out, out
+    rel = float(re.search(r"rel=(\S+)", out).group(1))
+    assert rel <= 1e-12
+    assert "max_abs_diff=0.000e+00" in out
