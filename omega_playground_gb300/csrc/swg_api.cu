@@ -323,6 +323,8 @@ extern "C" int swg_state_create(swg_mesh m, int ntracers, swg_state *out) {
   swg_state s = new (std::nothrow) swg_state_s();
   if (!s)
     return fail(SWG_ERR_OOM, "swg_state_create: host allocation");
+  static std::atomic<unsigned long long> next_serial{1};
+  s->serial = next_serial++;
   s->mesh = m;
   s->ntracers = ntracers;
   const size_t n = state_words(m, ntracers);
@@ -822,7 +824,7 @@ extern "C" int swg_step(swg_stepper sp, swg_state S, double t0, double dt,
       TRY(fused_step(sp, S, dt, st));
     return SWG_OK;
   }
-  if (!sp->graph || sp->graph_state != S || sp->graph_dt != dt) {
+  if (!sp->graph || sp->graph_serial != S->serial || sp->graph_dt != dt) {
     if (sp->graph) {
       cudaGraphExecDestroy(sp->graph);
       sp->graph = nullptr;
@@ -854,7 +856,7 @@ extern "C" int swg_step(swg_stepper sp, swg_state S, double t0, double dt,
       sp->graph = nullptr;
       return cuda_fail(err, "swg_step: graph instantiate");
     }
-    sp->graph_state = S;
+    sp->graph_serial = S->serial;
     sp->graph_dt = dt;
   }
   for (int s = 0; s < nsteps; ++s) {

@@ -207,6 +207,9 @@ struct swg_state_s {
   int ntracers;
   double *h, *vn, *tr;
   void *block;
+  // creation number, never reused: identifies the state in cached graphs
+  // (a handle address can be reused after destroy, with other device memory)
+  unsigned long long serial;
 };
 
 struct swg_model_s {
@@ -227,7 +230,7 @@ struct swg_stepper_s {
   std::vector<double> rka, rkb, rkc;
   swg_state tend, acc, p0, p1, old;
   cudaGraphExec_t graph;       // one captured step (fused path)
-  swg_state graph_state;
+  unsigned long long graph_serial; // the state the graph was captured for
   double graph_dt;
   long long graph_launches;    // kernels per captured step
 };
