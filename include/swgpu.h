@@ -267,19 +267,24 @@ int swg_batch_selftest_timeout(swg_batch batch, double limit_ms,
                                void *stream);
 
 /* ------------------------------------------ adjoint and tangent-linear ----
- * Differentiation of the RK4 step (no counterpart in the reference).  An
+ * Differentiation of the RK4 or low-storage RK step (no counterpart in the
+ * reference).  An
  * adjoint object is tied to a model (no forcing hook, edge_mask all ones,
  * dv >= dc/4) and owns `nsnapshots` state checkpoints for the binomial
  * checkpointing schedule, the stage tape of one step and the adjoint work
  * arrays.  Tendency level, in the style of an autograd Function's jvp/vjp:
  *   swg_tlm_tendency: dtend = J(x) dx        (exact forward-mode derivative)
  *   swg_adj_tendency: lambda = J(x)^T mu     (hand-written reverse mode)
- * Trajectory level (RK4, dt fixed):
+ * Trajectory level (the adjoint's stepper, dt fixed):
  *   swg_tlm_apply:   dx <- d x_N (propagated tangent of nsteps steps)
  *   swg_adj_forward: runs nsteps steps from state0 storing checkpoints,
  *                    writes x_N to final_out;
  *   swg_adj_backward: lambda (in: dL/dx_N) <- dL/dx_0. */
 int swg_adjoint_create(swg_model model, int nsnapshots, swg_adjoint *out);
+/* the same for another stepper: SWG_STEPPER_RK4 (nstages ignored) or
+ * SWG_STEPPER_LSRK with nstages 5 or 1 (lsrk.cpp:16-33, 36-89) */
+int swg_adjoint_create_stepper(swg_model model, int nsnapshots, int kind,
+                               int nstages, swg_adjoint *out);
 int swg_adjoint_destroy(swg_adjoint adj);
 int swg_tlm_tendency(swg_adjoint adj, swg_state x, swg_state dx,
                      swg_state dtend_out, void *stream);

@@ -133,6 +133,8 @@ _SIGS = {
                                      C.POINTER(C.c_int), _dp]),
     "swg_batch_selftest_timeout": (C.c_int, [_vp, C.c_double, _vp]),
     "swg_adjoint_create": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
+    "swg_adjoint_create_stepper": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int,
+                                             C.POINTER(_vp)]),
     "swg_adjoint_destroy": (C.c_int, [_vp]),
     "swg_tlm_tendency": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "swg_adj_tendency": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),

@@ -71,23 +71,29 @@ struct AdjIO {
   const double *h, *vn, *tr;    // state X
   const double *mh_, *mvn, *mtr; // mu (adjoint of the tendency)
   double *lh, *lvn, *ltr;        // lambda = J^T mu (written unless null)
-  // fused RK4 bookkeeping (each may be null): acc += lambda, and the next
-  // stage's mu_next = alpha * lam + beta * lambda
+  // fused stage bookkeeping (each may be null): acc += lambda, and the next
+  // stage's mu: RK4  mu_next = alpha * lam + beta * lambda;
+  //             LSRK mu_next = alpha * acc (after the update) + gamma * mu
   double *acc_h, *acc_vn, *acc_tr;
   double *nmu_h, *nmu_vn, *nmu_tr;
   const double *lam_h, *lam_vn, *lam_tr;
-  double alpha, beta;
+  double alpha, beta, gamma;
+  int lsrk;
 };
 
-__device__ __forceinline__ void emit(double *out, double *acc, double *nmu,
-                                     const double *lam, double alpha,
-                                     double beta, size_t i, double x) {
+__device__ __forceinline__ void emit(const AdjIO &io, double *out, double *acc,
+                                     double *nmu, const double *lam,
+                                     const double *mu, size_t i, double x) {
   if (out)
     out[i] = x;
-  if (acc)
-    acc[i] += x;
+  double a = 0;
+  if (acc) {
+    a = acc[i] + x;
+    acc[i] = a;
+  }
   if (nmu)
-    nmu[i] = fma(alpha, lam[i], beta * x);
+    nmu[i] = io.lsrk ? fma(io.alpha, a, io.gamma * mu[i])
+                     : fma(io.alpha, lam[i], io.beta * x);
 }
 
 // --- pass 1: transposed edge stencils of the velocity tendency (cells and
@@ -230,7 +236,7 @@ __global__ void __launch_bounds__(ATPB)
       for (int j = 0; j < MAXE; ++j)
         ln = fma(mnb[j], lL[size_t(nb[j]) * K + k], ln);
     }
-    emit(io.ltr, io.acc_tr, io.nmu_tr, io.lam_tr, io.alpha, io.beta, t,
+    emit(io, io.ltr, io.acc_tr, io.nmu_tr, io.lam_tr, io.mtr, t,
          ln * r);
     hsum = fma(ln, a.ntr[t], hsum);
   }
@@ -377,7 +383,7 @@ __global__ void __launch_bounds__(ATPB)
     lh += w.lhs[i];
   if (p.ntracers > 0)
     lh += w.lhtr[i];
-  emit(io.lh, io.acc_h, io.nmu_h, io.lam_h, io.alpha, io.beta, i, lh);
+  emit(io, io.lh, io.acc_h, io.nmu_h, io.lam_h, io.mh_, i, lh);
   if (p.do_vn && (p.vel_del2 | p.vel_del4))
     w.ldiv[i] = ld;
 }
@@ -401,7 +407,7 @@ __global__ void __launch_bounds__(ATPB)
       l = fma(__ldg(v.ccd_e2 + 2 * e + 1), w.ldiv[size_t(c1) * K + k], l);
     }
   }
-  emit(io.lvn, io.acc_vn, io.nmu_vn, io.lam_vn, io.alpha, io.beta, i, l);
+  emit(io, io.lvn, io.acc_vn, io.nmu_vn, io.lam_vn, io.mvn, i, l);
 }
 
 // y = alpha x1 + beta x2 (x2 may be null); dual pack / unpack
@@ -456,10 +462,14 @@ struct swg_adjoint_s {
   std::vector<void *> allocs;
   swg_stepper stepper = nullptr; // plain advances (graph replay)
   std::vector<swg_state> snaps;
-  swg_state cur = nullptr, next = nullptr, X[4] = {}, acc = nullptr,
+  // stepper differentiated: RK4 (4 stages) or LSRK with 5 or 1 stages;
+  // rka / rkb are its coefficients (as in swg_stepper_create)
+  int kind = SWG_STEPPER_RK4, ns = 4;
+  std::vector<double> rka, rkb;
+  swg_state cur = nullptr, next = nullptr, X[5] = {}, acc = nullptr,
             lam = nullptr, lacc = nullptr, mu = nullptr, mu2 = nullptr,
             lX = nullptr;
-  AuxView taux[4]{};              // intermediates of the taped stages
+  AuxView taux[5]{};              // intermediates of the taped stages
   cudaGraphExec_t tape_graph = nullptr;
   double tape_graph_dt = 0;
   long long tape_graph_launches = 0;
@@ -688,7 +698,7 @@ int alloc_tape(swg_adjoint ad, int s) {
   TRY(alloc_aux_like(ad, t));
   if (md->view.do_vn) {
     TRY(zal(A, V * K, &t.rhv));
-    if (s < 3)
+    if (s < ad->ns - 1)
       TRY(zal(A, E * K, &t.S1));
   }
   if (md->params.ntracers > 0)
@@ -799,9 +809,44 @@ void stage_ptrs(swg_adjoint ad, int s, const double **h, const double **vn,
   *tr = ad->X[s]->tr;
 }
 
+// Taped low-storage RK step (lsrk.cpp:36-89) from X0: stage s forms
+// T = a_s T + F(X_s) in ad->acc and X_{s+1} = X_s + dt b_s T in a separate
+// buffer (a copy of X_s updated by the same epilogue as the in-place
+// stepper, so the values are the stepper's bit for bit).  The last stage
+// only records its intermediates unless `out` takes the step's result.
+int tape_step_lsrk(swg_adjoint ad, double dt, swg_state out, cudaStream_t st) {
+  swg_model md = ad->model;
+  const ModelView &pv = md->view;
+  const int ns = ad->ns;
+  for (int s = 0; s < ns; ++s) {
+    const double *h, *vn, *tr;
+    stage_ptrs(ad, s, &h, &vn, &tr);
+    swg_state o = s < ns - 1 ? ad->X[s + 1] : out;
+    if (!o) {
+      launch_aux(md->mesh->view, pv, ad->taux[s], h, vn, tr, st, &md->fork);
+      continue;
+    }
+    TRY(swg_state_copy(o, ad->X[s], st));
+    StageArgs a{};
+    a.h = h;
+    a.vn = vn;
+    a.tr = tr;
+    a.fh = {ad->acc->h, nullptr, nullptr, o->h};
+    a.fvn = {ad->acc->vn, nullptr, nullptr, o->vn};
+    a.ftr = {ad->acc->tr, nullptr, nullptr, o->tr};
+    a.ep = {EPI_LSRK, ad->rka[s], dt * ad->rkb[s], 0.0};
+    launch_tendency(md->mesh->view, pv, ad->taux[s], a, st, &md->fork);
+  }
+  ++ad->taped_steps;
+  cudaError_t err = cudaGetLastError();
+  return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_adjoint: taped step");
+}
+
 // Taped RK4 step from X0 (the caller copies the step's start state there):
 // X1..X3 the stage inputs, and (when `out` is given) the step's result.
 int tape_step(swg_adjoint ad, double dt, swg_state out, cudaStream_t st) {
+  if (ad->kind != SWG_STEPPER_RK4)
+    return tape_step_lsrk(ad, dt, out, st);
   swg_model md = ad->model;
   const ModelView &pv = md->view;
   static const double rka[3] = {1. / 2, 1. / 2, 1};
@@ -836,18 +881,28 @@ int tape_step(swg_adjoint ad, double dt, swg_state out, cudaStream_t st) {
 // lam <- adjoint of the taped step applied to lam.  The output passes of
 // stage s accumulate lamX_s into lacc and form mu_{s-1} directly
 // (ping-pong mu buffers: the passes of stage s still read mu_s).
+//
+// Low-storage RK (ns stages): with lamX_s the adjoint of the stage input X_s
+// and mu_s that of T_s, mu_{ns-1} = dt b_{ns-1} lam,
+// lamX_s = lamX_{s+1} + J(X_s)^T mu_s and
+// mu_{s-1} = dt b_{s-1} lamX_s + a_s mu_s; the step's adjoint is lamX_0.
+// The output passes accumulate lamX in lacc and form mu_{s-1} from it.
 int adjoint_step(swg_adjoint ad, double dt, cudaStream_t st) {
-  static const double rka[3] = {1. / 2, 1. / 2, 1};
-  static const double rkb[4] = {1. / 6, 1. / 3, 1. / 3, 1. / 6};
+  static const double rk4a[3] = {1. / 2, 1. / 2, 1};
+  static const double rk4b[4] = {1. / 6, 1. / 3, 1. / 3, 1. / 6};
+  const bool lsrk = ad->kind != SWG_STEPPER_RK4;
+  const int ns = ad->ns;
+  const double *rka = lsrk ? ad->rka.data() : rk4a;
+  const double *rkb = lsrk ? ad->rkb.data() : rk4b;
   const long long n = (long long)words(ad->model);
   cudaError_t err = cudaMemcpyAsync(ad->lacc->h, ad->lam->h, n * 8,
                                     cudaMemcpyDeviceToDevice, st);
   if (err != cudaSuccess)
     return cuda_fail(err, "swg_adjoint: copy");
-  lincomb(ad->mu, ad->lam, nullptr, dt * rkb[3], 0.0, n, st);
+  lincomb(ad->mu, ad->lam, nullptr, dt * rkb[ns - 1], 0.0, n, st);
   swg_state mus[2] = {ad->mu, ad->mu2};
-  for (int s = 3; s >= 0; --s) {
-    swg_state mu = mus[(3 - s) % 2], nmu = mus[(4 - s) % 2];
+  for (int s = ns - 1; s >= 0; --s) {
+    swg_state mu = mus[(ns - 1 - s) % 2], nmu = mus[(ns - s) % 2];
     AdjIO io{};
     stage_ptrs(ad, s, &io.h, &io.vn, &io.tr);
     io.mh_ = mu->h;
@@ -864,7 +919,9 @@ int adjoint_step(swg_adjoint ad, double dt, cudaStream_t st) {
       io.lam_vn = ad->lam->vn;
       io.lam_tr = ad->lam->tr;
       io.alpha = dt * rkb[s - 1];
-      io.beta = dt * rka[s - 1];
+      io.beta = lsrk ? 0.0 : dt * rka[s - 1];
+      io.gamma = lsrk ? rka[s] : 0.0;
+      io.lsrk = lsrk;
     }
     adj_passes(ad, ad->taux[s], io, st);
   }
@@ -1036,15 +1093,27 @@ extern "C" int swg_adjoint_destroy(swg_adjoint ad);
 
 extern "C" int swg_adjoint_create(swg_model md, int nsnapshots,
                                   swg_adjoint *out) {
+  return swg_adjoint_create_stepper(md, nsnapshots, SWG_STEPPER_RK4, 4, out);
+}
+
+extern "C" int swg_adjoint_create_stepper(swg_model md, int nsnapshots,
+                                          int kind, int nstages,
+                                          swg_adjoint *out) {
   if (!out || nsnapshots < 1)
     return fail(SWG_ERR_ARG, "swg_adjoint_create: bad argument");
   *out = nullptr;
+  if (!(kind == SWG_STEPPER_RK4 ||
+        (kind == SWG_STEPPER_LSRK && (nstages == 5 || nstages == 1))))
+    return fail(SWG_ERR_ARG, "swg_adjoint_create: RK4, or LSRK with 5 or 1 "
+                             "stages");
   TRY(check_model(md));
   swg_adjoint ad = new (std::nothrow) swg_adjoint_s();
   if (!ad)
     return fail(SWG_ERR_OOM, "swg_adjoint_create: host allocation");
   ad->model = md;
   ad->nsnap = nsnapshots;
+  ad->kind = kind;
+  ad->ns = kind == SWG_STEPPER_RK4 ? 4 : nstages;
   const int T = md->params.ntracers;
   const size_t C = md->mesh->ncells, E = md->mesh->nedges,
                V = md->mesh->nvertices, K = md->mesh->nlayers;
@@ -1062,19 +1131,24 @@ extern "C" int swg_adjoint_create(swg_model md, int nsnapshots,
        (rc = zal(A, E * K, &w.Qmu)) ||
        (md->view.vel_del2 && (rc = zal(A, E * K, &w.gc2e)))))
     ;
-  swg_state *st[] = {&ad->cur, &ad->next, &ad->X[0], &ad->X[1], &ad->X[2],
-                     &ad->X[3], &ad->acc, &ad->lam, &ad->lacc, &ad->mu,
-                     &ad->mu2, &ad->lX};
+  swg_state *st[] = {&ad->cur, &ad->next, &ad->acc, &ad->lam, &ad->lacc,
+                     &ad->mu, &ad->mu2, &ad->lX};
   for (auto *p : st)
     if (rc == SWG_OK)
       rc = swg_state_create(md->mesh, T, p);
+  for (int s = 0; s < ad->ns && rc == SWG_OK; ++s) // stage inputs of the tape
+    rc = swg_state_create(md->mesh, T, &ad->X[s]);
   for (int s = 0; s < nsnapshots && rc == SWG_OK; ++s) {
     swg_state x = nullptr;
     rc = swg_state_create(md->mesh, T, &x);
     ad->snaps.push_back(x);
   }
   if (rc == SWG_OK)
-    rc = swg_stepper_create(md, SWG_STEPPER_RK4, 4, &ad->stepper);
+    rc = swg_stepper_create(md, kind, ad->ns, &ad->stepper);
+  if (rc == SWG_OK) { // the stepper's coefficients (lsrk.cpp:16-33)
+    ad->rka = ad->stepper->rka;
+    ad->rkb = ad->stepper->rkb;
+  }
   if (rc == SWG_OK) {
     cudaError_t e = cudaStreamCreateWithFlags(&ad->adv, cudaStreamNonBlocking);
     for (cudaEvent_t *ev : {&ad->go, &ad->ready, &ad->freed})
@@ -1085,12 +1159,12 @@ extern "C" int swg_adjoint_create(swg_model md, int nsnapshots,
   }
   const size_t n = words(md);
   if (rc == SWG_OK && ((rc = alloc_aux_like(ad, ad->daux)) ||
-                       (rc = alloc_tape(ad, 0)) || (rc = alloc_tape(ad, 1)) ||
-                       (rc = alloc_tape(ad, 2)) || (rc = alloc_tape(ad, 3)) ||
                        (rc = zal(A, n, &ad->dS)) ||
                        (rc = zal(A, n, &ad->dacc)) || (rc = zal(A, n, &ad->dP0)) ||
                        (rc = zal(A, n, &ad->dP1)) || (rc = zal(A, n, &ad->dT))))
     ;
+  for (int s = 0; s < ad->ns && rc == SWG_OK; ++s)
+    rc = alloc_tape(ad, s);
   if (rc != SWG_OK) {
     swg_adjoint_destroy(ad);
     return rc;
@@ -1111,6 +1185,7 @@ extern "C" int swg_adjoint_destroy(swg_adjoint ad) {
   if (ad->adv)
     cudaStreamDestroy(ad->adv);
   swg_state st[] = {ad->cur, ad->next, ad->X[0], ad->X[1], ad->X[2], ad->X[3],
+                    ad->X[4],
                     ad->acc, ad->lam, ad->lacc, ad->mu, ad->mu2, ad->lX};
   for (auto s : st)
     swg_state_destroy(s);
@@ -1193,6 +1268,27 @@ extern "C" int swg_tlm_apply(swg_adjoint ad, swg_state x0, swg_state dx,
   static const double rkb[4] = {1. / 6, 1. / 3, 1. / 3, 1. / 6};
   Dual *S = ad->dS, *A = ad->dacc, *P[2] = {ad->dP0, ad->dP1};
   auto fio = [&](Dual *base, size_t off) { return base ? base + off : nullptr; };
+  if (ad->kind != SWG_STEPPER_RK4) {
+    // low-storage RK on dual numbers, in place like the stepper
+    // (lsrk.cpp:36-89): tend = a_s tend + F, state += dt b_s tend
+    cudaError_t e = cudaMemsetAsync(ad->dT, 0, sizeof(Dual) * n, st);
+    if (e != cudaSuccess)
+      return cuda_fail(e, "swg_tlm_apply: tendency reset");
+    Dual *Tn = ad->dT;
+    for (int step = 0; step < nsteps; ++step)
+      for (int s = 0; s < ad->ns; ++s) {
+        StageArgsT<Dual> a{};
+        a.h = S;
+        a.vn = S + CKn;
+        a.tr = S + CKn + EKn;
+        a.fh = {Tn, nullptr, nullptr, S};
+        a.fvn = {Tn + CKn, nullptr, nullptr, S + CKn};
+        a.ftr = {Tn + CKn + EKn, nullptr, nullptr, S + CKn + EKn};
+        a.ep = {EPI_LSRK, ad->rka[s], dt * ad->rkb[s], 0.0};
+        launch_tendency_dual(md->mesh->view, pv, ad->daux, a, st);
+      }
+    nsteps = 0;
+  }
   for (int step = 0; step < nsteps; ++step) {
     Dual *in = S;
     for (int s = 0; s < 4; ++s) {

@@ -511,9 +511,12 @@ struct EnsembleStepper {
 //   lambda now holds dL/dx0.
 struct CheckpointedAdjoint {
   swg_adjoint m_handle = nullptr;
-  explicit CheckpointedAdjoint(ShallowWaterModel &model, Int nsnapshots = 32) {
+  // kind: SWG_STEPPER_RK4, or SWG_STEPPER_LSRK with nstages 5 or 1
+  explicit CheckpointedAdjoint(ShallowWaterModel &model, Int nsnapshots = 32,
+                               int kind = SWG_STEPPER_RK4, Int nstages = 4) {
     model.resolve_hook();
-    swg_check(swg_adjoint_create(model.m_handle, nsnapshots, &m_handle));
+    swg_check(swg_adjoint_create_stepper(model.m_handle, nsnapshots, kind,
+                                         nstages, &m_handle));
   }
   CheckpointedAdjoint(const CheckpointedAdjoint &) = delete;
   CheckpointedAdjoint &operator=(const CheckpointedAdjoint &) = delete;

@@ -450,14 +450,18 @@ class Batch:
 
 
 class Adjoint:
-    """Tangent-linear and adjoint models of the RK4 step with binomial
+    """Tangent-linear and adjoint models of the RK4 step, or of the
+    low-storage RK step (stepper="lsrk", nstages 5 or 1), with binomial
     checkpointing (swg_adjoint_* / swg_tlm_* / swg_adj_* in swgpu.h)."""
 
-    def __init__(self, model: ShallowWaterModel, nsnapshots: int = 32):
+    def __init__(self, model: ShallowWaterModel, nsnapshots: int = 32,
+                 stepper: str = "rk4", nstages: int = 4):
         self.model = model
         h = C.c_void_p()
-        check(lib().swg_adjoint_create(model.handle, int(nsnapshots),
-                                       C.byref(h)))
+        kind = 0 if stepper == "rk4" else 1
+        check(lib().swg_adjoint_create_stepper(model.handle, int(nsnapshots),
+                                               kind, int(nstages),
+                                               C.byref(h)))
         self._h = h
 
     @property
