@@ -243,6 +243,9 @@ int swg_step(swg_stepper stepper, swg_state state, double t0, double dt,
  * of every member.  One RK stage of all members is one persistent
  * cooperative kernel (six passes separated by bounded grid barriers), or one
  * launch per pass, whichever launch configuration is selected. */
+/* The batch keeps the member handles (and a CUDA graph of their device
+ * arrays): the models and states must outlive it, and no model or state may
+ * appear in two members (SWG_ERR_ARG). */
 int swg_batch_create(int nmembers, const swg_model *models,
                      const swg_state *states, int kind, int nstages,
                      swg_batch *out);

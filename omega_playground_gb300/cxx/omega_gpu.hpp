@@ -465,7 +465,8 @@ struct RK4Stepper : TimeStepper {
 
 // Many independent members (own mesh size, levels and tracers) advanced
 // together: one persistent kernel, or one launch per pass, per RK stage
-// (swg_batch_*).  Members must have distinct models and states.
+// (swg_batch_*).  Members must have distinct models and states, and those
+// must outlive the stepper (it keeps their handles).
 struct EnsembleStepper {
   swg_batch m_handle = nullptr;
   EnsembleStepper(const std::vector<ShallowWaterModel *> &models,
