@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-ensembles", action="store_true",
+                    help="leave the two ensemble summaries out of the line")
     ap.add_argument("--nx", type=int, default=0,
                     help="override nx = ny (small profiling cases)")
     ap.add_argument("--adjoint-steps", type=int, default=0,
@@ -408,6 +410,23 @@ def run_ours(args, wl):
     adjoint = None
     if rank == 0 and world == 1 and not args.no_adjoint:
         adjoint = adjoint_ratio(stream)
+    ens = adj_ens = None
+    if rank == 0 and world == 1 and not args.no_ensembles:
+        e = ensemble_line(10, 3)
+        ens = {"workload": "ensemble64", "value": e["value"], "unit": UNIT,
+               "single_instance_sequential": e["single_instance_sequential"],
+               "batch_over_single": e["batch_over_single"],
+               "launch_config": e["config"]["launch_config"],
+               "cell_levels": e["config"]["cell_levels"], "steps": 10}
+        a = adjoint_ensemble_line()
+        adj_ens = {"workload": "adjoint_ensemble32", "ratio": a["value"],
+                   "members": a["config"]["members"],
+                   "snapshots": a["config"]["snapshots"], "steps": a["steps"],
+                   "batched_forward_ms": a["batched_forward_ms"],
+                   "adjoint_forward_sweep_ms": a["adjoint_forward_sweep_ms"],
+                   "adjoint_backward_sweep_ms": a["adjoint_backward_sweep_ms"],
+                   "batched_over_sequential_speedup":
+                       a["batched_over_sequential_speedup"]}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl)
@@ -427,6 +446,7 @@ def run_ours(args, wl):
                                 / 1e9)},
             "roofline": roofline, "fp64_roofline": fp64, "kernels": kernels,
             "cpu_baseline": cpu, "e2e": e2e, "adjoint": adjoint,
+            "ensemble": ens, "adjoint_ensemble": adj_ens,
             "gpu_launches": launches,
             "clocks": clk,
         }
@@ -436,9 +456,14 @@ def run_ours(args, wl):
 
 
 def run_ensemble(args):
+    print(json.dumps(ensemble_line(args.steps, args.warmup)), flush=True)
+
+
+def ensemble_line(steps, warmup):
     """The batched ensemble: 64 members (nx from {32..192}, 16-96 levels,
-    1-4 tracers, RK4) advanced by one persistent kernel per stage, against
-    the same members advanced one at a time by the single-instance path."""
+    1-4 tracers, RK4) advanced together in the autotuned launch shape
+    (persistent kernel or one launch per pass, per RK stage), against the
+    same members advanced one at a time by the single-instance path."""
     import torch
     import omega_playground_gb300 as og
     from omega_playground_gb300.workloads import ensemble, initial_state
@@ -462,19 +487,19 @@ def run_ensemble(args):
     cfg, tune_ms = batch.autotune(dt, reps=2, stream=sh)
     for st, m in zip(states, members):
         st.upload(*m[3])
-    batch.step(0.0, dt, args.warmup, stream=sh)
+    batch.step(0.0, dt, warmup, stream=sh)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     l0 = og.kernel_launches()
     e0.record(stream)
-    batch.step(0.0, dt, args.steps, stream=sh, check_status=False)
+    batch.step(0.0, dt, steps, stream=sh, check_status=False)
     e1.record(stream)
     torch.cuda.synchronize()
     batch.check(sh)
     ms = e0.elapsed_time(e1)
     launches = og.kernel_launches() - l0
-    value = units_step * args.steps / (ms / 1e3)
+    value = units_step * steps / (ms / 1e3)
     # the same members one at a time (single-instance fused path, graph)
     single_ms = 0.0
     for (mesh, params, model, ic), st in zip(members, states):
@@ -482,15 +507,15 @@ def run_ensemble(args):
         stp.step(st, 0.0, dt, 1, stream=sh)
         torch.cuda.synchronize()
         e0.record(stream)
-        stp.step(st, 0.0, dt, args.steps, stream=sh)
+        stp.step(st, 0.0, dt, steps, stream=sh)
         e1.record(stream)
         torch.cuda.synchronize()
         single_ms += e0.elapsed_time(e1)
-    single = units_step * args.steps / (single_ms / 1e3)
+    single = units_step * steps / (single_ms / 1e3)
     big = max(range(len(wls)), key=lambda i: wls[i].ncells * wls[i].nlayers)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "steps": steps, "warmup": warmup,
+            "ms_per_step": ms / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)",
             "config": {"workload": "ensemble64", "members": len(wls),
@@ -503,12 +528,16 @@ def run_ensemble(args):
                        "stepper": "rk4", "launch_config": cfg,
                        "largest_member": wls[big].name},
             "single_instance_sequential": {"value": single,
-                                           "ms_per_step": single_ms / args.steps},
+                                           "ms_per_step": single_ms / steps},
             "batch_over_single": value / single, "gpu_launches": launches}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_adjoint_ensemble(args):
+    print(json.dumps(adjoint_ensemble_line()), flush=True)
+
+
+def adjoint_ensemble_line():
     """Batched adjoints: 32 members (nx from {32, 64, 96, 128}, 16-64 levels,
     2 tracers, RK4, 300 steps, per-cell log-normal viscosity), gradient of
     the region loss w.r.t. the initial state and the viscosity field, each
@@ -616,7 +645,7 @@ def run_adjoint_ensemble(args):
             "forward_updates_per_s": units / (fwd_ms / 1e3), "loss": loss,
             "grad_visc_norm": float(np.sqrt(sum(float(np.sum(g * g))
                                                 for g in gvisc)))}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_adjoint(args):
