@@ -57,6 +57,11 @@ SCENARIOS = {
     "rk4_10_steps": dict(nx=16, ny=16, dc=1e4, K=4, T=1, stepper="rk4",
                          nsteps=10, dt=20.19, f0=1e-4, grav=9.81,
                          visc_del2=1e3, seed=16),
+    # every term on, 5-stage LSRK, 1000 steps (long-run agreement)
+    "lsrk5_1000_steps": dict(nx=12, ny=10, dc=1e4, K=3, T=2, stepper="lsrk5",
+                             nsteps=1000, dt=20.0, f0=1e-4, grav=9.81,
+                             visc_del2=1e3, visc_del4=1e9, eddy_diff2=1e3,
+                             eddy_diff4=1e9, seed=17),
 }
 
 
@@ -99,12 +104,19 @@ def run_scenario(name: str, sc: dict, workdir: str) -> dict:
 
 
 def main() -> None:
+    """Regenerates every fixture and reference_tests.txt, or only the
+    scenarios named on the command line."""
+    only = sys.argv[1:]
     pyoracle.build(with_reference=True)
     with tempfile.TemporaryDirectory() as wd:
         for name, sc in SCENARIOS.items():
+            if only and name not in only:
+                continue
             rec = run_scenario(name, sc, wd)
             np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
             print(f"{name}: {len(rec)} arrays")
+    if only:
+        return
     lines = []
     for t in ("operator_convergence", "nonlinear_swe_convergence",
               "double_vortex", "tracer_advection_convergence",

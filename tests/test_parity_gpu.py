@@ -3,6 +3,7 @@
 Bounds (normwise relative, max|gpu - ref| / max|ref|, written per test):
   tendencies and auxiliary fields of one evaluation   <= 1e-12
   state after N steps (N <= 10)                       <= 1e-12
+  state after 1000 steps (lsrk5_1000_steps fixture)   <= 1e-10
 The kernels regroup the reference's FP64 sums (hoisted coefficients, fused
 multiply-adds, Newton reciprocals), so agreement is to round-off, not bit
 for bit."""
@@ -100,9 +101,11 @@ def test_golden_steps(name, use_graph):
     stepper = make_stepper(model, cfg["stepper"])
     stepper.step(state, cfg["t0"], cfg["dt"], cfg["nsteps"], use_graph=use_graph)
     h, vn, tr = state.download()
-    assert rel_diff(h, g["h_final"]) <= TOL
-    assert rel_diff(vn, g["vn_final"]) <= TOL
-    assert rel_diff(tr, g["tr_final"]) <= TOL
+    # round-off accumulates: 1e-12 up to 10 steps, 1e-10 for the 1000-step run
+    tol = TOL if cfg["nsteps"] <= 10 else 1e-10
+    assert rel_diff(h, g["h_final"]) <= tol
+    assert rel_diff(vn, g["vn_final"]) <= tol
+    assert rel_diff(tr, g["tr_final"]) <= tol
     assert abs(og.mass_integral(state, model) - g["mass1"][0]) <= \
         1e-13 * abs(g["mass1"][0])
 
