@@ -175,6 +175,29 @@ int swg_model_create_ex(swg_mesh mesh, const swg_params *params,
 int swg_linear_model_create(swg_mesh mesh, const swg_params *params, double h0,
                             swg_model *out);
 
+/* The model's tendency terms, in the order of the reference's members
+ * (shallow_water_model.hpp:19-29). */
+#define SWG_TERM_THICKNESS_HADV 0   /* ThicknessHorzAdvOnCell          */
+#define SWG_TERM_PV_FLUX 1          /* PotentialVortFluxOnEdge         */
+#define SWG_TERM_KE_GRAD 2          /* KineticEnergyGradOnEdge         */
+#define SWG_TERM_SSH_GRAD 3         /* SSHGradOnEdge                   */
+#define SWG_TERM_VEL_DIFF 4         /* VelocityDiffusionOnEdge         */
+#define SWG_TERM_VEL_HYPERDIFF 5    /* VelocityHyperDiffusionOnEdge    */
+#define SWG_TERM_TRACER_HADV 6      /* TracerHorzAdvOnCell             */
+#define SWG_TERM_TRACER_DIFF 7      /* TracerDiffusionOnCell           */
+#define SWG_TERM_TRACER_HYPERDIFF 8 /* TracerHyperDiffusionOnCell      */
+#define SWG_NTERMS 9
+/* replaces setting / reading a term member's m_enabled (read at compute
+ * time by shallow_water_model.cpp:43-311: replace zeroes the tendency, then
+ * each enabled term adds to it).  Switching a term off always works;
+ * switching on a dissipation term whose coefficient was 0 at create time is
+ * SWG_ERR_ARG (it adds nothing and its intermediates were not allocated).
+ * A switch applies to later evaluations and steps (steppers recapture their
+ * graph); batches and adjoints copy the terms when created, and the
+ * adjoint refuses a model whose terms differ from create's. */
+int swg_model_set_term_enabled(swg_model model, int term, int enabled);
+int swg_model_term_enabled(swg_model model, int term, int *enabled);
+
 /* replaces the virtual ShallowWaterModel::additional_tendency hook
  * (shallow_water_model.hpp:42-44).  Called on the host after the built-in
  * terms of every tendency evaluation with device pointers and the stream the

@@ -103,6 +103,8 @@ _SIGS = {
     "swg_state_copy": (C.c_int, [_vp, _vp, _vp]),
     "swg_state_fill": (C.c_int, [_vp, C.c_double, _vp]),
     "swg_model_create": (C.c_int, [_vp, C.POINTER(Params), C.POINTER(_vp)]),
+    "swg_model_set_term_enabled": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "swg_model_term_enabled": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
     "swg_model_create_ex": (C.c_int, [_vp, C.POINTER(Params),
                                       C.POINTER(ModelOptions),
                                       C.POINTER(_vp)]),

@@ -1081,6 +1081,9 @@ int check_model(swg_model md) {
   if (md->view.linear || md->view.drag)
     return fail(SWG_ERR_ARG, "swg_adjoint: the linear model and the bottom "
                              "drag are not differentiated");
+  if (md->terms_switched)
+    return fail(SWG_ERR_ARG, "swg_adjoint: models with switched tendency "
+                             "terms are not differentiated");
   if (md->mesh->view.dv4_differs)
     return fail(SWG_ERR_ARG, "swg_adjoint: meshes with dv < dc/4 are not "
                              "supported");
@@ -1321,6 +1324,9 @@ int fwd_begin(swg_adjoint ad, swg_state state0, double t0, double dt,
   if (nsteps > kMaxAdjointSteps)
     return fail(SWG_ERR_ARG, "swg_adj_forward: more steps than the schedule "
                              "planner takes (10000); split the trajectory");
+  if (ad->model->terms_switched)
+    return fail(SWG_ERR_STATE, "swg_adj_forward: a tendency term of the model "
+                               "was switched after the adjoint was created");
   Planner pl(nsteps, ad->nsnap - 1);
   if (pl.C(nsteps, ad->nsnap - 1) > kMaxReadvance * (long long)nsteps)
     return fail(SWG_ERR_BUDGET, "swg_adj_forward: too few snapshots: the "

@@ -552,6 +552,79 @@ extern "C" int swg_model_destroy(swg_model md) {
   return SWG_OK;
 }
 
+// The reference's per-term m_enabled switches (shallow_water_model.hpp:19-29,
+// read by compute_*_tendency in shallow_water_model.cpp:43-311).
+static int *term_flag(swg_model md, int term, bool *off) {
+  ModelView &p = md->view;
+  *off = true;
+  switch (term) {
+  case SWG_TERM_THICKNESS_HADV: return &p.off_hadv;
+  case SWG_TERM_PV_FLUX: return &p.off_pv;
+  case SWG_TERM_KE_GRAD: return &p.off_ke;
+  case SWG_TERM_SSH_GRAD: return &p.off_ssh;
+  case SWG_TERM_TRACER_HADV: return &p.off_tr_hadv;
+  default: break;
+  }
+  *off = false; // the dissipation terms: their enable flags
+  switch (term) {
+  case SWG_TERM_VEL_DIFF: return &p.vel_del2;
+  case SWG_TERM_VEL_HYPERDIFF: return &p.vel_del4;
+  case SWG_TERM_TRACER_DIFF: return &p.tr_del2;
+  case SWG_TERM_TRACER_HYPERDIFF: return &p.tr_del4;
+  default: return nullptr;
+  }
+}
+
+// what swg_model_create enabled (shallow_water_model.cpp:17-35)
+static bool created_on(swg_model md, int term) {
+  const swg_params &q = md->params;
+  switch (term) {
+  case SWG_TERM_VEL_DIFF: return q.visc_del2 > 0;
+  case SWG_TERM_VEL_HYPERDIFF: return q.visc_del4 > 0;
+  case SWG_TERM_TRACER_DIFF: return q.eddy_diff2 > 0;
+  case SWG_TERM_TRACER_HYPERDIFF: return q.eddy_diff4 > 0;
+  default: return true;
+  }
+}
+
+extern "C" int swg_model_set_term_enabled(swg_model md, int term,
+                                          int enabled) {
+  if (!md)
+    return fail(SWG_ERR_ARG, "swg_model_set_term_enabled: NULL model");
+  if (md->view.linear)
+    return fail(SWG_ERR_ARG, "swg_model_set_term_enabled: the linear model "
+                             "has no switchable terms");
+  bool off;
+  int *f = term_flag(md, term, &off);
+  if (!f)
+    return fail(SWG_ERR_ARG, "swg_model_set_term_enabled: unknown term");
+  if (enabled && !created_on(md, term))
+    return fail(SWG_ERR_ARG, "swg_model_set_term_enabled: a dissipation term "
+                             "whose coefficient is 0 has nothing to add");
+  const int v = off ? !enabled : (enabled != 0);
+  if (*f != v) {
+    *f = v;
+    ++md->version;
+  }
+  bool changed = false;
+  for (int t = 0; t < SWG_NTERMS; ++t) {
+    bool o;
+    const int *g = term_flag(md, t, &o);
+    changed |= (o ? *g != 0 : (*g != 0) != created_on(md, t));
+  }
+  md->terms_switched = changed;
+  return SWG_OK;
+}
+
+extern "C" int swg_model_term_enabled(swg_model md, int term, int *enabled) {
+  bool off;
+  int *f = md ? term_flag(md, term, &off) : nullptr;
+  if (!f || !enabled)
+    return fail(SWG_ERR_ARG, "swg_model_term_enabled: bad argument");
+  *enabled = off ? !*f : *f != 0;
+  return SWG_OK;
+}
+
 extern "C" int swg_model_set_forcing(swg_model md, swg_forcing_fn fn,
                                      void *user) {
   if (!md)
@@ -824,7 +897,8 @@ extern "C" int swg_step(swg_stepper sp, swg_state S, double t0, double dt,
       TRY(fused_step(sp, S, dt, st));
     return SWG_OK;
   }
-  if (!sp->graph || sp->graph_serial != S->serial || sp->graph_dt != dt) {
+  if (!sp->graph || sp->graph_serial != S->serial || sp->graph_dt != dt ||
+      sp->graph_version != sp->model->version) {
     if (sp->graph) {
       cudaGraphExecDestroy(sp->graph);
       sp->graph = nullptr;
@@ -857,6 +931,7 @@ extern "C" int swg_step(swg_stepper sp, swg_state S, double t0, double dt,
       return cuda_fail(err, "swg_step: graph instantiate");
     }
     sp->graph_serial = S->serial;
+    sp->graph_version = sp->model->version;
     sp->graph_dt = dt;
   }
   for (int s = 0; s < nsteps; ++s) {

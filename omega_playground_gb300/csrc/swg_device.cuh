@@ -253,30 +253,35 @@ __device__ __forceinline__ void pt_edge_final(const MeshView &m,
   const int K = m.nlayers;
   const int e = int(i / unsigned(K)), k = int(i - unsigned(e) * unsigned(K));
   // potential-vorticity flux: sum_j w_j F_j (Q_e + Q_j) / 4 with w/4 in woe
-  T S1, S2;
-  {
-    const int je = __ldg(m.eoe + NE * e);
-    const double w = __ldg(m.woe + NE * e);
-    S1 = w * a.F[size_t(je) * K + k];
-    S2 = w * a.G[size_t(je) * K + k];
-  }
+  T t{};
+  if (!p.off_pv) {
+    T S1, S2;
+    {
+      const int je = __ldg(m.eoe + NE * e);
+      const double w = __ldg(m.woe + NE * e);
+      S1 = w * a.F[size_t(je) * K + k];
+      S2 = w * a.G[size_t(je) * K + k];
+    }
 #pragma unroll
-  for (int j = 1; j < NE; ++j) {
-    const int je = __ldg(m.eoe + NE * e + j);
-    const double w = __ldg(m.woe + NE * e + j);
-    S1 = fma(w, a.F[size_t(je) * K + k], S1);
-    S2 = fma(w, a.G[size_t(je) * K + k], S2);
+    for (int j = 1; j < NE; ++j) {
+      const int je = __ldg(m.eoe + NE * e + j);
+      const double w = __ldg(m.woe + NE * e + j);
+      S1 = fma(w, a.F[size_t(je) * K + k], S1);
+      S2 = fma(w, a.G[size_t(je) * K + k], S2);
+    }
+    if (a.S1)
+      a.S1[i] = S1;
+    t = fma(a.Q[i], S1, S2);
   }
-  if (a.S1)
-    a.S1[i] = S1;
-  T t = fma(a.Q[i], S1, S2);
   const int c0 = __ldg(m.ce + 2 * e), c1 = __ldg(m.ce + 2 * e + 1);
   const double idc = __ldg(m.inv_dc + e);
   // kinetic-energy and sea-surface-height gradients (the differences are
   // taken before scaling, as in the reference, so g h ~ 1e4 never rounds)
-  t = fma(-idc, a.ke[size_t(c1) * K + k] - a.ke[size_t(c0) * K + k], t);
-  t = fma(-__ldg(p.gidc + e), s.h[size_t(c1) * K + k] - s.h[size_t(c0) * K + k],
-          t);
+  if (!p.off_ke)
+    t = fma(-idc, a.ke[size_t(c1) * K + k] - a.ke[size_t(c0) * K + k], t);
+  if (!p.off_ssh)
+    t = fma(-__ldg(p.gidc + e),
+            s.h[size_t(c1) * K + k] - s.h[size_t(c0) * K + k], t);
   if (p.drag && k == K - 1) {
     // bottom drag -c_d sqrt(ke_0 + ke_1) vn / mean_h on the lowest level
     // (the term commented out at shallow_water_hierarchical.cpp:479-486)
@@ -309,21 +314,32 @@ __device__ __forceinline__ void pt_cell_final(const MeshView &m,
   const unsigned CK = unsigned(m.ncells) * unsigned(K);
   const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * unsigned(K));
   // a_j = -F_j ccd_j / 2: half the flux divergence weight of edge j
-  T w[MAXE], Sa;
+  T w[MAXE], Sa{};
   int ej[MAXE];
 #pragma unroll
   for (int j = 0; j < MAXE; ++j) {
     ej[j] = __ldg(m.ec + 6 * c + j);
-    w[j] = __ldg(m.ccdh + 6 * c + j) * a.F[size_t(ej[j]) * K + k];
+    w[j] = T{};
   }
-  Sa = w[0] + w[1];
+  if (!p.off_hadv || !p.off_tr_hadv) {
 #pragma unroll
-  for (int j = 2; j < MAXE; ++j)
-    Sa += w[j];
-  if (p.do_h)
-    epilogue(s.ep, s.fh, i, 2.0 * Sa); // -sum_j ccd_j F_j
+    for (int j = 0; j < MAXE; ++j)
+      w[j] = __ldg(m.ccdh + 6 * c + j) * a.F[size_t(ej[j]) * K + k];
+    Sa = w[0] + w[1];
+#pragma unroll
+    for (int j = 2; j < MAXE; ++j)
+      Sa += w[j];
+  }
+  if (p.do_h) // -sum_j ccd_j F_j, or nothing with thickness advection off
+    epilogue(s.ep, s.fh, i, p.off_hadv ? T{} : 2.0 * Sa);
   if (p.ntracers == 0)
     return;
+  if (p.off_tr_hadv) { // tracer advection off: only diffusion weights
+    Sa = T{};
+#pragma unroll
+    for (int j = 0; j < MAXE; ++j)
+      w[j] = T{};
+  }
   // advection + del2: sum_j a_j (n_c + n_j) + b_j (n_j - n_c)
   T wc = Sa;
   if (p.tr_del2) {

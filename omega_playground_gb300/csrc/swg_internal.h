@@ -74,6 +74,9 @@ struct ModelView {
   // factor for the weights/4 table), and the optional bottom drag
   int linear, drag;
   double h0, f4, drag_coeff;
+  // tendency terms switched off after create (the reference's m_enabled
+  // members); zero = on, so zero-initialised views keep every term
+  int off_hadv, off_pv, off_ke, off_ssh, off_tr_hadv;
 };
 
 // Forward-mode dual number (value, tangent) of the tangent-linear model;
@@ -222,6 +225,9 @@ struct swg_model_s {
   swg_forcing_fn forcing;
   void *forcing_user;
   swg::Fork fork;
+  // bumped when a term is switched (captured step graphs hold the view)
+  unsigned long long version;
+  int terms_switched; // some term differs from what create enabled
 };
 
 struct swg_stepper_s {
@@ -231,6 +237,7 @@ struct swg_stepper_s {
   swg_state tend, acc, p0, p1, old;
   cudaGraphExec_t graph;       // one captured step (fused path)
   unsigned long long graph_serial; // the state the graph was captured for
+  unsigned long long graph_version; // and the model's term version
   double graph_dt;
   long long graph_launches;    // kernels per captured step
 };

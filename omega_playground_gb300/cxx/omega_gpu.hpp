@@ -330,10 +330,40 @@ struct ShallowWaterState {
 
 enum class AddMode { replace, increment };
 
+struct ShallowWaterModel;
+
+// A tendency-term member of the model (shallow_water_model.hpp:19-29): its
+// m_enabled reads and switches the term through the library, so
+// `model.m_pv_flux_edge.m_enabled = false;` works as in the reference.
+struct TermSwitch {
+  const ShallowWaterModel *m_model;
+  int m_term;
+  operator bool() const;
+  TermSwitch &operator=(bool on);
+  TermSwitch(const ShallowWaterModel *model, int term)
+      : m_model(model), m_term(term) {}
+  TermSwitch(const TermSwitch &) = delete;
+};
+struct TendencyTerm {
+  TermSwitch m_enabled;
+  TendencyTerm(const ShallowWaterModel *model, int term)
+      : m_enabled(model, term) {}
+};
+
 struct ShallowWaterModel {
   ShallowWaterParams m_params;
   MPASMesh *m_mesh;
   swg_model m_handle = nullptr;
+
+  TendencyTerm m_thickness_hadv_cell{this, SWG_TERM_THICKNESS_HADV};
+  TendencyTerm m_pv_flux_edge{this, SWG_TERM_PV_FLUX};
+  TendencyTerm m_ke_grad_edge{this, SWG_TERM_KE_GRAD};
+  TendencyTerm m_ssh_grad_edge{this, SWG_TERM_SSH_GRAD};
+  TendencyTerm m_vel_diff_edge{this, SWG_TERM_VEL_DIFF};
+  TendencyTerm m_vel_hyperdiff_edge{this, SWG_TERM_VEL_HYPERDIFF};
+  TendencyTerm m_tracer_hadv_cell{this, SWG_TERM_TRACER_HADV};
+  TendencyTerm m_tracer_diff_cell{this, SWG_TERM_TRACER_DIFF};
+  TendencyTerm m_tracer_hyperdiff_cell{this, SWG_TERM_TRACER_HYPERDIFF};
 
   // `options`: the linear variant or the opt-in bottom drag
   // (swg_model_options in swgpu.h); the default is the reference's model,
@@ -408,6 +438,16 @@ private:
       swg_model_set_forcing(self->m_handle, nullptr, nullptr);
   }
 };
+
+inline TermSwitch::operator bool() const {
+  int on = 0;
+  swg_check(swg_model_term_enabled(m_model->m_handle, m_term, &on));
+  return on != 0;
+}
+inline TermSwitch &TermSwitch::operator=(bool on) {
+  swg_check(swg_model_set_term_enabled(m_model->m_handle, m_term, on ? 1 : 0));
+  return *this;
+}
 
 // LinearShallowWaterModel and its parameters
 // (shallow_water_hierarchical.cpp:676-775): h_t = -h0 div(vn),

@@ -20,6 +20,7 @@ from __future__ import annotations
 import ctypes as C
 import dataclasses
 import enum
+import weakref
 
 import numpy as np
 
@@ -248,6 +249,35 @@ class ShallowWaterState:
             self._h = None
 
 
+# the reference's tendency-term members (shallow_water_model.hpp:19-29), in
+# the order of swgpu.h's SWG_TERM_* numbers
+TERMS = ("m_thickness_hadv_cell", "m_pv_flux_edge", "m_ke_grad_edge",
+         "m_ssh_grad_edge", "m_vel_diff_edge", "m_vel_hyperdiff_edge",
+         "m_tracer_hadv_cell", "m_tracer_diff_cell", "m_tracer_hyperdiff_cell")
+
+
+class TendencyTerm:
+    """One of the model's tendency terms; ``m_enabled`` reads and switches it
+    like the reference member's flag (read at compute time)."""
+
+    def __init__(self, model, term: int):
+        # weak: the model owns its terms, a strong back-reference would make
+        # a cycle and delay the model's release
+        self._model, self._term = weakref.ref(model), term
+
+    @property
+    def m_enabled(self) -> bool:
+        out = C.c_int()
+        check(lib().swg_model_term_enabled(self._model().handle, self._term,
+                                           C.byref(out)))
+        return bool(out.value)
+
+    @m_enabled.setter
+    def m_enabled(self, on: bool):
+        check(lib().swg_model_set_term_enabled(self._model().handle,
+                                               self._term, int(bool(on))))
+
+
 class ShallowWaterModel:
     """shallow_water_model.hpp:14-51.  Override ``additional_tendency`` to
     add forcing (it receives device pointers and the CUDA stream).
@@ -269,6 +299,8 @@ class ShallowWaterModel:
         check(lib().swg_model_create_ex(mesh.handle, C.byref(p), C.byref(o),
                                         C.byref(h)))
         self._h = h
+        for t, name in enumerate(TERMS):
+            setattr(self, name, TendencyTerm(self, t))
         self._cb = None
         if type(self).additional_tendency is not \
                 ShallowWaterModel.additional_tendency:

@@ -92,6 +92,8 @@ def lib():
         L.or_model_create_ex.argtypes = [C.POINTER(_Mesh), C.POINTER(_Params),
                                          C.c_int, C.c_double, C.c_int]
         L.or_model_create_ex.restype = C.c_void_p
+        L.or_model_set_term.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        L.or_model_set_term.restype = C.c_int
         L.or_model_destroy.argtypes = [C.c_void_p]
         L.or_model_aux.argtypes = [C.c_void_p, C.c_char_p,
                                    C.POINTER(C.c_size_t)]
@@ -200,6 +202,11 @@ class OracleModel:
         if not p:
             raise KeyError(name)
         return np.ctypeslib.as_array(p, shape=(n.value,)).copy()
+
+    def set_term(self, term: int, enabled: bool):
+        """A term member's m_enabled (terms numbered as SWG_TERM_*)."""
+        if lib().or_model_set_term(self._h, int(term), int(bool(enabled))):
+            raise ValueError("unknown term")
 
     def compute_tendency(self, h, vn, tr, t=0.0, add_mode=0, tend=None):
         sh, sv, st = self.shapes()

@@ -239,6 +239,8 @@ struct or_model {
   or_mesh m;
   or_params p;
   int en_vel_diff, en_vel_hyperdiff, en_tr_diff, en_tr_hyperdiff;
+  /* the always-on terms' m_enabled (shallow_water_model.cpp:17-21,29) */
+  int en_hadv, en_pv, en_ke, en_ssh, en_tr_hadv;
   /* variants from shallow_water_hierarchical.cpp: LinearShallowWaterModel
    * (h0) and the bottom drag that its nonlinear model leaves commented out */
   int linear, apply_drag;
@@ -275,6 +277,7 @@ or_model *or_model_create_ex(const or_mesh *m, const or_params *p, int linear,
   md->en_vel_hyperdiff = p->visc_del4 > 0;
   md->en_tr_diff = p->eddy_diff2 > 0;
   md->en_tr_hyperdiff = p->eddy_diff4 > 0;
+  md->en_hadv = md->en_pv = md->en_ke = md->en_ssh = md->en_tr_hadv = 1;
   const size_t K = m->nlayers, C = m->ncells, E = m->nedges, V = m->nvertices;
   const size_t T = p->ntracers;
   md->f_vertex = zalloc(V);
@@ -431,6 +434,8 @@ static void h_tendency(or_model *md, double *h_tend, const double *vn,
       const size_t i = (size_t)c * K + k;
       if (add_mode == 0)
         h_tend[i] = 0;
+      if (!md->en_hadv) /* ThicknessHorzAdvOnCell switched off */
+        continue;
       double accum = 0;
       for (int j = 0; j < m->nedges_on_cell[c]; ++j) {
         const int je = m->edges_on_cell[6 * c + j];
@@ -519,25 +524,29 @@ static void vn_tendency(or_model *md, double *vn_tend, const double *h,
       if (add_mode == 0)
         vn_tend[i] = 0;
       /* PotentialVortFluxOnEdge (pv_flux_edge.hpp:149-177) */
-      double qt = 0;
-      for (int j = 0; j < m->nedges_on_edge[e]; ++j) {
-        const int je = m->edges_on_edge[12 * e + j];
-        const size_t ij = (size_t)je * K + k;
-        const double norm_vort = (md->norm_rvort_edge[i] + md->norm_pvort_edge[i] +
-                                  md->norm_rvort_edge[ij] +
-                                  md->norm_pvort_edge[ij]) *
-                                 0.5;
-        qt += m->weights_on_edge[12 * e + j] * md->flux_h_edge[ij] * vn[ij] *
-              norm_vort;
+      if (md->en_pv) {
+        double qt = 0;
+        for (int j = 0; j < m->nedges_on_edge[e]; ++j) {
+          const int je = m->edges_on_edge[12 * e + j];
+          const size_t ij = (size_t)je * K + k;
+          const double norm_vort =
+              (md->norm_rvort_edge[i] + md->norm_pvort_edge[i] +
+               md->norm_rvort_edge[ij] + md->norm_pvort_edge[ij]) *
+              0.5;
+          qt += m->weights_on_edge[12 * e + j] * md->flux_h_edge[ij] * vn[ij] *
+                norm_vort;
+        }
+        vn_tend[i] += qt;
       }
-      vn_tend[i] += qt;
       /* KineticEnergyGradOnEdge (ke_grad_edge.hpp:223-237) */
-      vn_tend[i] -= (md->ke_cell[(size_t)c1 * K + k] -
-                     md->ke_cell[(size_t)c0 * K + k]) *
-                    inv_dc;
+      if (md->en_ke)
+        vn_tend[i] -= (md->ke_cell[(size_t)c1 * K + k] -
+                       md->ke_cell[(size_t)c0 * K + k]) *
+                      inv_dc;
       /* SSHGradOnEdge (ssh_grad_edge.hpp:281-294) */
-      vn_tend[i] -= p->grav *
-                    (h[(size_t)c1 * K + k] - h[(size_t)c0 * K + k]) * inv_dc;
+      if (md->en_ssh)
+        vn_tend[i] -= p->grav *
+                      (h[(size_t)c1 * K + k] - h[(size_t)c0 * K + k]) * inv_dc;
       /* bottom drag, opt-in: the term commented out at
        * shallow_water_hierarchical.cpp:479-486 with h_drag_edge = h_mean
        * (:258-276) on the lowest level (max_level_edge_top = nlayers) */
@@ -620,7 +629,7 @@ static void tr_tendency(or_model *md, double *tr_tend, const double *vn,
         if (add_mode == 0)
           tr_tend[i] = 0;
         /* TracerHorzAdvOnCell (tracer_hadv_cell.hpp:60-90) */
-        {
+        if (md->en_tr_hadv) {
           double accum = 0;
           for (int j = 0; j < m->nedges_on_cell[c]; ++j) {
             const int je = m->edges_on_cell[6 * c + j];
@@ -714,6 +723,18 @@ static void linear_tendency(or_model *md, double *h_tend, double *vn_tend,
           vn_tend[(size_t)e * K + k] = x;
       }
   }
+}
+
+/* Setting a term member's m_enabled (terms numbered as in
+ * shallow_water_model.hpp:19-29). */
+int or_model_set_term(or_model *md, int term, int enabled) {
+  int *f[9] = {&md->en_hadv, &md->en_pv, &md->en_ke, &md->en_ssh,
+               &md->en_vel_diff, &md->en_vel_hyperdiff, &md->en_tr_hadv,
+               &md->en_tr_diff, &md->en_tr_hyperdiff};
+  if (term < 0 || term > 8)
+    return 1;
+  *f[term] = enabled != 0;
+  return 0;
 }
 
 void or_compute_tendency(or_model *md, double *h_tend, double *vn_tend,

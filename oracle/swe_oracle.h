@@ -78,6 +78,12 @@ void or_model_destroy(or_model *md);
  * its element count.  Names follow the reference's member names. */
 double *or_model_aux(or_model *md, const char *name, size_t *n);
 
+/* Sets the m_enabled of term `term` (0 ThicknessHorzAdvOnCell, 1 PV flux,
+ * 2 KE gradient, 3 SSH gradient, 4 velocity del2, 5 velocity del4, 6 tracer
+ * advection, 7 tracer del2, 8 tracer del4: shallow_water_model.hpp:19-29).
+ * Returns 0, or 1 for an unknown term. */
+int or_model_set_term(or_model *md, int term, int enabled);
+
 /* ShallowWaterModel::compute_tendency (shallow_water_model.cpp:313-347).
  * add_mode: 0 replace, 1 increment. */
 void or_compute_tendency(or_model *md, double *h_tend, double *vn_tend,
