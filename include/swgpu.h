@@ -240,7 +240,12 @@ int swg_compute_tendency_noalloc(swg_mesh mesh, const swg_params *params,
  * "vel_div_cell", "ke_cell", "norm_tr_cell", "thick_flux_edge"
  * (mean h * vn), "mean_h_edge", "pv_edge" (sum of the two vertex q),
  * "vel_del2_edge", "vel_del2_rvort_vertex", "vel_del2_div_cell",
- * "tracer_del2_cell".  Fields a configuration does not need stay unwritten. */
+ * "tracer_del2_cell".  Fields a configuration does not need stay unwritten.
+ * "f_vertex" [V] is the model's Coriolis parameter per vertex, the
+ * reference's m_f_vertex (shallow_water_model.hpp:32, filled with f0 by
+ * shallow_water_model.cpp:39): the caller may write it (through a cast, e.g.
+ * a beta plane) and every later evaluation reads it; the linear model uses
+ * f0 instead. */
 int swg_model_aux(swg_model model, const char *name, const double **ptr,
                   long long *count);
 

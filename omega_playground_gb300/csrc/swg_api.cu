@@ -659,6 +659,8 @@ extern "C" int swg_model_aux(swg_model md, const char *name,
       {"vel_del2_rvort_vertex", a.z4, V * K},
       {"vel_del2_div_cell", a.d4, C * K},
       {"tracer_del2_cell", a.lap, T * C * K},
+      // the model's m_f_vertex (writable; read by every later evaluation)
+      {"f_vertex", md->view.f_vertex, V},
   };
   for (auto &t : tab)
     if (std::strcmp(t.n, name) == 0) {

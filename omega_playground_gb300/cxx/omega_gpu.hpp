@@ -364,6 +364,9 @@ struct ShallowWaterModel {
   TendencyTerm m_tracer_hadv_cell{this, SWG_TERM_TRACER_HADV};
   TendencyTerm m_tracer_diff_cell{this, SWG_TERM_TRACER_DIFF};
   TendencyTerm m_tracer_hyperdiff_cell{this, SWG_TERM_TRACER_HYPERDIFF};
+  // Coriolis parameter per vertex (shallow_water_model.hpp:32), f0 after
+  // construction; a user kernel may write it, later evaluations read it
+  Real1d m_f_vertex;
 
   // `options`: the linear variant or the opt-in bottom drag
   // (swg_model_options in swgpu.h); the default is the reference's model,
@@ -377,6 +380,11 @@ struct ShallowWaterModel {
                  params.m_disable_h_tendency ? 1 : 0,
                  params.m_disable_vn_tendency ? 1 : 0};
     swg_check(swg_model_create_ex(mesh->m_handle, &p, &options, &m_handle));
+    const double *fv = nullptr;
+    long long nfv = 0;
+    swg_check(swg_model_aux(m_handle, "f_vertex", &fv, &nfv));
+    m_f_vertex.m_data = const_cast<double *>(fv);
+    m_f_vertex.m_ext[0] = size_t(nfv);
     // The hook stays registered until the base no-op runs once; then the
     // steppers switch to the fused kernels (models that override
     // additional_tendency keep the unfused, hooked sequence).

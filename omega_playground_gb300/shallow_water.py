@@ -340,6 +340,28 @@ class ShallowWaterModel:
             raise _capi.SwgError(3, f"cudaMemcpy failed ({err})")
         return out
 
+    @property
+    def m_f_vertex(self) -> np.ndarray:
+        """Copy of the Coriolis parameter per vertex (the reference's
+        m_f_vertex, f0 after construction)."""
+        return self.aux("f_vertex")
+
+    @m_f_vertex.setter
+    def m_f_vertex(self, f):
+        """Writes the Coriolis parameter per vertex (e.g. a beta plane);
+        every later evaluation reads it."""
+        p, n = _dp(), C.c_longlong()
+        check(lib().swg_model_aux(self._h, b"f_vertex", C.byref(p),
+                                  C.byref(n)))
+        f = np.ascontiguousarray(f, np.float64)
+        if f.size != n.value:
+            raise ValueError(f"f_vertex needs {n.value} values")
+        err = _cudart().cudaMemcpy(C.cast(p, C.c_void_p),
+                                   f.ctypes.data_as(C.c_void_p),
+                                   C.c_size_t(8 * n.value), C.c_int(1))
+        if err:
+            raise _capi.SwgError(3, f"cudaMemcpy failed ({err})")
+
     def __del__(self):
         if getattr(self, "_h", None) and _capi._lib is not None:
             _capi._lib.swg_model_destroy(self._h)

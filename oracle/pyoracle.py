@@ -203,6 +203,12 @@ class OracleModel:
             raise KeyError(name)
         return np.ctypeslib.as_array(p, shape=(n.value,)).copy()
 
+    def set_f_vertex(self, f):
+        """Writes the Coriolis parameter per vertex (m_f_vertex)."""
+        n = C.c_size_t()
+        p = lib().or_model_aux(self._h, b"f_vertex", C.byref(n))
+        np.ctypeslib.as_array(p, shape=(n.value,))[:] = f
+
     def set_term(self, term: int, enabled: bool):
         """A term member's m_enabled (terms numbered as SWG_TERM_*)."""
         if lib().or_model_set_term(self._h, int(term), int(bool(enabled))):

@@ -338,6 +338,7 @@ double *or_model_aux(or_model *md, const char *name, size_t *n) {
       {"vel_del2_rvort_vertex", md->vel_del2_rvort_vertex, V * K},
       {"vel_del2_div_cell", md->vel_del2_div_cell, C * K},
       {"tracer_del2_cell", md->tracer_del2_cell, T * C * K},
+      {"f_vertex", md->f_vertex, V},
   };
   for (size_t i = 0; i < sizeof(tab) / sizeof(tab[0]); ++i)
     if (strcmp(tab[i].name, name) == 0) {

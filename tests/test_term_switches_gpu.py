@@ -132,3 +132,31 @@ def test_enabling_a_zero_coefficient_term_and_differentiating_are_errors():
         og.Adjoint(model, 4)
     model.m_ke_grad_edge.m_enabled = True          # back to create's set
     og.Adjoint(model, 4)
+
+
+def test_beta_plane_f_vertex_matches_oracle():
+    """The model's m_f_vertex (f0 after construction) written with a beta
+    plane f = f0 + beta (y - Ly/2) on both sides: tendencies and three RK4
+    steps (graph path) <= 1e-12, and the field reads back."""
+    mesh, params, model, omd = setup()
+    np.testing.assert_array_equal(model.m_f_vertex, COEF["f0"])
+    om = omd.mesh
+    f = COEF["f0"] + 1.6e-11 * (om.y_vertex - 0.5 * om.period_y)
+    model.m_f_vertex = f
+    omd.set_f_vertex(f)
+    np.testing.assert_array_equal(model.m_f_vertex, f)
+    x, base = state(mesh, 21), state(mesh, 22)
+    want = omd.compute_tendency(*x, tend=tuple(a.copy() for a in base))
+    got = gpu_tendency(model, mesh, params, x, base, 0)
+    for g, w in zip(got, want):
+        assert rel_diff(g, w) <= TOL
+    flat = gpu_tendency(og.ShallowWaterModel(mesh, params), mesh, params, x,
+                        base, 0)
+    assert np.any(got[1] != flat[1])              # vn feels the beta plane
+    S = og.ShallowWaterState(mesh, params)
+    S.upload(*x)
+    og.RK4Stepper(model).step(S, 0.0, 20.0, 3)
+    want = omd.step(*(a.copy() for a in x), 0.0, 20.0, 3, kind="rk4",
+                    nstages=4)
+    for g, w in zip(S.download(), want):
+        assert rel_diff(g, w) <= TOL
