@@ -188,6 +188,18 @@ class ShallowWaterParams:
                             int(self.m_disable_vn_tendency))
 
 
+class _DeviceArray:
+    """A dense float64 device array in the CUDA array interface (version 3)
+    with a reference to the object that owns the memory."""
+
+    def __init__(self, owner, ptr, shape):
+        self.owner = owner
+        self.__cuda_array_interface__ = {
+            "shape": tuple(int(n) for n in shape), "typestr": "<f8",
+            "data": (int(ptr), False), "strides": None, "version": 3,
+            "stream": None}
+
+
 class ShallowWaterState:
     """h_cell [C][K], vn_edge [E][K], tr_cell [T][C][K] on the GPU
     (shallow_water_state.cpp:7-14)."""
@@ -236,6 +248,23 @@ class ShallowWaterState:
         p = [_dp(), _dp(), _dp()]
         check(lib().swg_state_device_ptrs(self._h, *[C.byref(x) for x in p]))
         return tuple(C.cast(x, C.c_void_p).value for x in p)
+
+    def as_tensors(self):
+        """Zero-copy torch views (h [C][K], vn [E][K], tr [T][C][K]) of the
+        state's device memory, float64 on the state's GPU, valid while
+        this state is alive.  The views carry no stream: order torch work
+        against the state's own calls by running both on the same
+        stream."""
+        import torch
+        out = []
+        for ptr, shape in zip(self.device_ptrs(), self.shapes()):
+            if int(np.prod(shape)) == 0:
+                out.append(torch.empty(shape, dtype=torch.float64,
+                                       device="cuda"))
+            else:
+                out.append(torch.as_tensor(_DeviceArray(self, ptr, shape),
+                                           device="cuda"))
+        return tuple(out)
 
     def copy_from(self, other: "ShallowWaterState", stream=None):
         check(lib().swg_state_copy(self._h, other._h, _s(stream)))
