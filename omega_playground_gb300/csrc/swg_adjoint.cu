@@ -532,10 +532,27 @@ size_t words(swg_model md) {
          md->mesh->nlayers;
 }
 
-int slot_of(const std::vector<int> &list, int base, int n, int x) {
+// The o-th slot j < n of list[base...] holding x (o = 0: the first), or -1.
+int slot_of(const std::vector<int> &list, int base, int n, int x, int o = 0) {
   for (int j = 0; j < n; ++j)
-    if (list[base + j] == x)
+    if (list[base + j] == x && o-- == 0)
       return j;
+  return -1;
+}
+
+// How many of the slots before j hold the same entry as slot j.
+int occurrence(const std::vector<int> &list, int base, int j) {
+  int o = 0;
+  for (int i = 0; i < j; ++i)
+    o += list[base + i] == list[base + j];
+  return o;
+}
+
+// The o-th side s of edge e with pair[2e+s] == x, or -1.
+int side_of(const std::vector<int> &pair, int e, int x, int o) {
+  for (int s = 0; s < 2; ++s)
+    if (pair[2 * e + s] == x && o-- == 0)
+      return s;
   return -1;
 }
 
@@ -563,15 +580,23 @@ int build_tables(swg_adjoint ad) {
         hm_c[6 * c + j] = 0.5;
       if (me->ccd_h[6 * c + j] == 0.0 && me->ckq_h[6 * c + j] == 0.0)
         continue; // padding slot
+      // On a mesh one cell wide an edge can have the same cell on both
+      // sides; it then fills two slots of that cell, and the o-th of them
+      // stands for the o-th side, so each (edge, side) pair is transposed
+      // once.  Padding slots (zero coefficients) repeat the first edge and
+      // are not counted; real slots come first.
       const int e = me->ec_h[6 * c + j], n = me->nbc_h[6 * c + j];
-      const int jn = slot_of(me->ec_h, 6 * n, MAXE, e);
-      if (jn < 0)
+      const int nreal = me->nec_h[c];
+      const int o = occurrence(me->ec_h, 6 * c, j);
+      const int side = side_of(me->ce_h, e, c, o);
+      const int jn = slot_of(me->ec_h, 6 * n, me->nec_h[n], e, n == c ? o : 0);
+      if (j >= nreal || jn < 0 || side < 0)
         return fail(SWG_ERR_ARG, "swg_adjoint: edge missing from its neighbour");
       ccdh_nb[6 * c + j] = me->ccdh_h[6 * n + jn];
       ckq_nb[6 * c + j] = me->ckq_h[6 * n + jn];
       kd2_nb[6 * c + j] = kd2(n, jn);
       r4_nb[6 * c + j] = r4(n, jn);
-      const double sg = me->ce_h[2 * e] == c ? 1.0 : -1.0;
+      const double sg = side == 0 ? 1.0 : -1.0;
       keadj[6 * c + j] = sg * me->inv_dc_h[e];
       hsadj[6 * c + j] = sg * (P.grav * me->inv_dc_h[e]);
       d4adj[6 * c + j] = -(sg * (-(P.visc_del4 * me->scale4_h[e])) * me->inv_dc_h[e]);
@@ -593,9 +618,11 @@ int build_tables(swg_adjoint ad) {
   for (int e = 0; e < E; ++e)
     for (int s = 0; s < 2; ++s) {
       const int c = me->ce_h[2 * e + s];
-      const int j = slot_of(me->ec_h, 6 * c, MAXE, e);
+      const int j = slot_of(me->ec_h, 6 * c, me->nec_h[c], e,
+                            s == 1 && me->ce_h[2 * e] == c);
       const int v = me->ve_h[2 * e + s];
-      const int jv = slot_of(me->ev_h, 3 * v, 3, e);
+      const int jv = slot_of(me->ev_h, 3 * v, 3, e,
+                             s == 1 && me->ve_h[2 * e] == v);
       if (j < 0 || jv < 0)
         return fail(SWG_ERR_ARG, "swg_adjoint: inconsistent edge tables");
       ccd_e2[2 * e + s] = me->ccd_h[6 * c + j];
@@ -610,7 +637,10 @@ int build_tables(swg_adjoint ad) {
   for (int v = 0; v < V; ++v)
     for (int j = 0; j < 3; ++j) {
       const int e = me->ev_h[3 * v + j];
-      const double sg = me->ve_h[2 * e] == v ? -1.0 : 1.0;
+      const int side = side_of(me->ve_h, e, v, occurrence(me->ev_h, 3 * v, j));
+      if (side < 0)
+        return fail(SWG_ERR_ARG, "swg_adjoint: inconsistent vertex tables");
+      const double sg = side == 0 ? -1.0 : 1.0;
       z4adj[3 * v + j] = -(sg * (-(P.visc_del4 * me->scale4_h[e])) * me->inv_dv_h[e]);
       zetaadj[3 * v + j] = -(sg * me->inv_dv_h[e]);
     }

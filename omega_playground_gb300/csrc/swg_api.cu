@@ -245,6 +245,7 @@ extern "C" int swg_mesh_create(const swg_mesh_desc *d, swg_mesh *out) {
     m->scale4_h.assign(d->mesh_scaling_del4, d->mesh_scaling_del4 + E);
   m->ckq_h = ckq;
   m->ec_h = ec;
+  m->nec_h.assign(d->nedges_on_cell, d->nedges_on_cell + C);
   m->inv_dc_h = inv_dc;
   m->ev_h.assign(d->edges_on_vertex, d->edges_on_vertex + 3 * V);
   m->cv_h.assign(d->cells_on_vertex, d->cells_on_vertex + 3 * V);

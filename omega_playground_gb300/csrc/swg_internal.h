@@ -199,7 +199,7 @@ struct swg_mesh_s {
   std::vector<void *> allocs;
   // host copies of the per-edge scaling (the model scales them)
   std::vector<double> scale2_h, scale4_h, ckq_h, inv_dc_h;
-  std::vector<int> ec_h;
+  std::vector<int> ec_h, nec_h; // edges_on_cell (padded), nedges_on_cell
   // host copies of the derived tables (the adjoint builds transposes)
   std::vector<int> ev_h, cv_h, nbc_h, ce_h, ve_h, eoe_h;
   std::vector<double> cvr_h, kvh_h, ccd_h, cke_h, ccdh_h, inv_dv_h, woe_h;

@@ -54,8 +54,8 @@ struct HexGrid {
 
 int build_planar_hex(int nx, int ny, double dc, swg_hex_tables *t,
                      double *period_x, double *period_y) {
-  if (nx < 2 || ny < 2)
-    return fail(SWG_ERR_ARG, "planar hex mesh needs nx >= 2 and ny >= 2");
+  if (nx < 1 || ny < 1)
+    return fail(SWG_ERR_ARG, "planar hex mesh needs nx >= 1 and ny >= 1");
   if ((long long)nx * ny * 3 > 0x7fffffffLL)
     return fail(SWG_ERR_ARG, "planar hex mesh too large for int32 indices");
   const HexGrid g{nx, ny};

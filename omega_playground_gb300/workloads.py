@@ -258,7 +258,9 @@ def initial_state(mesh, wl: Workload):
                 ph = 2 * math.pi * r[4 * m + 3]
                 c += amp * np.sin(2 * math.pi * (kx * xc / Lx + ky * yc / Ly)
                                   + ph)
-            base[l] = (c - c.min()) / (c.max() - c.min())
+            span = c.max() - c.min()
+            # a one-cell mesh has no spread to rescale: uniform 1/2
+            base[l] = (c - c.min()) / span if span > 0 else 0.5
         alpha = 0.5 * np.arange(K) / max(K - 1, 1)            # [K]
         for l in range(T):
             nxt = base[(l + 1) % T]

@@ -57,6 +57,16 @@ SCENARIOS = {
     "rk4_10_steps": dict(nx=16, ny=16, dc=1e4, K=4, T=1, stepper="rk4",
                          nsteps=10, dt=20.19, f0=1e-4, grav=9.81,
                          visc_del2=1e3, seed=16),
+    # the smallest meshes: one column of cells (each cell its own east and
+    # west neighbour) and an odd 2x3 mesh, every term on
+    "tiny_1x2_lsrk5": dict(nx=1, ny=2, dc=1e4, K=2, T=1, stepper="lsrk5",
+                           nsteps=3, dt=20.0, f0=1e-4, grav=9.81,
+                           visc_del2=1e3, visc_del4=1e9, eddy_diff2=1e3,
+                           eddy_diff4=1e9, seed=18),
+    "tiny_2x3_rk4": dict(nx=2, ny=3, dc=1e4, K=3, T=2, stepper="rk4",
+                         nsteps=3, dt=20.0, f0=1e-4, grav=9.81,
+                         visc_del2=1e3, visc_del4=1e9, eddy_diff2=1e3,
+                         eddy_diff4=1e9, seed=19),
     # every term on, 5-stage LSRK, 1000 steps (long-run agreement)
     "lsrk5_1000_steps": dict(nx=12, ny=10, dc=1e4, K=3, T=2, stepper="lsrk5",
                              nsteps=1000, dt=20.0, f0=1e-4, grav=9.81,

@@ -118,6 +118,35 @@ def test_trajectory_dot_product_through_checkpointing(nsteps, nsnap):
         np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("nx,ny", [(1, 1), (1, 2), (2, 3)])
+@pytest.mark.parametrize("stepper,nstages", [("rk4", 4), ("lsrk", 5)])
+def test_tiny_mesh_dot_products(nx, ny, stepper, nstages):
+    """The smallest meshes, where a cell is its own neighbour and an edge
+    appears several times in another's edges-on-edge list (the transposed
+    tables then hold repeated entries): tendency and 6-step trajectory dot
+    products <= 1e-12."""
+    wl = ALL_TERMS.scaled(nx=nx, ny=ny, nlayers=3, ntracers=2)
+    mesh, params, model = setup(wl)
+    adj = og.Adjoint(model, 2, stepper, nstages)
+    x0 = initial_state(mesh, wl)
+    shapes = [a.shape for a in x0]
+    dx, mu = rand_like(shapes, 505, (1.0, 0.01, 10.0)), rand_like(shapes, 606)
+    X = make_state(mesh, params, x0)
+    JD, JT = og.ShallowWaterState(mesh, params), og.ShallowWaterState(mesh, params)
+    adj.tlm_tendency(X, make_state(mesh, params, dx), JD)
+    adj.adj_tendency(X, make_state(mesh, params, mu), JT)
+    lhs, rhs = dot(JD.download(), mu), dot(dx, JT.download())
+    assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+    XN = og.ShallowWaterState(mesh, params)
+    adj.forward(X, 0.0, wl.dt, 6, XN)
+    LAM = make_state(mesh, params, mu)
+    adj.backward(LAM)
+    DX = make_state(mesh, params, dx)
+    adj.tlm_apply(X, DX, 0.0, wl.dt, 6)
+    lhs, rhs = dot(DX.download(), mu), dot(dx, LAM.download())
+    assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+
+
 def _fd_check(wl, nsteps, nsnap, ndir, eps, stepper="rk4", nstages=4,
               richardson=False):
     """Worst relative difference between the adjoint gradient and central

@@ -150,3 +150,23 @@ def test_batch_rejects_shared_models_and_states():
     with pytest.raises(og.SwgError):
         og.Batch([model, other], [a, a])
     og.Batch([model, other], [a, b])  # distinct members are fine
+
+
+def test_tiny_members_match_single_instance_bitwise():
+    """The smallest meshes as members (one column of cells, each cell its own
+    east and west neighbour; an odd 2x3 mesh; one level, no tracers) beside
+    a regular one, in every launch configuration."""
+    from omega_playground_gb300.workloads import WORKLOADS
+    base = WORKLOADS["lsrk5_512x512"]
+    wls = [base.scaled(nx=1, ny=2, nlayers=1, ntracers=0, seed=71),
+           base.scaled(nx=2, ny=3, nlayers=3, ntracers=2, seed=72),
+           base.scaled(nx=1, ny=1, nlayers=5, ntracers=1, seed=73),
+           base.scaled(nx=8, ny=6, nlayers=33, ntracers=3, seed=74)]
+    members = build_members(wls)
+    ref = run_single(members, wls, "lsrk", 5, 3)
+    assert all(np.all(np.isfinite(x)) for r in ref for x in r)
+    for cfg in range(og.Batch.config_count()):
+        got, _ = run_batch(members, wls, "lsrk", 5, 3, config=cfg)
+        for m, (a, b) in enumerate(zip(got, ref)):
+            for x, y in zip(a, b):
+                np.testing.assert_array_equal(x, y, err_msg=f"config {cfg} member {m}")

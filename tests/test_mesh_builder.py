@@ -26,7 +26,9 @@ def product_tables(nx, ny, dc):
     return tabs, px.value, py.value
 
 
-@pytest.mark.parametrize("nx,ny,dc", [(2, 2, 1.0), (4, 4, 1e4), (5, 7, 1e4),
+@pytest.mark.parametrize("nx,ny,dc", [(1, 1, 1e4), (1, 2, 1e4), (2, 1, 1e4),
+                                      (2, 3, 1e4), (2, 2, 1.0), (4, 4, 1e4),
+                                      (5, 7, 1e4),
                                       (6, 10, 2e4), (16, 16, 1e4),
                                       (25, 29, 2e5), (64, 64, 1e4),
                                       (7, 6, 0.125)])
@@ -50,10 +52,11 @@ def test_matches_golden(name):
 
 def test_rejects_degenerate_sizes():
     tabs = _capi.HexTables()
-    rc = _capi.lib().swg_planar_hex_mesh_build(1, 4, 1.0, C.byref(tabs),
-                                               None, None)
-    assert rc == 1
-    assert b"nx >= 2" in _capi.lib().swg_last_error()
+    for nx, ny in ((0, 4), (3, 0), (-1, 2)):
+        rc = _capi.lib().swg_planar_hex_mesh_build(nx, ny, 1.0, C.byref(tabs),
+                                                   None, None)
+        assert rc == 1
+        assert b"nx >= 1" in _capi.lib().swg_last_error()
 
 
 def test_operator_convergence_on_tables():
