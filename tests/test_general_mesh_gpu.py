@@ -10,7 +10,7 @@ random 0/1 edge_mask and random per-column max levels for the diagnostics.
 The connectivity stays a valid mesh, so every index is in range.
 
 Bounds (normwise relative): tendencies and states after 3 steps <= 1e-12;
-diagnostics <= 1e-12 relative."""
+diagnostics <= 1e-12 relative; adjoint dot products <= 1e-12."""
 import numpy as np
 import pytest
 
@@ -29,7 +29,11 @@ TABLES = ("nedges_on_cell", "edges_on_cell", "nedges_on_edge",
           "area_triangle", "kiteareas_on_vertex", "edge_sign_on_vertex")
 
 
-def general_mesh(nx, ny, K, seed):
+def general_mesh(nx, ny, K, seed, adjoint_ready=False, cut_cells=None):
+    """Perturbed tables; with adjoint_ready the edge mask stays all ones,
+    every dv stays >= dc/4 and every cell keeps its 6 edges (the adjoint's
+    supported set: cutting a cell's list to 5 leaves an edge its neighbour
+    still lists, which no consistent mesh has and the adjoint rejects)."""
     om = pyoracle.OracleMesh(nx, ny, 1e4, K)
     t = om.tables
     C_, E, V = om.ncells, om.nedges, om.nvertices
@@ -44,9 +48,11 @@ def general_mesh(nx, ny, K, seed):
     jitter(t["kiteareas_on_vertex"], seed + 5)
     jitter(t["weights_on_edge"], seed + 6)
     u = uniform(seed + 7, E)
-    t["dv_edge"][u < 0.05] = 0.2 * t["dc_edge"][u < 0.05]
+    if not adjoint_ready:
+        t["dv_edge"][u < 0.05] = 0.2 * t["dc_edge"][u < 0.05]
     u = uniform(seed + 8, C_)
-    t["nedges_on_cell"][u < 0.1] = 5
+    if (not adjoint_ready) if cut_cells is None else cut_cells:
+        t["nedges_on_cell"][u < 0.1] = 5
     u = uniform(seed + 9, E)
     w = t["weights_on_edge"]
     for e in np.nonzero(u < 0.1)[0]:      # fill the hexagon's zero weights
@@ -56,7 +62,8 @@ def general_mesh(nx, ny, K, seed):
     t["nedges_on_edge"][(u > 0.9) & (u < 0.95)] = 7
     t["mesh_scaling_del2"][:] = 0.5 + uniform(seed + 10, E)
     t["mesh_scaling_del4"][:] = 0.5 + uniform(seed + 11, E)
-    t["edge_mask"][:] = (uniform(seed + 12, E * K) < 0.8).reshape(E, K)
+    if not adjoint_ready:
+        t["edge_mask"][:] = (uniform(seed + 12, E * K) < 0.8).reshape(E, K)
     mlc = (1 + uniform(seed + 13, C_) * K).astype(np.int32)
     mlv = (uniform(seed + 14, V) * (K + 1)).astype(np.int32)
     om.set_max_levels(np.minimum(mlc, K), np.minimum(mlv, K))
@@ -139,3 +146,48 @@ def test_general_mesh_diagnostics_with_max_levels():
     # the max levels matter: the full-column sums differ
     assert abs(og.mass_integral(S, model) - float(
         np.sum(om.area_cell[:, None] * h))) > 1e-6 * abs(omd.mass(h))
+
+
+@pytest.mark.parametrize("stepper,nstages", [("rk4", 4), ("lsrk", 5)])
+def test_general_mesh_adjoint_dot_products(stepper, nstages):
+    """The adjoint on perturbed tables (random geometry, 10 nonzero TRiSK
+    weights, shortened edges-on-edge lists, random del2/del4 scaling):
+    tendency and 5-step trajectory dot products against the tangent-linear
+    model <= 1e-12; tables that no consistent mesh has are rejected."""
+    cut = general_mesh(10, 8, 4, 7373, adjoint_ready=True, cut_cells=True)
+    with pytest.raises(og.SwgError, match="neighbour"):
+        og.Adjoint(models(*cut, 2)[2], 2)
+    om, gm = general_mesh(10, 8, 4, 7373, adjoint_ready=True)
+    T = 2
+    _, gp, model = models(om, gm, T)
+    adj = og.Adjoint(model, 2, stepper, nstages)
+    x = state(om, T, 41)
+    C_, E, K = om.ncells, om.nedges, om.nlayers
+    dx = (uniform(51, C_ * K).reshape(C_, K) - 0.5,
+          0.01 * (uniform(52, E * K).reshape(E, K) - 0.5),
+          10 * (uniform(53, T * C_ * K).reshape(T, C_, K) - 0.5))
+    mu = tuple(uniform(61 + j, a.size).reshape(a.shape) - 0.5
+               for j, a in enumerate(x))
+
+    def mk(a):
+        st = og.ShallowWaterState(gm, gp)
+        st.upload(*a)
+        return st
+
+    def dot(a, b):
+        return sum(float(np.sum(p * q)) for p, q in zip(a, b))
+
+    X = mk(x)
+    JD, JT = og.ShallowWaterState(gm, gp), og.ShallowWaterState(gm, gp)
+    adj.tlm_tendency(X, mk(dx), JD)
+    adj.adj_tendency(X, mk(mu), JT)
+    lhs, rhs = dot(JD.download(), mu), dot(dx, JT.download())
+    assert abs(lhs - rhs) <= TOL * max(abs(lhs), abs(rhs)), (lhs, rhs)
+    XN = og.ShallowWaterState(gm, gp)
+    adj.forward(X, 0.0, 5.0, 5, XN)
+    LAM = mk(mu)
+    adj.backward(LAM)
+    DX = mk(dx)
+    adj.tlm_apply(X, DX, 0.0, 5.0, 5)
+    lhs, rhs = dot(DX.download(), mu), dot(dx, LAM.download())
+    assert abs(lhs - rhs) <= TOL * max(abs(lhs), abs(rhs)), (lhs, rhs)
