@@ -49,6 +49,7 @@ typedef struct swg_model_s *swg_model;
 typedef struct swg_stepper_s *swg_stepper;
 typedef struct swg_batch_s *swg_batch;
 typedef struct swg_adjoint_s *swg_adjoint;
+typedef struct swg_host_stepper_s *swg_host_stepper;
 
 /* Message of the calling thread's last failed call ("" if none). */
 const char *swg_last_error(void);
@@ -261,6 +262,37 @@ int swg_stepper_destroy(swg_stepper stepper);
  * CUDA graph of one step (ignored when a forcing hook is set). */
 int swg_step(swg_stepper stepper, swg_state state, double t0, double dt,
              int nsteps, int use_graph, void *stream);
+
+/* ---------------------------------------------- host-resident states -----
+ * Steps a state that lives in host memory, for a host program that owns the
+ * state between steps (no counterpart in the reference, whose Kokkos views
+ * live in the execution space's memory).  The arrays have the layout of
+ * swg_state_upload: h [C][K], vn [E][K], tr [T][C][K].
+ * Every tendency term reads and writes one level at a time, so the levels
+ * are cut into chunks of `level_chunk` levels (the last chunk takes the
+ * rest; <= 0 or >= K: one chunk).  Each chunk is advanced by its own level
+ * slice of the model.  The chunks are pipelined on three streams: chunk c+1
+ * is copied in while chunk c is computed and chunk c-1 is copied out.
+ * Copies overlap only from page-locked host memory (swg_host_alloc or
+ * cudaHostAlloc); pageable arrays work but serialise.
+ * Results are bitwise equal to swg_state_upload + swg_step + swg_state_download
+ * on the same model.  Each call reads the model's term switches and its
+ * f_vertex.  The model must have no forcing hook, because the hook would see
+ * level slices.  The model must outlive the stepper.  kind and nstages are
+ * those of swg_stepper_create. */
+int swg_host_stepper_create(swg_model model, int kind, int nstages,
+                            int level_chunk, swg_host_stepper *out);
+int swg_host_stepper_destroy(swg_host_stepper hs);
+/* levels per chunk of the stepper's chunks (n entries; *n = count if NULL) */
+int swg_host_stepper_chunks(swg_host_stepper hs, int *levels, int *n);
+/* nsteps steps of size dt from t0, in place on the host arrays.  Ordered
+ * after the work already queued on `stream`; returns once the arrays hold
+ * the result.  tr may be NULL when the model has no tracers. */
+int swg_host_step(swg_host_stepper hs, double *h, double *vn, double *tr,
+                  double t0, double dt, int nsteps, void *stream);
+/* page-locked host memory (cudaHostAlloc) for the arrays above */
+int swg_host_alloc(unsigned long long bytes, void **out);
+int swg_host_free(void *p);
 
 /* ----------------------------------------------------------- batches -----
  * Ensembles of independent members with uneven mesh size, level count and

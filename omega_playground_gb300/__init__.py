@@ -7,6 +7,7 @@ in include/swgpu.h.  This package is the Python mirror of the reference's
 C++ classes (see shallow_water.py); the C++ mirror is cxx/omega_gpu.hpp.
 """
 from .shallow_water import (AddMode, Adjoint, Batch, LSRKStepper,  # noqa: F401
+                            HostStepper, pinned_empty,
                             MPASMesh, adjoint_batch_backward,
                             adjoint_batch_forward, checkpoint_cost,
                             PlanarHexagonalMesh, RK4Stepper,
@@ -19,7 +20,8 @@ from .shallow_water import (AddMode, Adjoint, Batch, LSRKStepper,  # noqa: F401
 from ._capi import SwgError, exported_symbols  # noqa: F401
 from . import workloads  # noqa: F401
 
-__all__ = ["AddMode", "Adjoint", "Batch", "checkpoint_cost",
+__all__ = ["AddMode", "Adjoint", "Batch", "checkpoint_cost", "HostStepper",
+           "pinned_empty",
            "LinearShallowWaterModel", "LinearShallowWaterParams",
            "adjoint_batch_forward", "adjoint_batch_backward", "LSRKStepper", "MPASMesh", "PlanarHexagonalMesh",
            "RK4Stepper", "ShallowWaterModel", "ShallowWaterParams",

@@ -123,6 +123,15 @@ _SIGS = {
     "swg_stepper_destroy": (C.c_int, [_vp]),
     "swg_step": (C.c_int, [_vp, _vp, C.c_double, C.c_double, C.c_int,
                            C.c_int, _vp]),
+    "swg_host_stepper_create": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int,
+                                          C.POINTER(_vp)]),
+    "swg_host_stepper_destroy": (C.c_int, [_vp]),
+    "swg_host_stepper_chunks": (C.c_int, [_vp, C.POINTER(C.c_int),
+                                          C.POINTER(C.c_int)]),
+    "swg_host_step": (C.c_int, [_vp, _dp, _dp, _dp, C.c_double, C.c_double,
+                                C.c_int, _vp]),
+    "swg_host_alloc": (C.c_int, [C.c_ulonglong, C.POINTER(_vp)]),
+    "swg_host_free": (C.c_int, [_vp]),
     "swg_batch_create": (C.c_int, [C.c_int, C.POINTER(_vp), C.POINTER(_vp),
                                    C.c_int, C.c_int, C.POINTER(_vp)]),
     "swg_batch_destroy": (C.c_int, [_vp]),

@@ -478,6 +478,7 @@ extern "C" int swg_model_create_ex(swg_mesh mesh, const swg_params *p,
   }
   pv.drag = !o.linear && o.apply_drag && p->drag_coeff > 0 && pv.do_vn;
   pv.drag_coeff = p->drag_coeff;
+  pv.drag_level = int(K) - 1; // the lowest level
 
   std::vector<double> f(V, p->f0), c2(E), c4(E), kd2(6 * C), r4(6 * C),
       r4s(C), gidc(E);

@@ -282,7 +282,7 @@ __device__ __forceinline__ void pt_edge_final(const MeshView &m,
   if (!p.off_ssh)
     t = fma(-__ldg(p.gidc + e),
             s.h[size_t(c1) * K + k] - s.h[size_t(c0) * K + k], t);
-  if (p.drag && k == K - 1) {
+  if (p.drag && k == p.drag_level) {
     // bottom drag -c_d sqrt(ke_0 + ke_1) vn / mean_h on the lowest level
     // (the term commented out at shallow_water_hierarchical.cpp:479-486)
     const T hm = 0.5 * (s.h[size_t(c0) * K + k] + s.h[size_t(c1) * K + k]);

@@ -1,0 +1,283 @@
+// Stepping a host-resident state in level chunks (swg_host_stepper_*).
+//
+// Every tendency term of the model reads and writes one vertical level at a
+// time (the functors of shallow_water_model.cpp:43-311 index [entity][k]
+// with the same k on both sides), so a state's levels [k0, k0 + kc) evolve
+// independently of the others.  The one term tied to a level's position,
+// the opt-in bottom drag, is given its level in each slice.  The host stepper cuts the levels into
+// chunks and gives each chunk a level slice of the caller's model: a mesh
+// that shares the caller's device tables but has kc levels (and its own
+// slice of the per-level edge mask), a model whose view is the caller's,
+// a device state of kc levels and an ordinary stepper with its graph.
+// A call copies chunk c in on one stream, steps it on another and copies it
+// out on a third, so with page-locked host arrays the copies of one chunk
+// overlap the compute of its neighbours.  Each level sees the same kernels
+// and operands as in the unsliced model, so the results are bitwise equal.
+#include "swg_internal.h"
+
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#define TRY(x)                                                                 \
+  do {                                                                         \
+    int rc_ = (x);                                                             \
+    if (rc_ != SWG_OK)                                                         \
+      return rc_;                                                              \
+  } while (0)
+
+using namespace swg;
+
+namespace {
+
+struct Chunk {
+  int k0 = 0, kc = 0;
+  swg_mesh mesh = nullptr;
+  swg_model model = nullptr;
+  swg_state state = nullptr;
+  swg_stepper stepper = nullptr;
+  cudaEvent_t in = nullptr, out = nullptr;
+};
+
+// Levels [k0, k0 + kc) of `src`: the K-independent device tables are
+// shared (not owned: the slice frees only its own edge-mask copy), the
+// per-level edge mask is copied, and the per-column maximum levels of the
+// diagnostics are dropped (slices run no diagnostics).
+int mesh_slice(swg_mesh src, int k0, int kc, swg_mesh *out) {
+  swg_mesh m = new (std::nothrow) swg_mesh_s(*src);
+  if (!m)
+    return fail(SWG_ERR_OOM, "swg_host_stepper_create: host allocation");
+  m->allocs.clear();
+  m->nlayers = kc;
+  m->view.nlayers = kc;
+  m->view.maxlev_c = m->view.maxlev_v = nullptr;
+  if (src->view.mask) {
+    const size_t E = src->nedges, K = src->nlayers;
+    void *d = nullptr;
+    cudaError_t err = cudaMalloc(&d, E * kc * sizeof(double));
+    if (err == cudaSuccess) {
+      m->allocs.push_back(d);
+      err = cudaMemcpy2D(d, kc * sizeof(double), src->view.mask + k0,
+                         K * sizeof(double), kc * sizeof(double), E,
+                         cudaMemcpyDeviceToDevice);
+    }
+    if (err != cudaSuccess) {
+      swg_mesh_destroy(m);
+      return cuda_fail(err, "swg_host_stepper_create: edge mask slice");
+    }
+    m->view.mask = static_cast<const double *>(d);
+  }
+  *out = m;
+  return SWG_OK;
+}
+
+// Copy levels [k0, k0 + kc) of `rows` rows of K levels between the host
+// array and a dense [rows][kc] device array.
+cudaError_t copy_levels(double *dst, size_t dpitch, const double *src,
+                        size_t spitch, int kc, size_t rows,
+                        cudaMemcpyKind kind, cudaStream_t st) {
+  if (rows == 0)
+    return cudaSuccess;
+  return cudaMemcpy2DAsync(dst, dpitch * sizeof(double), src,
+                           spitch * sizeof(double), kc * sizeof(double), rows,
+                           kind, st);
+}
+
+} // namespace
+
+struct swg_host_stepper_s {
+  swg_model model = nullptr;
+  int K = 0, T = 0;
+  std::vector<Chunk> chunks;
+  cudaStream_t h2d = nullptr, comp = nullptr, d2h = nullptr;
+  cudaEvent_t go = nullptr, done = nullptr;
+};
+
+extern "C" int swg_host_stepper_destroy(swg_host_stepper hs) {
+  if (!hs)
+    return SWG_OK;
+  for (Chunk &c : hs->chunks) {
+    swg_stepper_destroy(c.stepper);
+    swg_state_destroy(c.state);
+    swg_model_destroy(c.model);
+    swg_mesh_destroy(c.mesh);
+    if (c.in)
+      cudaEventDestroy(c.in);
+    if (c.out)
+      cudaEventDestroy(c.out);
+  }
+  for (cudaStream_t s : {hs->h2d, hs->comp, hs->d2h})
+    if (s)
+      cudaStreamDestroy(s);
+  for (cudaEvent_t e : {hs->go, hs->done})
+    if (e)
+      cudaEventDestroy(e);
+  delete hs;
+  return SWG_OK;
+}
+
+static int make_chunk(swg_host_stepper hs, int kind, int nstages, Chunk &c) {
+  swg_model src = hs->model;
+  TRY(mesh_slice(src->mesh, c.k0, c.kc, &c.mesh));
+  swg_model_options o{};
+  o.linear = src->view.linear;
+  o.h0 = src->view.h0;
+  o.apply_drag = src->view.drag;
+  TRY(swg_model_create_ex(c.mesh, &src->params, &o, &c.model));
+  TRY(swg_state_create(c.mesh, hs->T, &c.state));
+  TRY(swg_stepper_create(c.model, kind, nstages, &c.stepper));
+  cudaError_t err = cudaEventCreateWithFlags(&c.in, cudaEventDisableTiming);
+  if (err == cudaSuccess)
+    err = cudaEventCreateWithFlags(&c.out, cudaEventDisableTiming);
+  return err == cudaSuccess ? SWG_OK
+                            : cuda_fail(err, "swg_host_stepper_create: events");
+}
+
+extern "C" int swg_host_stepper_create(swg_model model, int kind, int nstages,
+                                       int level_chunk,
+                                       swg_host_stepper *out) {
+  if (!model || !out)
+    return fail(SWG_ERR_ARG, "swg_host_stepper_create: NULL argument");
+  *out = nullptr;
+  if (model->forcing)
+    return fail(SWG_ERR_ARG, "swg_host_stepper_create: the model has a "
+                             "forcing hook (it would see level slices)");
+  swg_host_stepper hs = new (std::nothrow) swg_host_stepper_s();
+  if (!hs)
+    return fail(SWG_ERR_OOM, "swg_host_stepper_create: host allocation");
+  hs->model = model;
+  hs->K = model->mesh->nlayers;
+  hs->T = model->params.ntracers;
+  const int kc = level_chunk <= 0 || level_chunk > hs->K ? hs->K : level_chunk;
+  for (int k0 = 0; k0 < hs->K; k0 += kc) {
+    Chunk c;
+    c.k0 = k0;
+    c.kc = std::min(kc, hs->K - k0);
+    hs->chunks.push_back(c);
+  }
+  int rc = SWG_OK;
+  for (Chunk &c : hs->chunks)
+    if ((rc = make_chunk(hs, kind, nstages, c)) != SWG_OK) {
+      swg_host_stepper_destroy(hs);
+      return rc;
+    }
+  cudaError_t err = cudaSuccess;
+  for (cudaStream_t *s : {&hs->h2d, &hs->comp, &hs->d2h})
+    if (err == cudaSuccess)
+      err = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
+  for (cudaEvent_t *e : {&hs->go, &hs->done})
+    if (err == cudaSuccess)
+      err = cudaEventCreateWithFlags(e, cudaEventDisableTiming);
+  if (err != cudaSuccess) {
+    swg_host_stepper_destroy(hs);
+    return cuda_fail(err, "swg_host_stepper_create: streams");
+  }
+  *out = hs;
+  return SWG_OK;
+}
+
+extern "C" int swg_host_stepper_chunks(swg_host_stepper hs, int *levels,
+                                       int *n) {
+  if (!hs || !n)
+    return fail(SWG_ERR_ARG, "swg_host_stepper_chunks: NULL argument");
+  if (levels)
+    for (int i = 0; i < *n && i < int(hs->chunks.size()); ++i)
+      levels[i] = hs->chunks[i].kc;
+  *n = int(hs->chunks.size());
+  return SWG_OK;
+}
+
+extern "C" int swg_host_step(swg_host_stepper hs, double *h, double *vn,
+                             double *tr, double t0, double dt, int nsteps,
+                             void *stream) {
+  if (!hs || !h || !vn || (hs->T > 0 && !tr) || nsteps < 0)
+    return fail(SWG_ERR_ARG, "swg_host_step: bad argument");
+  swg_model src = hs->model;
+  if (src->forcing)
+    return fail(SWG_ERR_ARG, "swg_host_step: the model has a forcing hook "
+                             "(it would see level slices)");
+  const size_t K = hs->K, C = src->mesh->ncells, E = src->mesh->nedges,
+               TC = size_t(hs->T) * C;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  NvtxRange range("host_step");
+  cudaError_t err = cudaEventRecord(hs->go, st);
+  for (cudaStream_t s : {hs->h2d, hs->comp, hs->d2h})
+    if (err == cudaSuccess)
+      err = cudaStreamWaitEvent(s, hs->go, 0);
+  // copies in, back to back on the copy-in stream
+  for (Chunk &c : hs->chunks) {
+    const int kc = c.kc;
+    if (err == cudaSuccess)
+      err = copy_levels(c.state->h, kc, h + c.k0, K, kc, C,
+                        cudaMemcpyHostToDevice, hs->h2d);
+    if (err == cudaSuccess)
+      err = copy_levels(c.state->vn, kc, vn + c.k0, K, kc, E,
+                        cudaMemcpyHostToDevice, hs->h2d);
+    if (err == cudaSuccess && TC)
+      err = copy_levels(c.state->tr, kc, tr + c.k0, K, kc, TC,
+                        cudaMemcpyHostToDevice, hs->h2d);
+    if (err == cudaSuccess)
+      err = cudaEventRecord(c.in, hs->h2d);
+  }
+  if (err != cudaSuccess)
+    return cuda_fail(err, "swg_host_step: copy in");
+  // each chunk's steps once its levels are in; the slice model takes the
+  // caller's current view (term switches, f_vertex) and its version, so a
+  // switch recaptures the chunk's step graph
+  for (Chunk &c : hs->chunks) {
+    err = cudaStreamWaitEvent(hs->comp, c.in, 0);
+    if (err != cudaSuccess)
+      return cuda_fail(err, "swg_host_step: stream order");
+    c.model->view = src->view;
+    // the bottom drag acts on the caller's lowest level only: in the slice
+    // holding it that is level drag_level - k0, in the others no level
+    c.model->view.drag_level = src->view.drag_level - c.k0;
+    c.model->version = src->version;
+    c.model->terms_switched = src->terms_switched;
+    TRY(swg_step(c.stepper, c.state, t0, dt, nsteps, 1, hs->comp));
+    err = cudaEventRecord(c.out, hs->comp);
+    if (err != cudaSuccess)
+      return cuda_fail(err, "swg_host_step: stream order");
+  }
+  // copies out as each chunk finishes
+  for (Chunk &c : hs->chunks) {
+    const int kc = c.kc;
+    if (err == cudaSuccess)
+      err = cudaStreamWaitEvent(hs->d2h, c.out, 0);
+    if (err == cudaSuccess)
+      err = copy_levels(h + c.k0, K, c.state->h, kc, kc, C,
+                        cudaMemcpyDeviceToHost, hs->d2h);
+    if (err == cudaSuccess)
+      err = copy_levels(vn + c.k0, K, c.state->vn, kc, kc, E,
+                        cudaMemcpyDeviceToHost, hs->d2h);
+    if (err == cudaSuccess && TC)
+      err = copy_levels(tr + c.k0, K, c.state->tr, kc, kc, TC,
+                        cudaMemcpyDeviceToHost, hs->d2h);
+  }
+  if (err == cudaSuccess)
+    err = cudaEventRecord(hs->done, hs->d2h);
+  if (err == cudaSuccess)
+    err = cudaStreamWaitEvent(st, hs->done, 0);
+  if (err == cudaSuccess)
+    err = cudaStreamSynchronize(st);
+  return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_host_step");
+}
+
+extern "C" int swg_host_alloc(unsigned long long bytes, void **out) {
+  if (!out)
+    return fail(SWG_ERR_ARG, "swg_host_alloc: NULL argument");
+  *out = nullptr;
+  cudaError_t err = cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocDefault);
+  if (err != cudaSuccess) {
+    *out = nullptr;
+    return cuda_fail(err, "swg_host_alloc");
+  }
+  return SWG_OK;
+}
+
+extern "C" int swg_host_free(void *p) {
+  if (!p)
+    return SWG_OK;
+  cudaError_t err = cudaFreeHost(p);
+  return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_host_free");
+}

@@ -73,6 +73,7 @@ struct ModelView {
   // LinearShallowWaterModel (mean thickness h0; f4 = 4 f0, the Coriolis
   // factor for the weights/4 table), and the optional bottom drag
   int linear, drag;
+  int drag_level; // the level of the model's arrays that carries the drag
   double h0, f4, drag_coeff;
   // tendency terms switched off after create (the reference's m_enabled
   // members); zero = on, so zero-initialised views keep every term

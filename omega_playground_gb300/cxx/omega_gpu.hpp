@@ -508,6 +508,29 @@ struct RK4Stepper : TimeStepper {
       : TimeStepper(shallow_water, SWG_STEPPER_RK4, 4) {}
 };
 
+// A state kept in host arrays (h [C][K], vn [E][K], tr [T][C][K]) advanced
+// in place, level chunk by level chunk, with each chunk's copies overlapping
+// the other chunks' compute (swg_host_stepper_*).  Bitwise equal to upload +
+// do_steps + download.  The model must have no additional_tendency override
+// and must outlive the stepper.  No counterpart in the reference.
+struct HostStepper {
+  swg_host_stepper m_handle = nullptr;
+  HostStepper(ShallowWaterModel &shallow_water, bool rk4 = false,
+              Int nstages = 5, Int level_chunk = 0) {
+    shallow_water.resolve_hook();
+    swg_check(swg_host_stepper_create(
+        shallow_water.m_handle, rk4 ? SWG_STEPPER_RK4 : SWG_STEPPER_LSRK,
+        rk4 ? 4 : nstages, level_chunk, &m_handle));
+  }
+  HostStepper(const HostStepper &) = delete;
+  HostStepper &operator=(const HostStepper &) = delete;
+  ~HostStepper() { swg_host_stepper_destroy(m_handle); }
+  void do_steps(Real t0, Real dt, double *h, double *vn, double *tr,
+                Int nsteps) const {
+    swg_check(swg_host_step(m_handle, h, vn, tr, t0, dt, nsteps, nullptr));
+  }
+};
+
 // ----------------------------------------------- ensembles and gradients --
 // Beside the plain solver; no counterpart in the reference.
 

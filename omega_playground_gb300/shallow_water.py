@@ -476,6 +476,83 @@ class LSRKStepper(TimeStepper):
         super().__init__(shallow_water, nstages)
 
 
+def pinned_empty(shape) -> np.ndarray:
+    """An uninitialised float64 array in page-locked host memory
+    (swg_host_alloc), freed when the last array viewing it goes away."""
+    shape = tuple(int(n) for n in np.atleast_1d(shape))
+    n = int(np.prod(shape))
+    p = C.c_void_p()
+    check(lib().swg_host_alloc(max(n, 1) * 8, C.byref(p)))
+    buf = (C.c_double * max(n, 1)).from_address(p.value)
+    buf._owner = _PinnedBlock(p.value)
+    return np.frombuffer(buf, np.float64, n).reshape(shape)
+
+
+class _PinnedBlock:
+    def __init__(self, ptr):
+        self.ptr = ptr
+
+    def __del__(self):
+        if _capi._lib is not None:
+            _capi._lib.swg_host_free(C.c_void_p(self.ptr))
+
+
+class HostStepper:
+    """Steps a state held in host arrays (h [C][K], vn [E][K], tr [T][C][K],
+    C-contiguous float64) in place, in chunks of `level_chunk` levels whose
+    copies overlap the other chunks' compute (swg_host_stepper_* in
+    swgpu.h).  Bitwise equal to upload + step + download; arrays from
+    pinned_empty let the copies overlap.  stepper is "rk4" or "lsrk"."""
+
+    def __init__(self, model: ShallowWaterModel, stepper: str = "lsrk",
+                 nstages: int = 5, level_chunk: int = 0):
+        self.model = model
+        h = C.c_void_p()
+        check(lib().swg_host_stepper_create(
+            model.handle, 0 if stepper == "rk4" else 1, int(nstages),
+            int(level_chunk), C.byref(h)))
+        self._h = h
+
+    @property
+    def chunks(self):
+        """Levels of each chunk."""
+        n = C.c_int(0)
+        check(lib().swg_host_stepper_chunks(self._h, None, C.byref(n)))
+        out = (C.c_int * n.value)()
+        check(lib().swg_host_stepper_chunks(self._h, out, C.byref(n)))
+        return list(out)
+
+    def pinned_state(self):
+        """(h, vn, tr) page-locked host arrays of the model's state shapes."""
+        m, T = self.model.m_mesh, self.model.m_params.m_ntracers
+        return (pinned_empty((m.m_ncells, m.m_nlayers)),
+                pinned_empty((m.m_nedges, m.m_nlayers)),
+                pinned_empty((T, m.m_ncells, m.m_nlayers)))
+
+    def step(self, h, vn, tr, t0: float, dt: float, nsteps: int = 1,
+             stream=None):
+        m, T = self.model.m_mesh, self.model.m_params.m_ntracers
+        want = ((m.m_ncells, m.m_nlayers), (m.m_nedges, m.m_nlayers),
+                (T, m.m_ncells, m.m_nlayers))
+        arrs = (h, vn, tr)
+        for name, a, shape in zip(("h", "vn", "tr"), arrs, want):
+            if a is None and name == "tr" and T == 0:
+                continue
+            if not isinstance(a, np.ndarray) or a.dtype != np.float64 or \
+                    not a.flags.c_contiguous or not a.flags.writeable or \
+                    a.size != int(np.prod(shape)):
+                raise TypeError(f"{name}: expected a writeable C-contiguous "
+                                f"float64 array of shape {shape}")
+        check(lib().swg_host_step(self._h, _d(h), _d(vn),
+                                  _d(tr) if T else None, float(t0),
+                                  float(dt), int(nsteps), _s(stream)))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _capi._lib is not None:
+            _capi._lib.swg_host_stepper_destroy(self._h)
+            self._h = None
+
+
 class Batch:
     """Ensemble of independent members (uneven nx, levels, tracers) advanced
     together by one persistent kernel per RK stage (swg_batch_* in swgpu.h).

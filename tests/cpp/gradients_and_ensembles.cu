@@ -2,8 +2,9 @@
 // user would: (1) a dot-product test of the checkpointed adjoint against the
 // tangent-linear model over 10 RK4 steps with every term on,
 // <J dx0, lamN> = <dx0, J^T lamN> to 1e-12; (2) three members of different
-// sizes advanced by EnsembleStepper equal, bit for bit, the same members
-// advanced one at a time by RK4Stepper.  Exits non-zero on failure.
+// sizes advanced by EnsembleStepper, and by HostStepper from host arrays,
+// equal, bit for bit, the same members advanced one at a time by
+// RK4Stepper.  Exits non-zero on failure.
 #include <omega_gpu.hpp>
 
 #include <cmath>
@@ -148,7 +149,22 @@ bool ensemble_test() {
       worst = std::fmax(worst, std::fabs(got.tr[i] - ref[m].tr[i]));
   }
   std::printf("ensemble max_abs_diff=%.3e\n", worst);
-  return worst == 0.0;
+  // the same members kept in host arrays, stepped in chunks of 2 levels
+  double worst_host = 0;
+  for (int m = 0; m < 3; ++m) {
+    Fields x = mem[m].x0;
+    HostStepper hs(*mem[m].model, true, 4, 2);
+    hs.do_steps(0, dt, x.h.data(), x.vn.data(),
+                x.tr.empty() ? nullptr : x.tr.data(), 3);
+    for (size_t i = 0; i < x.h.size(); ++i)
+      worst_host = std::fmax(worst_host, std::fabs(x.h[i] - ref[m].h[i]));
+    for (size_t i = 0; i < x.vn.size(); ++i)
+      worst_host = std::fmax(worst_host, std::fabs(x.vn[i] - ref[m].vn[i]));
+    for (size_t i = 0; i < x.tr.size(); ++i)
+      worst_host = std::fmax(worst_host, std::fabs(x.tr[i] - ref[m].tr[i]));
+  }
+  std::printf("host max_abs_diff=%.3e\n", worst_host);
+  return worst == 0.0 && worst_host == 0.0;
 }
 
 } // namespace

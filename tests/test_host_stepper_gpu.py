@@ -1,0 +1,153 @@
+"""Host-resident states stepped in level chunks (swg_host_stepper_* /
+og.HostStepper): bitwise equal to upload + swg_step + download on the same
+model, for ragged chunkings, both steppers, pinned and pageable arrays,
+general tables with a per-level edge mask, the linear model, the drag, the
+model's term switches and f_vertex read at each call, and the full-size
+512x512x64, 8-tracer workload."""
+import numpy as np
+import pytest
+
+import omega_playground_gb300 as og
+from omega_playground_gb300.workloads import WORKLOADS, initial_state
+
+pytestmark = pytest.mark.gpu
+
+WL = WORKLOADS["lsrk5_512x512"].scaled(nx=10, ny=8, nlayers=7, ntracers=2)
+
+
+def device_run(model, mesh, params, x, kind, nstages, t0, dt, nsteps):
+    S = og.ShallowWaterState(mesh, params)
+    S.upload(*x)
+    st = og.RK4Stepper(model) if kind == "rk4" else og.LSRKStepper(model,
+                                                                   nstages)
+    st.step(S, t0, dt, nsteps)
+    return S.download()
+
+
+def host_run(model, x, kind, nstages, chunk, t0, dt, nsteps, pinned=True):
+    hs = og.HostStepper(model, kind, nstages, chunk)
+    if pinned:
+        arrs = hs.pinned_state()
+        for a, b in zip(arrs, x):
+            a[...] = b
+    else:
+        arrs = tuple(np.array(a, copy=True) for a in x)
+    hs.step(*arrs, t0, dt, nsteps)
+    return arrs, hs
+
+
+def assert_bitwise(got, want):
+    for g, w in zip(got, want):
+        assert np.all(np.isfinite(w))
+        np.testing.assert_array_equal(g, w)
+
+
+@pytest.mark.parametrize("kind,nstages", [("rk4", 4), ("lsrk", 5),
+                                          ("lsrk", 1)])
+@pytest.mark.parametrize("chunk,want_chunks", [(0, [7]), (3, [3, 3, 1]),
+                                               (1, [1] * 7), (7, [7]),
+                                               (50, [7])])
+def test_bitwise_equal_to_device_stepper(kind, nstages, chunk, want_chunks):
+    mesh = og.PlanarHexagonalMesh(WL.nx, WL.ny, WL.dc, WL.nlayers)
+    params = WL.params()
+    model = og.ShallowWaterModel(mesh, params)
+    x = initial_state(mesh, WL)
+    want = device_run(model, mesh, params, x, kind, nstages, 5.0, WL.dt, 3)
+    got, hs = host_run(model, x, kind, nstages, chunk, 5.0, WL.dt, 3)
+    assert hs.chunks == want_chunks
+    assert_bitwise(got, want)
+    # a second call replays the chunks' graphs from the new host state
+    want2 = device_run(model, mesh, params, want, kind, nstages, 5.0, WL.dt, 2)
+    hs.step(*got, 5.0, WL.dt, 2)
+    assert_bitwise(got, want2)
+
+
+def test_pageable_arrays_no_tracers_and_zero_steps():
+    wl = WL.scaled(ntracers=0)
+    mesh = og.PlanarHexagonalMesh(wl.nx, wl.ny, wl.dc, wl.nlayers)
+    params = wl.params()
+    model = og.ShallowWaterModel(mesh, params)
+    x = initial_state(mesh, wl)
+    want = device_run(model, mesh, params, x, "rk4", 4, 0.0, wl.dt, 4)
+    got, hs = host_run(model, x, "rk4", 4, 2, 0.0, wl.dt, 4, pinned=False)
+    assert_bitwise(got[:2], want[:2])
+    before = tuple(a.copy() for a in got)
+    hs.step(got[0], got[1], None, 0.0, wl.dt, 0)
+    assert_bitwise(got[:2], before[:2])
+    with pytest.raises(TypeError):
+        hs.step(got[0].astype(np.float32), got[1], None, 0.0, wl.dt, 1)
+
+
+def test_general_tables_with_edge_mask():
+    from test_general_mesh_gpu import general_mesh, models, state
+    om, gm = general_mesh(10, 8, 7, 919)
+    T = 2
+    _, gp, model = models(om, gm, T)
+    x = state(om, T, 3)
+    want = device_run(model, gm, gp, x, "lsrk", 5, 0.0, 5.0, 3)
+    got, _ = host_run(model, x, "lsrk", 5, 3, 0.0, 5.0, 3)
+    assert_bitwise(got, want)
+
+
+def test_term_switches_and_f_vertex_are_read_at_each_call():
+    mesh = og.PlanarHexagonalMesh(WL.nx, WL.ny, WL.dc, WL.nlayers)
+    params = WL.params()
+    model = og.ShallowWaterModel(mesh, params)
+    x = initial_state(mesh, WL)
+    hs = og.HostStepper(model, "lsrk", 5, 4)
+    arrs = hs.pinned_state()
+    for a, b in zip(arrs, x):
+        a[...] = b
+    hs.step(*arrs, 0.0, WL.dt, 1)                 # graphs captured, all on
+    model.m_pv_flux_edge.m_enabled = False
+    model.m_tracer_hyperdiff_cell.m_enabled = False
+    f = model.m_f_vertex
+    model.m_f_vertex = f * (1.0 + 0.1 * np.sin(np.arange(f.size)))
+    for a, b in zip(arrs, x):
+        a[...] = b
+    hs.step(*arrs, 0.0, WL.dt, 3)
+    want = device_run(model, mesh, params, x, "lsrk", 5, 0.0, WL.dt, 3)
+    assert_bitwise(arrs, want)
+
+
+def test_linear_model_and_drag():
+    mesh = og.PlanarHexagonalMesh(WL.nx, WL.ny, WL.dc, WL.nlayers)
+    lp = og.LinearShallowWaterParams(m_h0=1000.0, m_f0=1e-4, m_grav=9.81)
+    lin = og.LinearShallowWaterModel(mesh, lp)
+    x = initial_state(mesh, WL.scaled(ntracers=0))
+    x = (x[0], x[1], np.zeros((0,) + x[0].shape))
+    want = device_run(lin, mesh, og.ShallowWaterParams(), x, "rk4", 4, 0.0,
+                      WL.dt, 3)
+    got, _ = host_run(lin, x, "rk4", 4, 2, 0.0, WL.dt, 3)
+    assert_bitwise(got[:2], want[:2])
+    params = WL.params()
+    params.m_drag_coeff = 2e-3
+    drag = og.ShallowWaterModel(mesh, params, apply_drag=True)
+    x = initial_state(mesh, WL)
+    want = device_run(drag, mesh, params, x, "lsrk", 5, 0.0, WL.dt, 3)
+    got, _ = host_run(drag, x, "lsrk", 5, 2, 0.0, WL.dt, 3)
+    assert_bitwise(got, want)
+
+
+def test_hooked_model_is_rejected():
+    mesh = og.PlanarHexagonalMesh(6, 6, 1e4, 2)
+    params = og.ShallowWaterParams(m_f0=1e-4)
+
+    class Forced(og.ShallowWaterModel):
+        def additional_tendency(self, h_tend, vn_tend, h, vn, t, stream):
+            pass
+
+    with pytest.raises(og.SwgError, match="forcing hook"):
+        og.HostStepper(Forced(mesh, params), "rk4", 4, 1)
+
+
+def test_full_size_workload_one_step():
+    wl = WORKLOADS["lsrk5_512x512"]
+    mesh = og.PlanarHexagonalMesh(wl.nx, wl.ny, wl.dc, wl.nlayers)
+    params = wl.params()
+    model = og.ShallowWaterModel(mesh, params)
+    x = initial_state(mesh, wl)
+    want = device_run(model, mesh, params, x, "lsrk", 5, 0.0, wl.dt, 1)
+    got, hs = host_run(model, x, "lsrk", 5, 16, 0.0, wl.dt, 1)
+    assert hs.chunks == [16] * 4
+    assert_bitwise(got, want)

@@ -98,9 +98,11 @@ def test_benchmark_driver_runs():
 def test_cpp_gradient_and_ensemble_classes():
     """The C++ drop-in's CheckpointedAdjoint (dot product against the
     tangent-linear model, 10 RK4 steps, every term on, <= 1e-12) and
-    EnsembleStepper (three uneven members bitwise equal to RK4Stepper)."""
+    EnsembleStepper and HostStepper (three uneven members bitwise equal to
+    RK4Stepper)."""
     out = run("gradients_and_ensembles")
     assert "PASS" in out, out
     rel = float(re.search(r"rel=(\S+)", out).group(1))
     assert rel <= 1e-12
-    assert "max_abs_diff=0.000e+00" in out
+    assert "ensemble max_abs_diff=0.000e+00" in out
+    assert "host max_abs_diff=0.000e+00" in out
