@@ -187,11 +187,8 @@ extern "C" int swg_host_stepper_chunks(swg_host_stepper hs, int *levels,
   return SWG_OK;
 }
 
-extern "C" int swg_host_step(swg_host_stepper hs, double *h, double *vn,
-                             double *tr, double t0, double dt, int nsteps,
-                             void *stream) {
-  if (!hs || !h || !vn || (hs->T > 0 && !tr) || nsteps < 0)
-    return fail(SWG_ERR_ARG, "swg_host_step: bad argument");
+static int host_step(swg_host_stepper hs, double *h, double *vn, double *tr,
+                     double t0, double dt, int nsteps, void *stream) {
   swg_model src = hs->model;
   if (src->forcing)
     return fail(SWG_ERR_ARG, "swg_host_step: the model has a forcing hook "
@@ -261,6 +258,18 @@ extern "C" int swg_host_step(swg_host_stepper hs, double *h, double *vn,
   if (err == cudaSuccess)
     err = cudaStreamSynchronize(st);
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_host_step");
+}
+
+extern "C" int swg_host_step(swg_host_stepper hs, double *h, double *vn,
+                             double *tr, double t0, double dt, int nsteps,
+                             void *stream) {
+  if (!hs || !h || !vn || (hs->T > 0 && !tr) || nsteps < 0)
+    return fail(SWG_ERR_ARG, "swg_host_step: bad argument");
+  const int rc = host_step(hs, h, vn, tr, t0, dt, nsteps, stream);
+  if (rc != SWG_OK) // no copy queued before the failure outlives the call
+    for (cudaStream_t s : {hs->h2d, hs->comp, hs->d2h})
+      cudaStreamSynchronize(s);
+  return rc;
 }
 
 extern "C" int swg_host_alloc(unsigned long long bytes, void **out) {
