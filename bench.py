@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--level-chunk", type=int, default=16,
                     help="levels per chunk of the host-state stepper that "
                          "the end-to-end number goes through")
+    ap.add_argument("--levels", default="",
+                    help="chunk sizes of the host-state stepper, comma "
+                         "separated (overrides --level-chunk)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
@@ -405,7 +408,10 @@ def run_ours(args, wl):
     # chunks' compute), and beside it the serial upload + step + download
     e2e = None
     if not args.no_e2e:
-        hs = og.HostStepper(model, wl.stepper, wl.nstages, args.level_chunk)
+        hs = og.HostStepper(
+            model, wl.stepper, wl.nstages, args.level_chunk,
+            levels=[int(n) for n in args.levels.split(",")] if args.levels
+            else None)
         hh, vv, tt = hs.pinned_state()
         hh[...], vv[...], tt[...] = h0, vn0, tr0
         nbytes_in = hh.nbytes + vv.nbytes + tt.nbytes

@@ -282,6 +282,12 @@ int swg_step(swg_stepper stepper, swg_state state, double t0, double dt,
  * those of swg_stepper_create. */
 int swg_host_stepper_create(swg_model model, int kind, int nstages,
                             int level_chunk, swg_host_stepper *out);
+/* the same with chunk sizes given one by one (levels[0..nchunks), each >= 1,
+ * adding up to K).  Smaller first and last chunks shorten the copy-in that
+ * precedes the first compute and the copy-out that follows the last. */
+int swg_host_stepper_create_levels(swg_model model, int kind, int nstages,
+                                   int nchunks, const int *levels,
+                                   swg_host_stepper *out);
 int swg_host_stepper_destroy(swg_host_stepper hs);
 /* levels per chunk of the stepper's chunks (n entries; *n = count if NULL) */
 int swg_host_stepper_chunks(swg_host_stepper hs, int *levels, int *n);

@@ -125,6 +125,9 @@ _SIGS = {
                            C.c_int, _vp]),
     "swg_host_stepper_create": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int,
                                           C.POINTER(_vp)]),
+    "swg_host_stepper_create_levels": (C.c_int, [_vp, C.c_int, C.c_int,
+                                                 C.c_int, C.POINTER(C.c_int),
+                                                 C.POINTER(_vp)]),
     "swg_host_stepper_destroy": (C.c_int, [_vp]),
     "swg_host_stepper_chunks": (C.c_int, [_vp, C.POINTER(C.c_int),
                                           C.POINTER(C.c_int)]),

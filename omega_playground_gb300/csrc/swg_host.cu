@@ -133,26 +133,36 @@ static int make_chunk(swg_host_stepper hs, int kind, int nstages, Chunk &c) {
                             : cuda_fail(err, "swg_host_stepper_create: events");
 }
 
-extern "C" int swg_host_stepper_create(swg_model model, int kind, int nstages,
-                                       int level_chunk,
-                                       swg_host_stepper *out) {
-  if (!model || !out)
-    return fail(SWG_ERR_ARG, "swg_host_stepper_create: NULL argument");
+extern "C" int swg_host_stepper_create_levels(swg_model model, int kind,
+                                              int nstages, int nchunks,
+                                              const int *levels,
+                                              swg_host_stepper *out) {
+  if (!model || !out || nchunks < 1 || !levels)
+    return fail(SWG_ERR_ARG, "swg_host_stepper_create: bad argument");
   *out = nullptr;
   if (model->forcing)
     return fail(SWG_ERR_ARG, "swg_host_stepper_create: the model has a "
                              "forcing hook (it would see level slices)");
+  long long sum = 0;
+  for (int i = 0; i < nchunks; ++i) {
+    if (levels[i] < 1)
+      return fail(SWG_ERR_ARG, "swg_host_stepper_create: a chunk needs at "
+                               "least one level");
+    sum += levels[i];
+  }
+  if (sum != model->mesh->nlayers)
+    return fail(SWG_ERR_ARG, "swg_host_stepper_create: the chunks' levels "
+                             "must add up to the model's level count");
   swg_host_stepper hs = new (std::nothrow) swg_host_stepper_s();
   if (!hs)
     return fail(SWG_ERR_OOM, "swg_host_stepper_create: host allocation");
   hs->model = model;
   hs->K = model->mesh->nlayers;
   hs->T = model->params.ntracers;
-  const int kc = level_chunk <= 0 || level_chunk > hs->K ? hs->K : level_chunk;
-  for (int k0 = 0; k0 < hs->K; k0 += kc) {
+  for (int i = 0, k0 = 0; i < nchunks; k0 += levels[i++]) {
     Chunk c;
     c.k0 = k0;
-    c.kc = std::min(kc, hs->K - k0);
+    c.kc = levels[i];
     hs->chunks.push_back(c);
   }
   int rc = SWG_OK;
@@ -174,6 +184,20 @@ extern "C" int swg_host_stepper_create(swg_model model, int kind, int nstages,
   }
   *out = hs;
   return SWG_OK;
+}
+
+extern "C" int swg_host_stepper_create(swg_model model, int kind, int nstages,
+                                       int level_chunk,
+                                       swg_host_stepper *out) {
+  if (!model || !out)
+    return fail(SWG_ERR_ARG, "swg_host_stepper_create: NULL argument");
+  const int K = model->mesh->nlayers;
+  const int kc = level_chunk <= 0 || level_chunk > K ? K : level_chunk;
+  std::vector<int> levels;
+  for (int k0 = 0; k0 < K; k0 += kc)
+    levels.push_back(std::min(kc, K - k0));
+  return swg_host_stepper_create_levels(model, kind, nstages,
+                                        int(levels.size()), levels.data(), out);
 }
 
 extern "C" int swg_host_stepper_chunks(swg_host_stepper hs, int *levels,

@@ -505,12 +505,21 @@ class HostStepper:
     pinned_empty let the copies overlap.  stepper is "rk4" or "lsrk"."""
 
     def __init__(self, model: ShallowWaterModel, stepper: str = "lsrk",
-                 nstages: int = 5, level_chunk: int = 0):
+                 nstages: int = 5, level_chunk: int = 0, levels=None):
+        """level_chunk: levels per chunk (0: one chunk); or levels: the
+        chunk sizes one by one, adding up to the level count."""
         self.model = model
         h = C.c_void_p()
-        check(lib().swg_host_stepper_create(
-            model.handle, 0 if stepper == "rk4" else 1, int(nstages),
-            int(level_chunk), C.byref(h)))
+        kind = 0 if stepper == "rk4" else 1
+        if levels is not None:
+            arr = (C.c_int * len(levels))(*[int(n) for n in levels])
+            check(lib().swg_host_stepper_create_levels(
+                model.handle, kind, int(nstages), len(levels), arr,
+                C.byref(h)))
+        else:
+            check(lib().swg_host_stepper_create(
+                model.handle, kind, int(nstages), int(level_chunk),
+                C.byref(h)))
         self._h = h
 
     @property

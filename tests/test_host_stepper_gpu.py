@@ -62,6 +62,25 @@ def test_bitwise_equal_to_device_stepper(kind, nstages, chunk, want_chunks):
     assert_bitwise(got, want2)
 
 
+def test_explicit_chunk_sizes():
+    mesh = og.PlanarHexagonalMesh(WL.nx, WL.ny, WL.dc, WL.nlayers)
+    params = WL.params()
+    model = og.ShallowWaterModel(mesh, params)
+    x = initial_state(mesh, WL)
+    want = device_run(model, mesh, params, x, "lsrk", 5, 0.0, WL.dt, 2)
+    for levels in ([1, 5, 1], [2, 2, 3], [7]):
+        hs = og.HostStepper(model, "lsrk", 5, levels=levels)
+        assert hs.chunks == levels
+        arrs = hs.pinned_state()
+        for a, b in zip(arrs, x):
+            a[...] = b
+        hs.step(*arrs, 0.0, WL.dt, 2)
+        assert_bitwise(arrs, want)
+    for bad in ([3, 3], [4, 4], [0, 7], [-1, 8]):
+        with pytest.raises(og.SwgError):
+            og.HostStepper(model, "lsrk", 5, levels=bad)
+
+
 def test_pageable_arrays_no_tracers_and_zero_steps():
     wl = WL.scaled(ntracers=0)
     mesh = og.PlanarHexagonalMesh(wl.nx, wl.ny, wl.dc, wl.nlayers)
