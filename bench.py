@@ -49,9 +49,11 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="lsrk5_512x512")
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--level-chunk", type=int, default=16,
+    ap.add_argument("--level-chunk", type=int, default=-1,
                     help="levels per chunk of the host-state stepper that "
-                         "the end-to-end number goes through")
+                         "the end-to-end number goes through (-1: the "
+                         "fastest of one chunk, 32, 16 and 8 levels on this "
+                         "machine)")
     ap.add_argument("--levels", default="",
                     help="chunk sizes of the host-state stepper, comma "
                          "separated (overrides --level-chunk)")
@@ -408,10 +410,15 @@ def run_ours(args, wl):
     # chunks' compute), and beside it the serial upload + step + download
     e2e = None
     if not args.no_e2e:
-        hs = og.HostStepper(
-            model, wl.stepper, wl.nstages, args.level_chunk,
-            levels=[int(n) for n in args.levels.split(",")] if args.levels
-            else None)
+        tuning = None
+        if args.levels or args.level_chunk >= 0:
+            hs = og.HostStepper(
+                model, wl.stepper, wl.nstages, max(args.level_chunk, 0),
+                levels=[int(n) for n in args.levels.split(",")]
+                if args.levels else None)
+        else:
+            hs, tuning = og.HostStepper.autotuned(
+                model, wl.stepper, wl.nstages, (h0, vn0, tr0), wl.dt)
         hh, vv, tt = hs.pinned_state()
         hh[...], vv[...], tt[...] = h0, vn0, tr0
         nbytes_in = hh.nbytes + vv.nbytes + tt.nbytes
@@ -440,6 +447,8 @@ def run_ours(args, wl):
                "ms_per_step": e2e_ms / args.e2e_steps,
                "api": "swg_host_step (HostStepper), page-locked host arrays",
                "level_chunks": hs.chunks,
+               "chunk_tuning_ms_per_step": tuning and {
+                   str(k): round(v, 2) for k, v in tuning.items()},
                "serial_upload_step_download": {
                    "value": ups / (serial_ms / 1e3),
                    "ms_per_step": serial_ms / args.e2e_steps}}

@@ -522,6 +522,40 @@ class HostStepper:
                 C.byref(h)))
         self._h = h
 
+    @classmethod
+    def autotuned(cls, model: ShallowWaterModel, stepper: str = "lsrk",
+                  nstages: int = 5, state=None, dt: float = 1.0,
+                  candidates=(0, 32, 16, 8), reps: int = 2):
+        """The stepper whose level chunk (0: one chunk) steps fastest on
+        this machine, and {chunk: ms per step}.  Each candidate is timed
+        (host wall clock, the call being synchronous) over `reps` one-step
+        calls after one untimed call, on page-locked copies of `state` =
+        (h, vn, tr) host arrays, which are left unchanged.  The fastest layout
+        depends on the host link (2-D copies of short level rows run below
+        the contiguous rate on some links)."""
+        import time
+        K = model.m_mesh.m_nlayers
+        best, table = None, {}
+        for c in dict.fromkeys(min(int(c), K) if c > 0 else 0
+                               for c in candidates):
+            hs = cls(model, stepper, nstages, c)
+            arrs = hs.pinned_state()
+            if state is not None:
+                for a, b in zip(arrs, state):
+                    if a.size:
+                        a[...] = b
+            else:
+                for a in arrs:
+                    a.fill(1.0)
+            hs.step(*arrs, 0.0, dt, 1)
+            t0 = time.perf_counter()
+            for _ in range(reps):  # one call per step: copies every step
+                hs.step(*arrs, 0.0, dt, 1)
+            table[c] = (time.perf_counter() - t0) * 1e3 / reps
+            if best is None or table[c] < table[best[0]]:
+                best = (c, hs)
+        return best[1], table
+
     @property
     def chunks(self):
         """Levels of each chunk."""

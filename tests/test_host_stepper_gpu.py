@@ -170,3 +170,25 @@ def test_full_size_workload_one_step():
     got, hs = host_run(model, x, "lsrk", 5, 16, 0.0, wl.dt, 1)
     assert hs.chunks == [16] * 4
     assert_bitwise(got, want)
+
+
+def test_autotuned_picks_a_timed_candidate_and_leaves_the_state():
+    mesh = og.PlanarHexagonalMesh(WL.nx, WL.ny, WL.dc, WL.nlayers)
+    params = WL.params()
+    model = og.ShallowWaterModel(mesh, params)
+    x = initial_state(mesh, WL)
+    keep = tuple(a.copy() for a in x)
+    hs, table = og.HostStepper.autotuned(model, "lsrk", 5, x, WL.dt,
+                                         candidates=(0, 4, 2, 50))
+    assert set(table) == {0, 4, 2, 7}
+    best = min(table, key=table.get)
+    assert sum(hs.chunks) == WL.nlayers
+    assert hs.chunks == ([WL.nlayers] if best in (0, 7) else
+                         og.HostStepper(model, "lsrk", 5, best).chunks)
+    assert_bitwise(x, keep)
+    want = device_run(model, mesh, params, x, "lsrk", 5, 0.0, WL.dt, 2)
+    arrs = hs.pinned_state()
+    for a, b in zip(arrs, x):
+        a[...] = b
+    hs.step(*arrs, 0.0, WL.dt, 2)
+    assert_bitwise(arrs, want)
