@@ -93,6 +93,19 @@ def test_null_handles_are_errors_not_crashes():
     assert lib.swg_step(None, None, 0.0, 1.0, 1, 0, None) == 1
     assert lib.swg_compute_tendency(None, None, None, 0.0, 0, None) == 1
     assert lib.swg_mesh_destroy(None) == 0
+    # host-resident states
+    out = C.c_void_p()
+    assert lib.swg_host_stepper_create(None, 1, 5, 16, C.byref(out)) == 1
+    assert not out.value
+    levels = (C.c_int * 2)(3, 4)
+    assert lib.swg_host_stepper_create_levels(None, 1, 5, 2, levels,
+                                              C.byref(out)) == 1
+    assert lib.swg_host_step(None, None, None, None, 0.0, 1.0, 1, None) == 1
+    n = C.c_int(0)
+    assert lib.swg_host_stepper_chunks(None, None, C.byref(n)) == 1
+    assert lib.swg_host_stepper_destroy(None) == 0
+    assert lib.swg_host_alloc(8, None) == 1
+    assert lib.swg_host_free(None) == 0
 
 
 def test_checkpoint_cost_matches_binomial_formula():
