@@ -493,13 +493,6 @@ struct swg_adjoint_s {
 
 namespace {
 
-#define TRY(x)                                                                 \
-  do {                                                                         \
-    int rc_ = (x);                                                             \
-    if (rc_ != SWG_OK)                                                         \
-      return rc_;                                                              \
-  } while (0)
-
 template <class T>
 int up(std::vector<void *> &allocs, const std::vector<T> &h, const T **d) {
   void *p = nullptr;

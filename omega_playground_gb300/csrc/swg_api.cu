@@ -63,13 +63,6 @@ void free_all(std::vector<void *> &allocs) {
   allocs.clear();
 }
 
-#define TRY(x)                                                                 \
-  do {                                                                         \
-    int rc_ = (x);                                                             \
-    if (rc_ != SWG_OK)                                                         \
-      return rc_;                                                              \
-  } while (0)
-
 bool in_range(const int *a, size_t n, int lo, int hi) {
   for (size_t i = 0; i < n; ++i)
     if (a[i] < lo || a[i] >= hi)

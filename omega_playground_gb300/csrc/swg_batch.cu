@@ -207,13 +207,6 @@ struct swg_batch_s {
 
 namespace {
 
-#define TRY(x)                                                                 \
-  do {                                                                         \
-    int rc_ = (x);                                                             \
-    if (rc_ != SWG_OK)                                                         \
-      return rc_;                                                              \
-  } while (0)
-
 void pass_units(const swg_model md, unsigned units[NPASS], unsigned &base) {
   const ModelView &p = md->view;
   const long long K = md->mesh->nlayers, C = md->mesh->ncells,

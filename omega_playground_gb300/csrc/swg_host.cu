@@ -19,13 +19,6 @@
 #include <new>
 #include <vector>
 
-#define TRY(x)                                                                 \
-  do {                                                                         \
-    int rc_ = (x);                                                             \
-    if (rc_ != SWG_OK)                                                         \
-      return rc_;                                                              \
-  } while (0)
-
 using namespace swg;
 
 namespace {

@@ -16,6 +16,15 @@ namespace swg {
 int fail(int code, const std::string &msg);
 // Maps a CUDA error to SWG_ERR_CUDA (or SWG_ERR_OOM) with context.
 int cuda_fail(cudaError_t err, const char *what);
+
+// Return the status of a call that failed (anything but SWG_OK).
+#define TRY(x)                                                                 \
+  do {                                                                         \
+    int rc_ = (x);                                                             \
+    if (rc_ != SWG_OK)                                                         \
+      return rc_;                                                              \
+  } while (0)
+
 int build_planar_hex(int nx, int ny, double dc, swg_hex_tables *t,
                      double *period_x, double *period_y);
 
