@@ -200,6 +200,12 @@ struct PlanarHexagonalMesh : MPASMesh {
   Int m_nx, m_ny;
   Real m_dc, m_period_x, m_period_y;
 
+  // True for odd ny: the half-cell shift of alternate rows does not
+  // alternate across the periodic y boundary, so the reference's parallel
+  // construction writes some table slots twice (a race) and the rows meet
+  // irregularly there.  The tables are the reference's serial result.
+  bool odd_row_seam() const { return m_ny % 2 == 1; }
+
   PlanarHexagonalMesh(Int nx, Int ny, Int nlayers = 1)
       : PlanarHexagonalMesh(nx, ny, 1. / nx, nlayers) {}
   PlanarHexagonalMesh(Int nx, Int ny, Real dc, Int nlayers = 1)

@@ -165,6 +165,15 @@ class PlanarHexagonalMesh(MPASMesh):
         self.m_period_x, self.m_period_y = px.value, py.value
         self.finalize(**finalize_kw)
 
+    @property
+    def odd_row_seam(self) -> bool:
+        """True for odd ny: the half-cell shift of alternate rows does not
+        alternate across the periodic y boundary, so the reference's
+        parallel construction writes some table slots twice (a race) and
+        the rows meet irregularly there.  The tables are the reference's
+        serial result."""
+        return self.m_ny % 2 == 1
+
 
 @dataclasses.dataclass
 class ShallowWaterParams:

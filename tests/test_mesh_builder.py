@@ -100,3 +100,12 @@ def test_operator_convergence_on_tables():
         e = errs[name]
         rate = np.log2(e[-2] / e[-1])
         assert abs(rate - expect) < 0.05, (name, e, rate)
+
+
+def test_odd_row_seam_flag():
+    """Odd ny is flagged on the mesh classes (the reference races there)."""
+    from omega_playground_gb300.shallow_water import PlanarHexagonalMesh
+    assert PlanarHexagonalMesh.odd_row_seam.fget(
+        type("M", (), {"m_ny": 29})())
+    assert not PlanarHexagonalMesh.odd_row_seam.fget(
+        type("M", (), {"m_ny": 28})())
