@@ -1445,6 +1445,9 @@ extern "C" int swg_adj_backward(swg_adjoint ad, swg_state lambda,
     return fail(SWG_ERR_ARG, "swg_adj_backward: bad argument");
   if (ad->state != 1)
     return fail(SWG_ERR_STATE, "swg_adj_backward: call swg_adj_forward first");
+  if (ad->model->terms_switched) // the re-advances would differ from the tape
+    return fail(SWG_ERR_STATE, "swg_adj_backward: a tendency term of the "
+                               "model was switched after swg_adj_forward");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   NvtxRange range("adjoint_backward_sweep");
   TRY(bwd_begin(ad, lambda, st));
@@ -1496,6 +1499,10 @@ extern "C" int swg_adj_batch_backward(int n, const swg_adjoint *adjs,
   for (int m = 0; m < n; ++m)
     if (!adjs[m] || !same_layout(adjs[m], lambdas[m]) || adjs[m]->state != 1)
       return fail(SWG_ERR_ARG, "swg_adj_batch_backward: member not ready");
+    else if (adjs[m]->model->terms_switched)
+      return fail(SWG_ERR_STATE, "swg_adj_batch_backward: a tendency term of "
+                                 "a member's model was switched after the "
+                                 "forward sweep");
   if (!distinct_members(n, adjs))
     return fail(SWG_ERR_ARG, "swg_adj_batch_backward: members must have "
                              "distinct adjoints and models");

@@ -160,3 +160,60 @@ def test_beta_plane_f_vertex_matches_oracle():
                     nstages=4)
     for g, w in zip(S.download(), want):
         assert rel_diff(g, w) <= TOL
+
+
+def test_switch_between_adjoint_forward_and_backward_is_an_error():
+    """The reverse sweep re-runs plain steps with the model's current terms
+    and replays the tape captured with the forward's: a switch in between
+    is refused; switching back restores the forward's set."""
+    mesh, params, model, _ = setup()
+    adj = og.Adjoint(model, 2)
+    x = state(mesh, 31)
+    X = og.ShallowWaterState(mesh, params)
+    X.upload(*x)
+    XN = og.ShallowWaterState(mesh, params)
+    adj.forward(X, 0.0, 20.0, 4, XN)
+    model.m_ke_grad_edge.m_enabled = False
+    LAM = og.ShallowWaterState(mesh, params)
+    LAM.upload(*state(mesh, 32))
+    with pytest.raises(og.SwgError, match="switched"):
+        adj.backward(LAM)
+    model.m_ke_grad_edge.m_enabled = True
+    adj.backward(LAM)
+
+
+def test_adjoint_with_beta_plane_f_vertex_dot_product():
+    """A written m_f_vertex enters the taped PV and its adjoint: tendency
+    and trajectory dot products against the tangent-linear model <= 1e-12."""
+    mesh, params, model, omd = setup()
+    om = omd.mesh
+    model.m_f_vertex = COEF["f0"] + 1.6e-11 * (om.y_vertex - 0.5 * om.period_y)
+    adj = og.Adjoint(model, 2)
+    x = state(mesh, 41)
+    dx = tuple(1e-3 * (uniform(50 + j, a.size).reshape(a.shape) - 0.5)
+               for j, a in enumerate(x))
+    mu = tuple(uniform(60 + j, a.size).reshape(a.shape) - 0.5
+               for j, a in enumerate(x))
+
+    def mk(a):
+        st = og.ShallowWaterState(mesh, params)
+        st.upload(*a)
+        return st
+
+    def dot(a, b):
+        return sum(float(np.sum(p * q)) for p, q in zip(a, b))
+
+    X = mk(x)
+    JD, JT = og.ShallowWaterState(mesh, params), og.ShallowWaterState(mesh, params)
+    adj.tlm_tendency(X, mk(dx), JD)
+    adj.adj_tendency(X, mk(mu), JT)
+    lhs, rhs = dot(JD.download(), mu), dot(dx, JT.download())
+    assert abs(lhs - rhs) <= TOL * max(abs(lhs), abs(rhs)), (lhs, rhs)
+    XN = og.ShallowWaterState(mesh, params)
+    adj.forward(X, 0.0, 20.0, 5, XN)
+    LAM = mk(mu)
+    adj.backward(LAM)
+    DX = mk(dx)
+    adj.tlm_apply(X, DX, 0.0, 20.0, 5)
+    lhs, rhs = dot(DX.download(), mu), dot(dx, LAM.download())
+    assert abs(lhs - rhs) <= TOL * max(abs(lhs), abs(rhs)), (lhs, rhs)
