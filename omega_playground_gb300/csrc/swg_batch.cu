@@ -195,6 +195,7 @@ struct swg_batch_s {
   BatchSync *d_sync = nullptr;
   std::vector<unsigned> prefix_h; // host copy of the prefix tables
   std::vector<Member> mem_h;
+  std::vector<unsigned long long> versions; // members' model versions built
   double dt_built = -1.0;
   int config = 0;
   int sms = 0;
@@ -255,7 +256,34 @@ StageArgs member_stage(const swg_batch_s *b, int m, int stage, double dt) {
   return a;
 }
 
+int upload_prefix(swg_batch b, unsigned vbsize);
+
+// A member's model switched a tendency term since its descriptor was built:
+// take its current view and pass sizes, and rebuild the prefix tables and
+// the step graph (both hold the pass sizes).
+int refresh_members(swg_batch b) {
+  bool changed = false;
+  for (int m = 0; m < b->nmem; ++m)
+    if (b->versions[m] != b->models[m]->version) {
+      Member &M = b->mem_h[m];
+      M.p = b->models[m]->view;
+      pass_units(b->models[m], M.units, M.aux2_base);
+      b->versions[m] = b->models[m]->version;
+      changed = true;
+    }
+  if (!changed)
+    return SWG_OK;
+  b->dt_built = -1.0;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  const LaunchConfig &c = kConfigs[b->config];
+  return upload_prefix(b, unsigned(c.block * c.items));
+}
+
 int upload_members(swg_batch b, double dt) {
+  TRY(refresh_members(b));
   if (b->dt_built == dt)
     return SWG_OK;
   for (int m = 0; m < b->nmem; ++m)
@@ -472,6 +500,7 @@ extern "C" int swg_batch_create(int nmembers, const swg_model *models,
     M.p = models[m]->view;
     M.a = models[m]->aux;
     pass_units(models[m], M.units, M.aux2_base);
+    b->versions.push_back(models[m]->version);
   }
   cudaError_t err = cudaSuccess;
   if (rc == SWG_OK) {

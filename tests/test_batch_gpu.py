@@ -170,3 +170,41 @@ def test_tiny_members_match_single_instance_bitwise():
         for m, (a, b) in enumerate(zip(got, ref)):
             for x, y in zip(a, b):
                 np.testing.assert_array_equal(x, y, err_msg=f"config {cfg} member {m}")
+
+
+def test_term_switch_after_first_batch_step_is_followed():
+    """A member's model switches terms between batch steps (the reference's
+    m_enabled members): the batch takes the new set at its next step, graph
+    path included, bitwise equal to the single-instance stepper doing the
+    same."""
+    members = build_members(SMALL)
+    states = []
+    for mesh, params, model, ic in members:
+        st = og.ShallowWaterState(mesh, params)
+        st.upload(*ic)
+        states.append(st)
+    b = og.Batch([m[2] for m in members], states, "rk4", 4)
+    b.step(0.0, SMALL[0].dt, 2)
+    singles = []
+    for mesh, params, model, ic in members:
+        st = og.ShallowWaterState(mesh, params)
+        st.upload(*ic)
+        og.RK4Stepper(model).step(st, 0.0, SMALL[0].dt, 2, use_graph=False)
+        singles.append(st)
+    m1 = members[1][2]
+    m1.m_pv_flux_edge.m_enabled = False
+    m1.m_tracer_hadv_cell.m_enabled = False
+    members[3][2].m_vel_diff_edge.m_enabled = False
+    b.step(0.0, SMALL[0].dt, 3)
+    for (mesh, params, model, ic), st in zip(members, singles):
+        og.RK4Stepper(model).step(st, 0.0, SMALL[0].dt, 3, use_graph=False)
+    for m, (a, s) in enumerate(zip(states, singles)):
+        for x, y in zip(a.download(), s.download()):
+            assert np.all(np.isfinite(y))
+            np.testing.assert_array_equal(x, y, err_msg=f"member {m}")
+    # and back on
+    m1.m_pv_flux_edge.m_enabled = True
+    b.step(0.0, SMALL[0].dt, 1)
+    og.RK4Stepper(m1).step(singles[1], 0.0, SMALL[0].dt, 1, use_graph=False)
+    for x, y in zip(states[1].download(), singles[1].download()):
+        np.testing.assert_array_equal(x, y)
