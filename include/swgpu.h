@@ -348,7 +348,10 @@ int swg_batch_selftest_timeout(swg_batch batch, double limit_ms,
  *   swg_tlm_apply:   dx <- d x_N (propagated tangent of nsteps steps)
  *   swg_adj_forward: runs nsteps steps from state0 storing checkpoints,
  *                    writes x_N to final_out;
- *   swg_adj_backward: lambda (in: dL/dx_N) <- dL/dx_0. */
+ *   swg_adj_backward: lambda (in: dL/dx_N) <- dL/dx_0.
+ * The adjoint differentiates the terms the model had when it was created:
+ * while a term is switched (swg_model_set_term_enabled) every call below
+ * returns SWG_ERR_STATE. */
 int swg_adjoint_create(swg_model model, int nsnapshots, swg_adjoint *out);
 /* the same for another stepper: SWG_STEPPER_RK4 (nstages ignored) or
  * SWG_STEPPER_LSRK with nstages 5 or 1 (lsrk.cpp:16-33, 36-89) */

@@ -1242,6 +1242,10 @@ extern "C" int swg_adj_tendency(swg_adjoint ad, swg_state x, swg_state mu,
   if (!ad || !same_layout(ad, x) || !same_layout(ad, mu) ||
       !same_layout(ad, lambda_out))
     return fail(SWG_ERR_ARG, "swg_adj_tendency: bad argument");
+  if (ad->model->terms_switched)
+    return fail(SWG_ERR_STATE, "swg_adj_tendency: a tendency term of the "
+                               "model was switched after the adjoint was "
+                               "created");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   adj_tendency(ad, x->h, x->vn, x->tr, mu, lambda_out, st);
   cudaError_t err = cudaGetLastError();
@@ -1253,6 +1257,10 @@ extern "C" int swg_tlm_tendency(swg_adjoint ad, swg_state x, swg_state dx,
   if (!ad || !same_layout(ad, x) || !same_layout(ad, dx) ||
       !same_layout(ad, dtend_out))
     return fail(SWG_ERR_ARG, "swg_tlm_tendency: bad argument");
+  if (ad->model->terms_switched)
+    return fail(SWG_ERR_STATE, "swg_tlm_tendency: a tendency term of the "
+                               "model was switched after the adjoint was "
+                               "created");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   swg_model md = ad->model;
   const long long n = (long long)words(md);
@@ -1282,6 +1290,9 @@ extern "C" int swg_tlm_apply(swg_adjoint ad, swg_state x0, swg_state dx,
   (void)t0;
   if (!ad || !same_layout(ad, x0) || !same_layout(ad, dx) || nsteps < 0)
     return fail(SWG_ERR_ARG, "swg_tlm_apply: bad argument");
+  if (ad->model->terms_switched)
+    return fail(SWG_ERR_STATE, "swg_tlm_apply: a tendency term of the model "
+                               "was switched after the adjoint was created");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   swg_model md = ad->model;
   const ModelView &pv = md->view;

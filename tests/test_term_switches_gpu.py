@@ -178,6 +178,11 @@ def test_switch_between_adjoint_forward_and_backward_is_an_error():
     LAM.upload(*state(mesh, 32))
     with pytest.raises(og.SwgError, match="switched"):
         adj.backward(LAM)
+    for call in (lambda: adj.adj_tendency(X, LAM, XN),
+                 lambda: adj.tlm_tendency(X, LAM, XN),
+                 lambda: adj.tlm_apply(X, LAM, 0.0, 20.0, 1)):
+        with pytest.raises(og.SwgError, match="switched"):
+            call()
     model.m_ke_grad_edge.m_enabled = True
     adj.backward(LAM)
 
