@@ -52,8 +52,8 @@ def parse():
     ap.add_argument("--level-chunk", type=int, default=-1,
                     help="levels per chunk of the host-state stepper that "
                          "the end-to-end number goes through (-1: the "
-                         "fastest of one chunk, 32, 16 and 8 levels on this "
-                         "machine)")
+                         "fastest chunk layout on this machine, "
+                         "HostStepper.autotuned)")
     ap.add_argument("--levels", default="",
                     help="chunk sizes of the host-state stepper, comma "
                          "separated (overrides --level-chunk)")
@@ -448,7 +448,7 @@ def run_ours(args, wl):
                "api": "swg_host_step (HostStepper), page-locked host arrays",
                "level_chunks": hs.chunks,
                "chunk_tuning_ms_per_step": tuning and {
-                   str(k): round(v, 2) for k, v in tuning.items()},
+                   k: round(v, 2) for k, v in tuning.items()},
                "serial_upload_step_download": {
                    "value": ups / (serial_ms / 1e3),
                    "ms_per_step": serial_ms / args.e2e_steps}}

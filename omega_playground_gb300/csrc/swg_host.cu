@@ -16,6 +16,7 @@
 #include "swg_internal.h"
 
 #include <algorithm>
+#include <cstddef>
 #include <new>
 #include <vector>
 
@@ -76,11 +77,63 @@ cudaError_t copy_levels(double *dst, size_t dpitch, const double *src,
                            kind, st);
 }
 
+// Levels [k0, k0 + kc) of `rows` rows of K levels between host memory
+// mapped into the device address space and a dense [rows][kc] device array,
+// moved by the SMs.  The copy engines move rows of a few levels at a
+// fraction of the link rate (64-byte rows at about half of it); a grid of
+// threads issuing the rows together runs near the full rate.  Every index
+// stays inside its array: r*K + k0 + j < rows*K because k0 + kc <= K.
+__global__ void k_levels_in(double *__restrict__ dst,
+                            const double *__restrict__ host, long long rows,
+                            int K, int k0, int kc) {
+  const long long n = rows * kc;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long r = i / kc;
+    dst[i] = host[r * K + k0 + (i - r * kc)];
+  }
+}
+
+__global__ void k_levels_out(double *__restrict__ host,
+                             const double *__restrict__ src, long long rows,
+                             int K, int k0, int kc) {
+  const long long n = rows * kc;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long r = i / kc;
+    host[r * K + k0 + (i - r * kc)] = src[i];
+  }
+}
+
+// The device address of a host array of n doubles when the whole array is
+// page-locked memory mapped into the device address space (cudaHostAlloc,
+// or cudaHostRegister with mapping): both ends are mapped host memory at the
+// same offset.  nullptr otherwise (pageable or managed memory), which keeps
+// those arrays on the copy engines.
+double *mapped(double *p, size_t n) {
+  if (!p || n == 0)
+    return nullptr;
+  cudaPointerAttributes a{}, b{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess ||
+      cudaPointerGetAttributes(&b, p + (n - 1)) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || b.type != cudaMemoryTypeHost ||
+      !a.devicePointer || !b.devicePointer ||
+      static_cast<double *>(b.devicePointer) -
+              static_cast<double *>(a.devicePointer) !=
+          std::ptrdiff_t(n - 1))
+    return nullptr;
+  return static_cast<double *>(a.devicePointer);
+}
+
 } // namespace
 
 struct swg_host_stepper_s {
   swg_model model = nullptr;
   int K = 0, T = 0;
+  int copy_grid = 0; // blocks of the SM copies (8 per SM)
   std::vector<Chunk> chunks;
   cudaStream_t h2d = nullptr, comp = nullptr, d2h = nullptr;
   cudaEvent_t go = nullptr, done = nullptr;
@@ -165,6 +218,10 @@ extern "C" int swg_host_stepper_create_levels(swg_model model, int kind,
       return rc;
     }
   cudaError_t err = cudaSuccess;
+  int dev = 0, sms = 0;
+  if ((err = cudaGetDevice(&dev)) == cudaSuccess)
+    err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  hs->copy_grid = 8 * std::max(sms, 1);
   for (cudaStream_t *s : {&hs->h2d, &hs->comp, &hs->d2h})
     if (err == cudaSuccess)
       err = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
@@ -214,6 +271,32 @@ static int host_step(swg_host_stepper hs, double *h, double *vn, double *tr,
                TC = size_t(hs->T) * C;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   NvtxRange range("host_step");
+  // The first chunk's copy-in precedes all compute and the last chunk's
+  // copy-out follows it, so the SMs are idle then: those two go through the
+  // SM copies when the arrays are mapped page-locked memory.  The other
+  // chunks' copies overlap compute and stay on the copy engines.
+  double *mh = mapped(h, C * K), *mv = mapped(vn, E * K),
+         *mt = TC ? mapped(tr, TC * K) : nullptr;
+  const bool sm_copies = mh && mv && (mt || !TC);
+  auto levels_in = [&](double *dst, const double *host, size_t rows, int k0,
+                       int kc) {
+    if (rows == 0)
+      return cudaSuccess;
+    k_levels_in<<<hs->copy_grid, 256, 0, hs->h2d>>>(dst, host, (long long)rows,
+                                                    int(K), k0, kc);
+    ++g_launches;
+    return cudaGetLastError();
+  };
+  auto levels_out = [&](double *host, const double *src, size_t rows, int k0,
+                        int kc) {
+    if (rows == 0)
+      return cudaSuccess;
+    k_levels_out<<<hs->copy_grid, 256, 0, hs->d2h>>>(host, src,
+                                                     (long long)rows, int(K),
+                                                     k0, kc);
+    ++g_launches;
+    return cudaGetLastError();
+  };
   cudaError_t err = cudaEventRecord(hs->go, st);
   for (cudaStream_t s : {hs->h2d, hs->comp, hs->d2h})
     if (err == cudaSuccess)
@@ -221,15 +304,24 @@ static int host_step(swg_host_stepper hs, double *h, double *vn, double *tr,
   // copies in, back to back on the copy-in stream
   for (Chunk &c : hs->chunks) {
     const int kc = c.kc;
-    if (err == cudaSuccess)
-      err = copy_levels(c.state->h, kc, h + c.k0, K, kc, C,
-                        cudaMemcpyHostToDevice, hs->h2d);
-    if (err == cudaSuccess)
-      err = copy_levels(c.state->vn, kc, vn + c.k0, K, kc, E,
-                        cudaMemcpyHostToDevice, hs->h2d);
-    if (err == cudaSuccess && TC)
-      err = copy_levels(c.state->tr, kc, tr + c.k0, K, kc, TC,
-                        cudaMemcpyHostToDevice, hs->h2d);
+    if (sm_copies && &c == &hs->chunks.front()) {
+      if (err == cudaSuccess)
+        err = levels_in(c.state->h, mh, C, c.k0, kc);
+      if (err == cudaSuccess)
+        err = levels_in(c.state->vn, mv, E, c.k0, kc);
+      if (err == cudaSuccess && TC)
+        err = levels_in(c.state->tr, mt, TC, c.k0, kc);
+    } else {
+      if (err == cudaSuccess)
+        err = copy_levels(c.state->h, kc, h + c.k0, K, kc, C,
+                          cudaMemcpyHostToDevice, hs->h2d);
+      if (err == cudaSuccess)
+        err = copy_levels(c.state->vn, kc, vn + c.k0, K, kc, E,
+                          cudaMemcpyHostToDevice, hs->h2d);
+      if (err == cudaSuccess && TC)
+        err = copy_levels(c.state->tr, kc, tr + c.k0, K, kc, TC,
+                          cudaMemcpyHostToDevice, hs->h2d);
+    }
     if (err == cudaSuccess)
       err = cudaEventRecord(c.in, hs->h2d);
   }
@@ -258,6 +350,15 @@ static int host_step(swg_host_stepper hs, double *h, double *vn, double *tr,
     const int kc = c.kc;
     if (err == cudaSuccess)
       err = cudaStreamWaitEvent(hs->d2h, c.out, 0);
+    if (sm_copies && &c == &hs->chunks.back()) {
+      if (err == cudaSuccess)
+        err = levels_out(mh, c.state->h, C, c.k0, kc);
+      if (err == cudaSuccess)
+        err = levels_out(mv, c.state->vn, E, c.k0, kc);
+      if (err == cudaSuccess && TC)
+        err = levels_out(mt, c.state->tr, TC, c.k0, kc);
+      continue;
+    }
     if (err == cudaSuccess)
       err = copy_levels(h + c.k0, K, c.state->h, kc, kc, C,
                         cudaMemcpyDeviceToHost, hs->d2h);
@@ -293,7 +394,8 @@ extern "C" int swg_host_alloc(unsigned long long bytes, void **out) {
   if (!out)
     return fail(SWG_ERR_ARG, "swg_host_alloc: NULL argument");
   *out = nullptr;
-  cudaError_t err = cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocDefault);
+  cudaError_t err = cudaHostAlloc(out, bytes ? bytes : 1,
+                                  cudaHostAllocMapped | cudaHostAllocPortable);
   if (err != cudaSuccess) {
     *out = nullptr;
     return cuda_fail(err, "swg_host_alloc");

@@ -531,23 +531,48 @@ class HostStepper:
                 C.byref(h)))
         self._h = h
 
+    @staticmethod
+    def edge_layout(nlayers: int, chunk: int, edge: int):
+        """Chunk sizes with `edge` levels first and last and chunks of
+        `chunk` levels between them (the last of those ragged): the small
+        end chunks shorten the copy-in before the first compute and the
+        copy-out after the last."""
+        K, c, e = int(nlayers), int(chunk), int(edge)
+        if K <= 2 * e or c < 1:
+            return [K]
+        mid = [min(c, K - 2 * e - k) for k in range(0, K - 2 * e, c)]
+        return [e] + mid + [e]
+
     @classmethod
     def autotuned(cls, model: ShallowWaterModel, stepper: str = "lsrk",
                   nstages: int = 5, state=None, dt: float = 1.0,
-                  candidates=(0, 32, 16, 8), reps: int = 2):
-        """The stepper whose level chunk (0: one chunk) steps fastest on
-        this machine, and {chunk: ms per step}.  Each candidate is timed
-        (host wall clock, the call being synchronous) over `reps` one-step
-        calls after one untimed call, on page-locked copies of `state` =
-        (h, vn, tr) host arrays, which are left unchanged.  The fastest layout
-        depends on the host link (2-D copies of short level rows run below
-        the contiguous rate on some links)."""
+                  candidates=None, reps: int = 2):
+        """The stepper whose chunk layout steps fastest on this machine,
+        and {layout: ms per step}.  A candidate is a level chunk (int, 0:
+        one chunk) or a list of chunk sizes; the default tries one chunk,
+        chunks of 32, 16 and 8, and chunks of 16 or 32 between end chunks of
+        4 or 8 levels.  Each candidate is timed (host wall clock, the call
+        being synchronous) over `reps` one-step calls after one untimed
+        call, on page-locked copies of `state` = (h, vn, tr) host arrays,
+        which are left unchanged.  The fastest layout depends on the host
+        link."""
         import time
         K = model.m_mesh.m_nlayers
+        if candidates is None:
+            candidates = [0, 32, 16, 8] + [cls.edge_layout(K, c, e)
+                                           for c, e in ((16, 4), (16, 8),
+                                                        (32, 8))]
+        layouts = {}
+        for c in candidates:
+            if isinstance(c, (list, tuple)):
+                layout = [int(n) for n in c]
+            else:
+                c = min(int(c), K) if c > 0 else K
+                layout = [min(c, K - k) for k in range(0, K, c)]
+            layouts[",".join(map(str, layout))] = layout
         best, table = None, {}
-        for c in dict.fromkeys(min(int(c), K) if c > 0 else 0
-                               for c in candidates):
-            hs = cls(model, stepper, nstages, c)
+        for key, layout in layouts.items():
+            hs = cls(model, stepper, nstages, levels=layout)
             arrs = hs.pinned_state()
             if state is not None:
                 for a, b in zip(arrs, state):
@@ -560,9 +585,9 @@ class HostStepper:
             t0 = time.perf_counter()
             for _ in range(reps):  # one call per step: copies every step
                 hs.step(*arrs, 0.0, dt, 1)
-            table[c] = (time.perf_counter() - t0) * 1e3 / reps
-            if best is None or table[c] < table[best[0]]:
-                best = (c, hs)
+            table[key] = (time.perf_counter() - t0) * 1e3 / reps
+            if best is None or table[key] < table[best[0]]:
+                best = (key, hs)
         return best[1], table
 
     @property

@@ -126,3 +126,12 @@ def test_checkpoint_cost_matches_binomial_formula():
     assert lib.swg_checkpoint_cost(10001, 32) == -1
     assert lib.swg_checkpoint_cost(0, 32) == -1
     assert lib.swg_checkpoint_cost(10, 0) == -1
+
+
+def test_host_stepper_edge_layout():
+    """Chunk layouts with small end chunks (host-state stepper autotuning)."""
+    import omega_playground_gb300 as og
+    assert og.HostStepper.edge_layout(64, 16, 8) == [8, 16, 16, 16, 8]
+    assert og.HostStepper.edge_layout(64, 16, 4) == [4, 16, 16, 16, 8, 4]
+    assert og.HostStepper.edge_layout(7, 3, 1) == [1, 3, 2, 1]
+    assert og.HostStepper.edge_layout(6, 3, 3) == [6]
