@@ -274,7 +274,11 @@ int swg_step(swg_stepper stepper, swg_state state, double t0, double dt,
  * slice of the model.  The chunks are pipelined on three streams: chunk c+1
  * is copied in while chunk c is computed and chunk c-1 is copied out.
  * Copies overlap only from page-locked host memory (swg_host_alloc or
- * cudaHostAlloc); pageable arrays work but serialise.
+ * cudaHostAlloc); pageable arrays work but serialise.  When the arrays are
+ * mapped into the device address space (swg_host_alloc, cudaHostAlloc
+ * under unified addressing), the first chunk's copy-in and the last
+ * chunk's copy-out, which no compute overlaps, run as SM copy kernels,
+ * which move short level rows several times faster than the copy engines.
  * Results are bitwise equal to swg_state_upload + swg_step + swg_state_download
  * on the same model.  Each call reads the model's term switches and its
  * f_vertex.  The model must have no forcing hook, because the hook would see
