@@ -43,7 +43,7 @@ constexpr int ATPB = 256;
 struct AdjView {
   // cells [C][6]
   const double *ccdh_nb, *ckq_nb, *kd2_nb, *r4_nb; // neighbour's coefficient
-  const double *keadj, *d4adj, *hsadj, *divadj;    // transposed edge terms
+  const double *keadj, *d4adj, *divadj;    // transposed edge terms
   const int *cvtx;                                 // vertices of the cell
   const double *ckvh;                              // their kite weight for c
   const double *hm_c;                              // 0.5 on edges, 0 on padding
@@ -60,7 +60,7 @@ struct AdjView {
 
 struct AdjWork {
   double *lL, *ln;                      // [T][C][K]
-  double *lke, *ld4, *lhs, *lhtr, *ldiv; // [C][K]
+  double *lke, *ld4, *lhtr, *ldiv; // [C][K]
   double *lz4, *lzeta, *lhv;            // [V][K]
   double *lQ, *lmh, *lvnp, *ld2u;       // [E][K]
   double *Qmu;                          // [E][K] Q mu_vn of the stage
@@ -124,16 +124,16 @@ __global__ void __launch_bounds__(ATPB)
   }
   i -= VK;
   const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
-  double ke = 0, d4 = 0, hs = 0;
+  // the SSH gradient's transpose is g times the kinetic-energy gradient's
+  // (both are -(x_1 - x_0)/dc per edge), applied where lke is read
+  double ke = 0, d4 = 0;
   for (int j = 0; j < MAXE; ++j) {
     const double mu = io.mvn[size_t(__ldg(m.ec + 6 * c + j)) * K + k];
     ke = fma(__ldg(v.keadj + 6 * c + j), mu, ke);
-    hs = fma(__ldg(v.hsadj + 6 * c + j), mu, hs);
     if (p.vel_del4)
       d4 = fma(__ldg(v.d4adj + 6 * c + j), mu, d4);
   }
   w.lke[i] = ke;
-  w.lhs[i] = hs;
   if (p.vel_del4)
     w.ld4[i] = d4;
 }
@@ -380,7 +380,7 @@ __global__ void __launch_bounds__(ATPB)
     }
   }
   if (p.do_vn)
-    lh += w.lhs[i];
+    lh = fma(p.grav, w.lke[i], lh); // SSH gradient: g times the KE term
   if (p.ntracers > 0)
     lh += w.lhtr[i];
   emit(io, io.lh, io.acc_h, io.nmu_h, io.lam_h, io.mh_, i, lh);
@@ -555,7 +555,7 @@ int build_tables(swg_adjoint ad) {
   const swg_params &P = md->params;
   const int C = me->ncells, E = me->nedges, V = me->nvertices;
   std::vector<double> ccdh_nb(6 * C, 0), ckq_nb(6 * C, 0), kd2_nb(6 * C, 0),
-      r4_nb(6 * C, 0), keadj(6 * C, 0), d4adj(6 * C, 0), hsadj(6 * C, 0),
+      r4_nb(6 * C, 0), keadj(6 * C, 0), d4adj(6 * C, 0),
       divadj(6 * C, 0), ckvh(6 * C, 0);
   std::vector<int> cvtx(6 * C, 0);
   std::vector<double> ccd_e2(2 * E), ccdh_e2(2 * E), cke_e2(2 * E),
@@ -591,7 +591,6 @@ int build_tables(swg_adjoint ad) {
       r4_nb[6 * c + j] = r4(n, jn);
       const double sg = side == 0 ? 1.0 : -1.0;
       keadj[6 * c + j] = sg * me->inv_dc_h[e];
-      hsadj[6 * c + j] = sg * (P.grav * me->inv_dc_h[e]);
       d4adj[6 * c + j] = -(sg * (-(P.visc_del4 * me->scale4_h[e])) * me->inv_dc_h[e]);
       divadj[6 * c + j] = -(sg * me->inv_dc_h[e]);
     }
@@ -669,7 +668,7 @@ int build_tables(swg_adjoint ad) {
   if ((rc = up(A, ccdh_nb, &a.ccdh_nb)) || (rc = up(A, ckq_nb, &a.ckq_nb)) ||
       (rc = up(A, kd2_nb, &a.kd2_nb)) || (rc = up(A, r4_nb, &a.r4_nb)) ||
       (rc = up(A, keadj, &a.keadj)) || (rc = up(A, d4adj, &a.d4adj)) ||
-      (rc = up(A, hsadj, &a.hsadj)) || (rc = up(A, divadj, &a.divadj)) ||
+      (rc = up(A, divadj, &a.divadj)) ||
       (rc = up(A, cvtx, &a.cvtx)) || (rc = up(A, ckvh, &a.ckvh)) ||
       (rc = up(A, ccd_e2, &a.ccd_e2)) || (rc = up(A, ccdh_e2, &a.ccdh_e2)) ||
       (rc = up(A, cke_e2, &a.cke_e2)) || (rc = up(A, ckq_e2, &a.ckq_e2)) ||
@@ -1149,7 +1148,7 @@ extern "C" int swg_adjoint_create_stepper(swg_model md, int nsnapshots,
   if (rc == SWG_OK &&
       ((rc = zal(A, T * C * K, &w.lL)) || (rc = zal(A, T * C * K, &w.ln)) ||
        (rc = zal(A, C * K, &w.lke)) || (rc = zal(A, C * K, &w.ld4)) ||
-       (rc = zal(A, C * K, &w.lhs)) || (rc = zal(A, C * K, &w.lhtr)) ||
+       (rc = zal(A, C * K, &w.lhtr)) ||
        (rc = zal(A, C * K, &w.ldiv)) || (rc = zal(A, V * K, &w.lz4)) ||
        (rc = zal(A, V * K, &w.lzeta)) || (rc = zal(A, V * K, &w.lhv)) ||
        (rc = zal(A, E * K, &w.lQ)) || (rc = zal(A, E * K, &w.lmh)) ||
