@@ -98,3 +98,31 @@ def test_reference_arm_runs_on_rank_zero_only():
     line = json.loads(got[0].strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_reference_arm_json_line(capsys, monkeypatch):
+    """The reference arm's single JSON line on a small workload: the keys
+    the contract names, impl "reference", cpu_baseline and a zero-copy
+    e2e with the line's own value and unit."""
+    import json
+    import types
+    sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle")]
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        monkeypatch.delenv(k, raising=False)
+    import bench
+    from omega_playground_gb300.workloads import WORKLOADS
+    wl = WORKLOADS["lsrk5_512x512"].scaled(nx=8, ny=8, nlayers=4, ntracers=2)
+    args = types.SimpleNamespace(gpus=1, steps=2, warmup=1)
+    bench.run_reference(args, wl)
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup",
+                "ms_per_step", "higher_is_better", "scaling", "vs_baseline",
+                "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["steps"] == 2 and line["warmup"] == 1
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"]
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"],
+                           "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert line["config"]["workload"] == wl.name
