@@ -875,6 +875,21 @@ int tape_step(swg_adjoint ad, double dt, swg_state out, cudaStream_t st) {
   static const double rkb[4] = {1. / 6, 1. / 3, 1. / 3, 1. / 6};
   swg_state S = ad->X[0];
   const int last = out ? 3 : 2;
+  if (out) {
+    // a field whose tendency is disabled ends the step as it began; the
+    // stage epilogues write only the enabled fields of `out`
+    const size_t CK = size_t(md->mesh->ncells) * md->mesh->nlayers,
+                 EK = size_t(md->mesh->nedges) * md->mesh->nlayers;
+    cudaError_t e = cudaSuccess;
+    if (!pv.do_h)
+      e = cudaMemcpyAsync(out->h, S->h, CK * sizeof(double),
+                          cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess && !pv.do_vn)
+      e = cudaMemcpyAsync(out->vn, S->vn, EK * sizeof(double),
+                          cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess)
+      return cuda_fail(e, "swg_adjoint: taped step");
+  }
   for (int s = 0; s <= last; ++s) {
     StageArgs a{};
     const double *h, *vn, *tr;

@@ -67,6 +67,15 @@ SCENARIOS = {
                          nsteps=3, dt=20.0, f0=1e-4, grav=9.81,
                          visc_del2=1e3, visc_del4=1e9, eddy_diff2=1e3,
                          eddy_diff4=1e9, seed=19),
+    # one field frozen: h (RK4 stage inputs keep the step's h) and vn
+    "frozen_h_rk4": dict(nx=8, ny=6, dc=1e4, K=3, T=2, stepper="rk4",
+                         nsteps=3, dt=20.0, f0=1e-4, grav=9.81,
+                         visc_del2=1e3, visc_del4=1e9, eddy_diff2=1e3,
+                         eddy_diff4=1e9, disable_h=1, seed=20),
+    "frozen_vn_lsrk5": dict(nx=6, ny=8, dc=1e4, K=2, T=2, stepper="lsrk5",
+                            nsteps=3, dt=20.0, f0=1e-4, grav=9.81,
+                            visc_del2=1e3, visc_del4=1e9, eddy_diff2=1e3,
+                            eddy_diff4=1e9, disable_vn=1, seed=21),
     # every term on, 5-stage LSRK, 1000 steps (long-run agreement)
     "lsrk5_1000_steps": dict(nx=12, ny=10, dc=1e4, K=3, T=2, stepper="lsrk5",
                              nsteps=1000, dt=20.0, f0=1e-4, grav=9.81,

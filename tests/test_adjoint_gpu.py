@@ -55,6 +55,8 @@ ALL_TERMS = WORKLOADS["lsrk5_512x512"].scaled(nx=12, ny=10, nlayers=5,
 
 @pytest.mark.parametrize("over", [{}, {"m_disable_h_tendency": True,
                                        "m_disable_vn_tendency": True},
+                                  {"m_disable_h_tendency": True},
+                                  {"m_disable_vn_tendency": True},
                                   {"m_visc_del4": 0.0, "m_eddy_diff4": 0.0}])
 def test_tendency_dot_product(over):
     mesh, params, model = setup(ALL_TERMS, **over)
@@ -87,11 +89,17 @@ def test_tendency_dot_product(over):
         assert np.max(np.abs(a - b)) / scale < 1e-5
 
 
-@pytest.mark.parametrize("nsteps,nsnap", [(1, 1), (7, 1), (7, 3), (20, 4),
-                                          (9, 12)])
-def test_trajectory_dot_product_through_checkpointing(nsteps, nsnap):
+@pytest.mark.parametrize("nsteps,nsnap,over", [
+    (1, 1, {}), (7, 1, {}), (7, 3, {}), (20, 4, {}), (9, 12, {}),
+    (6, 2, {"m_disable_h_tendency": True}),
+    (6, 2, {"m_disable_vn_tendency": True})])
+def test_trajectory_dot_product_through_checkpointing(nsteps, nsnap, over):
+    """RK4 adjoint against the tangent-linear model through schedules of 1
+    to 12 snapshots, <= 1e-12, and the forward sweep's x_N bitwise equal to
+    the plain stepper's; also with h or vn frozen (a frozen field of x_N is
+    the step's input, which the taped last step copies)."""
     wl = ALL_TERMS
-    mesh, params, model = setup(wl)
+    mesh, params, model = setup(wl, **over)
     adj = og.Adjoint(model, nsnap)
     x0 = initial_state(mesh, wl)
     shapes = [a.shape for a in x0]
@@ -223,16 +231,18 @@ def test_checkpoint_budget_and_step_limit_are_errors():
     assert adj.info() == (og.checkpoint_cost(20, 1), 20)
 
 
-@pytest.mark.parametrize("nstages,nsteps,nsnap", [(5, 1, 1), (5, 7, 3),
-                                                  (5, 20, 4), (1, 9, 2),
-                                                  (1, 12, 12)])
+@pytest.mark.parametrize("nstages,nsteps,nsnap,over", [
+    (5, 1, 1, {}), (5, 7, 3, {}), (5, 20, 4, {}), (1, 9, 2, {}),
+    (1, 12, 12, {}), (5, 6, 2, {"m_disable_h_tendency": True}),
+    (5, 6, 2, {"m_disable_vn_tendency": True})])
 def test_lsrk_trajectory_dot_product_through_checkpointing(nstages, nsteps,
-                                                           nsnap):
+                                                           nsnap, over):
     """The low-storage RK adjoint (5-stage Carpenter-Kennedy and 1-stage
     Euler) against its dual-number tangent-linear model, <= 1e-12, and the
-    forward sweep's x_N bitwise equal to the plain LSRK stepper's."""
+    forward sweep's x_N bitwise equal to the plain LSRK stepper's; also with
+    h or vn frozen."""
     wl = ALL_TERMS
-    mesh, params, model = setup(wl)
+    mesh, params, model = setup(wl, **over)
     adj = og.Adjoint(model, nsnap, "lsrk", nstages)
     x0 = initial_state(mesh, wl)
     shapes = [a.shape for a in x0]
