@@ -1,0 +1,155 @@
+"""Configurations crossed with the stepping paths.
+
+A model's enabled set (h or vn frozen, no tracers, each dissipation term
+alone) changes which passes run and which buffers a stage reads, so every
+path is run on each:
+- the steppers (RK4, LSRK5, Euler) against the oracle, 3 steps, <= 1e-12;
+- batches of such members, bitwise equal to each member stepped alone;
+- the adjoint's tendency and 6-step trajectory dot products against the
+  tangent-linear model, <= 1e-12, and its forward sweep's x_N bitwise equal
+  to the plain stepper's."""
+import numpy as np
+import pytest
+
+import omega_playground_gb300 as og
+import pyoracle
+from helpers import rel_diff
+from omega_playground_gb300.workloads import uniform
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+ALL = dict(f0=1e-4, grav=9.81, visc_del2=1e3, visc_del4=1e9, eddy_diff2=1e3,
+           eddy_diff4=1e9)
+CONFIGS = {
+    "h_frozen": dict(ALL, disable_h=True),
+    "vn_frozen": dict(ALL, disable_vn=True),
+    "no_tracers": dict(ALL, T=0),
+    "del2_only": dict(f0=1e-4, grav=9.81, visc_del2=1e3, eddy_diff2=1e3),
+    "del4_only": dict(f0=1e-4, grav=9.81, visc_del4=1e9, eddy_diff4=1e9),
+    "tracer_del4_only": dict(f0=1e-4, grav=9.81, eddy_diff4=1e9),
+    "inviscid": dict(f0=1e-4, grav=9.81),
+}
+STEPPERS = [("rk4", 4), ("lsrk", 5), ("lsrk", 1)]
+
+
+def build(nx, ny, K, cfg):
+    c = dict(cfg)
+    T = c.pop("T", 2)
+    dh, dv = c.pop("disable_h", False), c.pop("disable_vn", False)
+    mesh = og.PlanarHexagonalMesh(nx, ny, 1e4, K)
+    params = og.ShallowWaterParams(
+        m_f0=c.get("f0", 0.0), m_grav=c.get("grav", 9.81),
+        m_visc_del2=c.get("visc_del2", 0.0), m_visc_del4=c.get("visc_del4", 0.0),
+        m_eddy_diff2=c.get("eddy_diff2", 0.0),
+        m_eddy_diff4=c.get("eddy_diff4", 0.0), m_ntracers=T,
+        m_disable_h_tendency=dh, m_disable_vn_tendency=dv)
+    om = pyoracle.OracleMesh(nx, ny, 1e4, K)
+    omd = pyoracle.OracleModel(om, ntracers=T, disable_h_tendency=dh,
+                               disable_vn_tendency=dv, **c)
+    return mesh, params, og.ShallowWaterModel(mesh, params), omd
+
+
+def state(mesh, T, seed):
+    C_, E, K = mesh.m_ncells, mesh.m_nedges, mesh.m_nlayers
+    h = 1000.0 + 3.0 * uniform(seed, C_ * K).reshape(C_, K)
+    vn = 0.2 * (uniform(seed + 1, E * K).reshape(E, K) - 0.5)
+    tr = h[None] * (0.5 + uniform(seed + 2, T * C_ * K).reshape(T, C_, K))
+    return h, vn, tr
+
+
+@pytest.mark.parametrize("kind,nstages", STEPPERS)
+@pytest.mark.parametrize("name", ["h_frozen", "vn_frozen", "no_tracers",
+                                  "tracer_del4_only"])
+def test_steppers_against_oracle(name, kind, nstages):
+    mesh, params, model, omd = build(10, 8, 4, CONFIGS[name])
+    T = params.m_ntracers
+    x = state(mesh, T, 17)
+    want = omd.step(*(a.copy() for a in x), 0.0, 20.0, 3, kind=kind,
+                    nstages=nstages)
+    for use_graph in (False, True):
+        S = og.ShallowWaterState(mesh, params)
+        S.upload(*x)
+        st = og.RK4Stepper(model) if kind == "rk4" else og.LSRKStepper(model,
+                                                                       nstages)
+        st.step(S, 0.0, 20.0, 3, use_graph=use_graph)
+        for g, w in zip(S.download(), want):
+            if w.size:
+                assert rel_diff(g, w) <= TOL, (name, kind, nstages)
+    if name == "h_frozen":
+        np.testing.assert_array_equal(S.download()[0], x[0])
+    if name == "vn_frozen":
+        np.testing.assert_array_equal(S.download()[1], x[1])
+
+
+@pytest.mark.parametrize("kind,nstages", STEPPERS)
+def test_batch_of_mixed_configurations(kind, nstages):
+    members = []
+    for j, name in enumerate(CONFIGS):
+        mesh, params, model, _ = build(6 + 2 * (j % 3), 6 + 2 * (j % 2),
+                                       3 + j, CONFIGS[name])
+        members.append((mesh, params, model,
+                        state(mesh, params.m_ntracers, 50 + 3 * j)))
+    singles = []
+    for mesh, params, model, x in members:
+        S = og.ShallowWaterState(mesh, params)
+        S.upload(*x)
+        st = og.RK4Stepper(model) if kind == "rk4" else og.LSRKStepper(model,
+                                                                       nstages)
+        st.step(S, 0.0, 20.0, 3, use_graph=False)
+        singles.append(S.download())
+    for cfg in range(og.Batch.config_count()):
+        states = []
+        for mesh, params, model, x in members:
+            S = og.ShallowWaterState(mesh, params)
+            S.upload(*x)
+            states.append(S)
+        b = og.Batch([m[2] for m in members], states, kind, nstages)
+        b.set_config(cfg)
+        b.step(0.0, 20.0, 3)
+        for m, (S, want) in enumerate(zip(states, singles)):
+            for g, w in zip(S.download(), want):
+                np.testing.assert_array_equal(g, w, err_msg=f"{cfg} {m}")
+
+
+def dot(a, b):
+    return sum(float(np.sum(p * q)) for p, q in zip(a, b))
+
+
+@pytest.mark.parametrize("kind,nstages", [("rk4", 4), ("lsrk", 5)])
+@pytest.mark.parametrize("name", list(CONFIGS))
+def test_adjoint_dot_products(name, kind, nstages):
+    mesh, params, model, _ = build(10, 8, 3, CONFIGS[name])
+    T = params.m_ntracers
+    adj = og.Adjoint(model, 2, kind, nstages)
+    x = state(mesh, T, 71)
+    dx = tuple(s * (uniform(80 + j, a.size).reshape(a.shape) - 0.5)
+               for j, (a, s) in enumerate(zip(x, (1.0, 0.01, 10.0))))
+    mu = tuple(uniform(90 + j, a.size).reshape(a.shape) - 0.5
+               for j, a in enumerate(x))
+
+    def mk(a):
+        st = og.ShallowWaterState(mesh, params)
+        st.upload(*a)
+        return st
+
+    X = mk(x)
+    JD, JT = og.ShallowWaterState(mesh, params), og.ShallowWaterState(mesh, params)
+    adj.tlm_tendency(X, mk(dx), JD)
+    adj.adj_tendency(X, mk(mu), JT)
+    lhs, rhs = dot(JD.download(), mu), dot(dx, JT.download())
+    assert abs(lhs - rhs) <= TOL * max(abs(lhs), abs(rhs), 1e-300), (lhs, rhs)
+    XN = og.ShallowWaterState(mesh, params)
+    adj.forward(X, 0.0, 20.0, 6, XN)
+    LAM = mk(mu)
+    adj.backward(LAM)
+    DX = mk(dx)
+    adj.tlm_apply(X, DX, 0.0, 20.0, 6)
+    lhs, rhs = dot(DX.download(), mu), dot(dx, LAM.download())
+    assert abs(lhs - rhs) <= TOL * max(abs(lhs), abs(rhs)), (lhs, rhs)
+    ref = mk(x)
+    st = og.RK4Stepper(model) if kind == "rk4" else og.LSRKStepper(model,
+                                                                   nstages)
+    st.step(ref, 0.0, 20.0, 6, use_graph=False)
+    for g, w in zip(XN.download(), ref.download()):
+        np.testing.assert_array_equal(g, w)
