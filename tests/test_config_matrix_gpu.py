@@ -7,7 +7,9 @@ path is run on each:
 - batches of such members, bitwise equal to each member stepped alone;
 - the adjoint's tendency and 6-step trajectory dot products against the
   tangent-linear model, <= 1e-12, and its forward sweep's x_N bitwise equal
-  to the plain stepper's."""
+  to the plain stepper's;
+- the host-state stepper, bitwise equal to upload + step + download.
+(The allocation-free tendency takes the same sets in test_zz_no_alloc.py.)"""
 import numpy as np
 import pytest
 
@@ -153,3 +155,26 @@ def test_adjoint_dot_products(name, kind, nstages):
     st.step(ref, 0.0, 20.0, 6, use_graph=False)
     for g, w in zip(XN.download(), ref.download()):
         np.testing.assert_array_equal(g, w)
+
+
+@pytest.mark.parametrize("name", list(CONFIGS))
+def test_host_stepper(name):
+    """The host-state stepper (chunks of 2 of 5 levels) on each enabled
+    set, bitwise equal to upload + step + download."""
+    mesh, params, model, _ = build(10, 8, 5, CONFIGS[name])
+    T = params.m_ntracers
+    x = state(mesh, T, 33)
+    for kind, nstages in STEPPERS:
+        S = og.ShallowWaterState(mesh, params)
+        S.upload(*x)
+        st = og.RK4Stepper(model) if kind == "rk4" else og.LSRKStepper(model,
+                                                                       nstages)
+        st.step(S, 0.0, 20.0, 3)
+        hs = og.HostStepper(model, kind, nstages, 2)
+        arrs = hs.pinned_state()
+        for a, b in zip(arrs, x):
+            if a.size:
+                a[...] = b
+        hs.step(*arrs, 0.0, 20.0, 3)
+        for g, w in zip(arrs, S.download()):
+            np.testing.assert_array_equal(g, w, err_msg=f"{name} {kind}")

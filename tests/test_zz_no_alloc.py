@@ -114,3 +114,32 @@ def test_noalloc_increment_and_size_limit():
     assert "static maximum" in msg and "64 MiB" in msg
     h, vn, tr = tb.download()
     assert not h.any() and not vn.any() and not tr.any()
+
+
+@pytest.mark.parametrize("name", ["h_frozen", "vn_frozen", "no_tracers",
+                                  "del2_only", "del4_only", "tracer_del4_only",
+                                  "inviscid"])
+def test_noalloc_enabled_sets(name):
+    """Each enabled set (frozen fields, no tracers, single dissipation terms)
+    in both add modes, against the allocating entry point."""
+    from test_config_matrix_gpu import CONFIGS, state
+    c = dict(CONFIGS[name])
+    cfg = dict(nx=10, ny=8, dc=1e4, K=5, T=c.pop("T", 2),
+               disable_h=c.pop("disable_h", False),
+               disable_vn=c.pop("disable_vn", False),
+               f0=c.get("f0", 0.0), grav=c.get("grav", 9.81),
+               visc_del2=c.get("visc_del2", 0.0),
+               visc_del4=c.get("visc_del4", 0.0),
+               eddy_diff2=c.get("eddy_diff2", 0.0),
+               eddy_diff4=c.get("eddy_diff4", 0.0))
+    mesh, params = _setup(cfg)
+    S = og.ShallowWaterState(mesh, params)
+    S.upload(*state(mesh, cfg["T"], 23))
+    ref = _allocating(mesh, params, S)
+    tend = og.ShallowWaterState(mesh, params)
+    assert _noalloc(mesh, params, S, tend, 0) == 0
+    for a, b in zip(tend.download(), ref):
+        assert rel_diff(a, b) <= TOL, name
+    assert _noalloc(mesh, params, S, tend, 1) == 0
+    for a, b in zip(tend.download(), ref):
+        assert rel_diff(a, 2 * b) <= TOL, name
