@@ -178,3 +178,40 @@ def test_host_stepper(name):
         hs.step(*arrs, 0.0, 20.0, 3)
         for g, w in zip(arrs, S.download()):
             np.testing.assert_array_equal(g, w, err_msg=f"{name} {kind}")
+
+
+@pytest.mark.parametrize("kind,nstages", [("rk4", 4), ("lsrk", 5)])
+def test_batch_of_general_meshes(kind, nstages):
+    """Members on perturbed general MPAS tables (10 nonzero TRiSK weights,
+    so the 10-wide edges-on-edge kernels; random 0/1 edge masks, scaling and
+    5-edge cells), bitwise equal to each member stepped alone, in every
+    launch configuration."""
+    from test_general_mesh_gpu import general_mesh, models
+    from test_general_mesh_gpu import state as gstate
+    members = []
+    for j, (nx, ny, K, T) in enumerate(((10, 8, 5, 2), (6, 6, 9, 1),
+                                        (8, 10, 3, 3))):
+        om, gm = general_mesh(nx, ny, K, 300 + j)
+        _, gp, model = models(om, gm, T)
+        members.append((gm, gp, model, gstate(om, T, 400 + j)))
+    singles = []
+    for gm, gp, model, x in members:
+        S = og.ShallowWaterState(gm, gp)
+        S.upload(*x)
+        st = og.RK4Stepper(model) if kind == "rk4" else og.LSRKStepper(model,
+                                                                       nstages)
+        st.step(S, 0.0, 5.0, 3, use_graph=False)
+        singles.append(S.download())
+    for cfg in range(og.Batch.config_count()):
+        states = []
+        for gm, gp, model, x in members:
+            S = og.ShallowWaterState(gm, gp)
+            S.upload(*x)
+            states.append(S)
+        b = og.Batch([m[2] for m in members], states, kind, nstages)
+        b.set_config(cfg)
+        b.step(0.0, 5.0, 3)
+        for m, (S, want) in enumerate(zip(states, singles)):
+            for g, w in zip(S.download(), want):
+                assert np.all(np.isfinite(w))
+                np.testing.assert_array_equal(g, w, err_msg=f"{cfg} {m}")
