@@ -215,3 +215,43 @@ def test_batch_of_general_meshes(kind, nstages):
             for g, w in zip(S.download(), want):
                 assert np.all(np.isfinite(w))
                 np.testing.assert_array_equal(g, w, err_msg=f"{cfg} {m}")
+
+
+@pytest.mark.parametrize("kind,nstages", [("rk4", 4), ("lsrk", 5)])
+def test_forcing_hook_on_a_frozen_field(kind, nstages):
+    """The forcing hook with h frozen adds c to h's tendency.  The reference
+    zeroes a tendency only inside that field's compute_*_tendency
+    (shallow_water_model.cpp:52-60, 323-345), so a frozen field's tendency is
+    never reset and the hook's additions accumulate over evaluations:
+    - RK4 (rk4.cpp:28-104, four evaluations per step, replace mode): the
+      e-th evaluation leaves e*c, so a step adds dt*c*sum_s b_s*(4n+s+1);
+    - LSRK (tendency scaled by a_s, then incremented): exactly dt*c a step.
+    The GPU reproduces both (absolute error <= 1e-10 on h ~ 1000)."""
+    torch = pytest.importorskip("torch")
+    from omega_playground_gb300.shallow_water import _DeviceArray
+    mesh, params, _, _ = build(8, 6, 3, CONFIGS["h_frozen"])
+    C_, K = mesh.m_ncells, mesh.m_nlayers
+    c, dt, n = 1e-3, 20.0, 4
+
+    class Forced(og.ShallowWaterModel):
+        def additional_tendency(self, h_tend, vn_tend, h, vn, t, stream):
+            torch.as_tensor(_DeviceArray(None, h_tend, (C_, K)),
+                            device="cuda").add_(c)
+
+    model = Forced(mesh, params)
+    x = state(mesh, params.m_ntracers, 61)
+    S = og.ShallowWaterState(mesh, params)
+    S.upload(*x)
+    st = og.RK4Stepper(model) if kind == "rk4" else og.LSRKStepper(model,
+                                                                   nstages)
+    st.step(S, 0.0, dt, n)
+    torch.cuda.synchronize()
+    if kind == "rk4":
+        b = (1 / 6, 1 / 3, 1 / 3, 1 / 6)
+        rise = dt * c * sum(b[s] * (4 * j + s + 1) for j in range(n)
+                            for s in range(4))
+    else:
+        rise = n * dt * c
+    got = S.download()[0] - x[0]
+    # h ~ 1000: round-off of the updates is ~1e-13 absolute
+    assert np.max(np.abs(got - rise)) <= 1e-10, (got.min(), got.max(), rise)
