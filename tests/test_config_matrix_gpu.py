@@ -1,7 +1,7 @@
 """Configurations crossed with the stepping paths.
 
-A model's enabled set (h or vn frozen, no tracers, each dissipation term
-alone) changes which passes run and which buffers a stage reads, so every
+A model's enabled set (h or vn frozen, no or 12 tracers, each dissipation
+term alone) changes which passes run and which buffers a stage reads, so every
 path is run on each:
 - the steppers (RK4, LSRK5, Euler) against the oracle, 3 steps, <= 1e-12;
 - batches of such members, bitwise equal to each member stepped alone;
@@ -31,6 +31,7 @@ CONFIGS = {
     "del4_only": dict(f0=1e-4, grav=9.81, visc_del4=1e9, eddy_diff4=1e9),
     "tracer_del4_only": dict(f0=1e-4, grav=9.81, eddy_diff4=1e9),
     "inviscid": dict(f0=1e-4, grav=9.81),
+    "many_tracers": dict(ALL, T=12),
 }
 STEPPERS = [("rk4", 4), ("lsrk", 5), ("lsrk", 1)]
 
@@ -62,7 +63,7 @@ def state(mesh, T, seed):
 
 @pytest.mark.parametrize("kind,nstages", STEPPERS)
 @pytest.mark.parametrize("name", ["h_frozen", "vn_frozen", "no_tracers",
-                                  "tracer_del4_only"])
+                                  "tracer_del4_only", "many_tracers"])
 def test_steppers_against_oracle(name, kind, nstages):
     mesh, params, model, omd = build(10, 8, 4, CONFIGS[name])
     T = params.m_ntracers

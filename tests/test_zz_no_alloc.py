@@ -118,7 +118,7 @@ def test_noalloc_increment_and_size_limit():
 
 @pytest.mark.parametrize("name", ["h_frozen", "vn_frozen", "no_tracers",
                                   "del2_only", "del4_only", "tracer_del4_only",
-                                  "inviscid"])
+                                  "inviscid", "many_tracers"])
 def test_noalloc_enabled_sets(name):
     """Each enabled set (frozen fields, no tracers, single dissipation terms)
     in both add modes, against the allocating entry point."""
