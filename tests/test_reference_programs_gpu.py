@@ -106,3 +106,14 @@ def test_cpp_gradient_and_ensemble_classes():
     assert rel <= 1e-12
     assert "ensemble max_abs_diff=0.000e+00" in out
     assert "host max_abs_diff=0.000e+00" in out
+
+
+def test_cpp_term_members_and_f_vertex():
+    """The C++ drop-in's nine tendency-term members: each switched off
+    alone changes only the fields its term writes, reads back false, equals
+    the same term switched through the C ABI bit for bit, and switching it
+    back restores the tendency; a beta plane written into m_f_vertex by a
+    user kernel changes only vn's tendency."""
+    out = run("term_switches")
+    assert "PASS" in out, out
+    assert out.count(" 1, equals the C ABI switch 1, restored 1") == 9, out
