@@ -117,3 +117,11 @@ def test_cpp_term_members_and_f_vertex():
     out = run("term_switches")
     assert "PASS" in out, out
     assert out.count(" 1, equals the C ABI switch 1, restored 1") == 9, out
+
+
+def test_cpp_model_variants():
+    """The C++ LinearShallowWaterModel and the drag option against twins
+    made through the C ABI: tendencies and RK4 / LSRK5 steps bitwise
+    equal."""
+    out = run("model_variants")
+    assert "PASS" in out and out.count("twin 1") == 2, out
