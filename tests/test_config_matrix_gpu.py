@@ -256,3 +256,46 @@ def test_forcing_hook_on_a_frozen_field(kind, nstages):
     got = S.download()[0] - x[0]
     # h ~ 1000: round-off of the updates is ~1e-13 absolute
     assert np.max(np.abs(got - rise)) <= 1e-10, (got.min(), got.max(), rise)
+
+
+def test_paths_on_a_caller_stream():
+    """Every stepping path launched on a non-blocking stream of the
+    caller's (fork/join branches, graph replays, the adjoint's advance
+    stream and the batch's launches must order against it): results
+    bitwise equal to the same calls on the legacy stream."""
+    torch = pytest.importorskip("torch")
+    s = torch.cuda.Stream()
+    sp = s.cuda_stream
+    mesh, params, model, _ = build(10, 8, 5, CONFIGS["many_tracers"])
+    T = params.m_ntracers
+    x = state(mesh, T, 5)
+
+    def run(stream):
+        out = {}
+        S = og.ShallowWaterState(mesh, params)
+        S.upload(*x, stream=stream)
+        og.LSRKStepper(model, 5).step(S, 0.0, 20.0, 3, stream=stream)
+        og.RK4Stepper(model).step(S, 0.0, 20.0, 2, stream=stream)
+        out["steps"] = S.download(stream=stream)
+        Tn = og.ShallowWaterState(mesh, params)
+        model.compute_tendency(Tn, S, 0.0, stream=stream)
+        out["tend"] = Tn.download(stream=stream)
+        adj = og.Adjoint(model, 2)
+        XN = og.ShallowWaterState(mesh, params)
+        adj.forward(S, 0.0, 20.0, 5, XN, stream=stream)
+        L = og.ShallowWaterState(mesh, params)
+        L.upload(*state(mesh, T, 9), stream=stream)
+        adj.backward(L, stream=stream)
+        out["grad"] = L.download(stream=stream)
+        B = og.ShallowWaterState(mesh, params)
+        B.upload(*x, stream=stream)
+        b = og.Batch([model], [B], "lsrk", 5)
+        b.step(0.0, 20.0, 3, stream=stream)
+        out["batch"] = B.download(stream=stream)
+        return out
+
+    ref = run(None)
+    got = run(sp)
+    for k in ref:
+        for a, bb in zip(got[k], ref[k]):
+            np.testing.assert_array_equal(a, bb, err_msg=k)
