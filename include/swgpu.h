@@ -394,7 +394,8 @@ int swg_adj_info(swg_adjoint adj, long long *plain_steps,
  * per-cell field mapped to edges as visc_e = (visc_c0 + visc_c1) / 2
  * (realised through mesh_scaling_del2, vel_diff_edge.hpp:83-84).  Only the
  * momentum term is differentiated: with eddy_diff2 > 0 the same scaling
- * also enters tracer diffusion, which this gradient leaves out. */
+ * also enters tracer diffusion, which this gradient leaves out.
+ * SWG_ERR_STATE until a backward sweep has completed. */
 int swg_adj_grad_visc(swg_adjoint adj, double *grad_edge, double *grad_cell,
                       void *stream);
 /* plain advances of the optimal binomial schedule (host only; -1 for

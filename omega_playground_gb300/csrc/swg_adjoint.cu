@@ -484,6 +484,7 @@ struct swg_adjoint_s {
   double t0 = 0, dt = 0;
   long long plain_steps = 0, taped_steps = 0;
   int state = 0; // 0 idle, 1 forward done (first step taped)
+  bool grad_ready = false; // a backward sweep has completed
   // backward sweep: restores, stores and plain advances run on `adv`,
   // concurrently with the caller's stream, which tapes and reverses each
   // step; `ready` = x_i is in cur, `freed` = cur was copied to the tape
@@ -1444,6 +1445,7 @@ int bwd_next(swg_adjoint ad, swg_state lambda, cudaStream_t st, bool *done) {
     return cuda_fail(e, "swg_adj_backward: stream handshake");
   TRY(swg_state_copy(lambda, ad->lam, st));
   ad->state = 0;
+  ad->grad_ready = true;
   *done = true;
   return SWG_OK;
 }
@@ -1569,6 +1571,9 @@ extern "C" int swg_adj_grad_visc(swg_adjoint ad, double *grad_edge,
   if (!ad->aw.gc2e)
     return fail(SWG_ERR_STATE, "swg_adj_grad_visc: the model has no del2 "
                                "viscosity term");
+  if (!ad->grad_ready)
+    return fail(SWG_ERR_STATE, "swg_adj_grad_visc: no backward sweep has "
+                               "completed");
   swg_mesh me = ad->model->mesh;
   const int E = me->nedges, C = me->ncells, K = me->nlayers;
   cudaStream_t st = static_cast<cudaStream_t>(stream);

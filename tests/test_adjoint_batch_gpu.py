@@ -38,6 +38,8 @@ def test_viscosity_field_gradient_fd():
     region = region_cells(mesh, wl.seed + 99)
     x0 = initial_state(mesh, wl)
     adj = og.Adjoint(model, 5)
+    with pytest.raises(og.SwgError, match="no backward sweep"):
+        adj.grad_visc()                      # nothing to report yet
     X0 = og.ShallowWaterState(mesh, params)
     X0.upload(*x0)
     XN = og.ShallowWaterState(mesh, params)
