@@ -18,7 +18,13 @@
  *    device.
  *  - Handles are thread-confined.  Compute calls take a cudaStream_t (passed
  *    as void*, NULL = legacy default stream) and are asynchronous on it;
- *    only swg_state_download, swg_diag_* and swg_sync block the host.
+ *    the calls that block the host are swg_state_download, swg_diag_*,
+ *    swg_sync, swg_host_step, swg_batch_check, swg_batch_autotune,
+ *    swg_adj_grad_visc and swg_profile_read.
+ *  - A model's intermediate fields are shared by every call on it (as the
+ *    reference's model holds one auxiliary state), so calls on one model, or
+ *    on steppers and adjoints built on it, must be ordered: one stream, or
+ *    events between streams.  Different models run concurrently.
  *  - Connectivity is validated on the host at swg_mesh_create: every index
  *    is checked against its table's range before any kernel can read it.
  */
