@@ -1,8 +1,8 @@
 """1000-step parity with the oracle on the setups of the reference's
 convergence and conservation tests.
 
-Each case takes the mesh, stepper, enabled terms, coefficients and time step
-of one reference test (test/double_vortex.cpp, test/tracer_*_convergence.cpp,
+Each case but the last takes the mesh, stepper, enabled terms, coefficients
+and time step of one reference test (test/double_vortex.cpp, test/tracer_*_convergence.cpp,
 test/nonlinear_swe_convergence.cpp) and runs 1000 steps on the GPU and on
 the oracle from the same seeded initial state (a stand-in for the test's
 analytic one), then compares h, vn and the tracers.  The manufactured
@@ -75,6 +75,12 @@ CASES = {
     "nonlinear_swe": dict(nx=50, ny=50, dc=1e7 / 50, K=1, T=0, kind="rk4",
                           f0=1e-4, grav=9.80616, h0=1000.0, hs=1.0, vs=0.1,
                           dt_per_km=3.0),
+    # every term on (all four dissipation terms, 2 tracers), RK4, 3 levels,
+    # at the 64x64 workload's spacing and a 0.2 gravity-wave CFL
+    "rk4_all_terms": dict(nx=12, ny=10, dc=1e4, K=3, T=2, kind="rk4",
+                          f0=1e-4, grav=9.81, visc_del2=1e3, visc_del4=1e9,
+                          eddy_diff2=1e3, eddy_diff4=1e9, h0=1000.0, hs=5.0,
+                          vs=0.1, cfl=0.2),
 }
 
 
@@ -84,13 +90,16 @@ def test_1000_steps_against_oracle(name):
     om = pyoracle.OracleMesh(c["nx"], c["ny"], c["dc"], c["K"])
     disable = c.get("disable", False)
     kw = dict(f0=c.get("f0", 0.0), grav=c.get("grav", 9.81),
+              visc_del2=c.get("visc_del2", 0.0),
+              visc_del4=c.get("visc_del4", 0.0),
               eddy_diff2=c.get("eddy_diff2", 0.0),
               eddy_diff4=c.get("eddy_diff4", 0.0), ntracers=c["T"],
               disable_h_tendency=disable, disable_vn_tendency=disable)
     omd = pyoracle.OracleModel(om, **kw)
     mesh = og.PlanarHexagonalMesh(c["nx"], c["ny"], c["dc"], c["K"])
     params = og.ShallowWaterParams(
-        m_f0=kw["f0"], m_grav=kw["grav"], m_eddy_diff2=kw["eddy_diff2"],
+        m_f0=kw["f0"], m_grav=kw["grav"], m_visc_del2=kw["visc_del2"],
+        m_visc_del4=kw["visc_del4"], m_eddy_diff2=kw["eddy_diff2"],
         m_eddy_diff4=kw["eddy_diff4"], m_ntracers=c["T"],
         m_disable_h_tendency=disable, m_disable_vn_tendency=disable)
     model = og.ShallowWaterModel(mesh, params)
