@@ -34,6 +34,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 namespace omega {
@@ -69,8 +70,11 @@ template <class T, int R> struct DeviceView {
       n *= size_t(m_ext[r]);
     return n;
   }
-  operator DeviceView<const T, R>() const {
-    DeviceView<const T, R> v;
+  // a view of mutable elements converts to a read-only view
+  template <class U = T,
+            class = typename std::enable_if<!std::is_const<U>::value>::type>
+  operator DeviceView<const U, R>() const {
+    DeviceView<const U, R> v;
     v.m_data = m_data;
     for (int r = 0; r < R; ++r)
       v.m_ext[r] = m_ext[r];
@@ -401,10 +405,13 @@ struct ShallowWaterModel {
   ShallowWaterModel &operator=(const ShallowWaterModel &) = delete;
   virtual ~ShallowWaterModel() { swg_model_destroy(m_handle); }
 
-  // shallow_water_model.hpp:42-44
-  virtual void additional_tendency(Real2d h_tend_cell, Real2d vn_tend_edge,
-                                   RealConst2d h_cell, RealConst2d vn_edge,
-                                   Real t) const {
+  // shallow_water_model.hpp:42-44 (h_tend_cell, vn_tend_edge, h_cell,
+  // vn_edge, t); the base adds nothing
+  virtual void additional_tendency(Real2d /*h_tend_cell*/,
+                                   Real2d /*vn_tend_edge*/,
+                                   RealConst2d /*h_cell*/,
+                                   RealConst2d /*vn_edge*/,
+                                   Real /*t*/) const {
     m_default_hook = true;
   }
 
