@@ -299,3 +299,34 @@ def test_paths_on_a_caller_stream():
     for k in ref:
         for a, bb in zip(got[k], ref[k]):
             np.testing.assert_array_equal(a, bb, err_msg=k)
+
+
+def test_batch_of_many_small_members():
+    """300 members of 1 to 4x4 cells, 1 to 6 levels, 0 to 3 tracers: the
+    member table and the per-pass block prefixes at that count, bitwise
+    against each member stepped alone, persistent and per-pass shapes."""
+    members = []
+    for j in range(300):
+        nx, ny = 1 + j % 4, 1 + (j // 4) % 4
+        cfg = dict(CONFIGS["many_tracers"], T=j % 4)
+        mesh, params, model, _ = build(nx, ny, 1 + j % 6, cfg)
+        members.append((mesh, params, model,
+                        state(mesh, params.m_ntracers, 1000 + 3 * j)))
+    singles = []
+    for mesh, params, model, x in members:
+        S = og.ShallowWaterState(mesh, params)
+        S.upload(*x)
+        og.LSRKStepper(model, 5).step(S, 0.0, 20.0, 2, use_graph=False)
+        singles.append(S.download())
+    for cfg in (0, og.Batch.config_count() - 1):
+        states = []
+        for mesh, params, model, x in members:
+            S = og.ShallowWaterState(mesh, params)
+            S.upload(*x)
+            states.append(S)
+        b = og.Batch([m[2] for m in members], states, "lsrk", 5)
+        b.set_config(cfg)
+        b.step(0.0, 20.0, 2)
+        for m, (S, want) in enumerate(zip(states, singles)):
+            for g, w in zip(S.download(), want):
+                np.testing.assert_array_equal(g, w, err_msg=f"{cfg} {m}")
