@@ -196,11 +196,13 @@ def test_graph_and_direct_launches_agree_bitwise():
         np.testing.assert_array_equal(a, b)
 
 
-def test_full_size_512x512_one_step_against_oracle():
-    """The full 512x512x64, 8-tracer LSRK5 workload: one step on the GPU
-    against one step of the oracle (all host cores)."""
+@pytest.mark.parametrize("nsteps", [1, 10])
+def test_full_size_512x512_against_oracle(nsteps):
+    """The full 512x512x64, 8-tracer LSRK5 workload (the benchmarked one):
+    1 and 10 steps on the GPU against the oracle (all host cores, about 3 s
+    a step), <= 1e-12."""
     wl = WORKLOADS["lsrk5_512x512"]
-    (h, vn, tr), (rh, rvn, rtr) = _oracle_vs_gpu(wl, 1)
+    (h, vn, tr), (rh, rvn, rtr) = _oracle_vs_gpu(wl, nsteps)
     assert rel_diff(h, rh) <= TOL
     assert rel_diff(vn, rvn) <= TOL
     assert rel_diff(tr, rtr) <= TOL
