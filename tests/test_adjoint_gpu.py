@@ -209,6 +209,30 @@ def test_finite_differences_full_adjoint_workload():
     assert _fd_check(wl, wl.nsteps, 32, 16, 1e-4) <= 1e-6
 
 
+def test_dot_product_full_adjoint_workload():
+    """The adjoint workload itself (128x128 cells, 32 levels, 2 tracers,
+    RK4, 1000 steps, 32 snapshots): <dx_N, lam_N> from the tangent-linear
+    model against <dx_0, lam_0> from the checkpointed adjoint, <= 1e-12."""
+    wl = WORKLOADS["rk4_128x128_adjoint"]
+    mesh, params, model = setup(wl)
+    adj = og.Adjoint(model, 32)
+    x0 = initial_state(mesh, wl)
+    shapes = [a.shape for a in x0]
+    dx0 = rand_like(shapes, 515, (1.0, 0.01, 10.0))
+    lamN = rand_like(shapes, 616)
+    X0 = make_state(mesh, params, x0)
+    XN = og.ShallowWaterState(mesh, params)
+    adj.forward(X0, 0.0, wl.dt, wl.nsteps, XN)
+    LAM = make_state(mesh, params, lamN)
+    adj.backward(LAM)
+    assert adj.info() == (og.checkpoint_cost(wl.nsteps, 32), wl.nsteps)
+    DX = make_state(mesh, params, dx0)
+    adj.tlm_apply(X0, DX, 0.0, wl.dt, wl.nsteps)
+    lhs, rhs = dot(DX.download(), lamN), dot(dx0, LAM.download())
+    assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), abs(rhs)), \
+        (lhs, rhs, abs(lhs - rhs) / max(abs(lhs), abs(rhs)))
+
+
 def test_checkpoint_budget_and_step_limit_are_errors():
     """A budget whose schedule would re-run more than 32 plain steps per step
     is SWG_ERR_BUDGET (one snapshot for 200 steps: 99.5 per step); more steps
