@@ -109,3 +109,16 @@ def test_odd_row_seam_flag():
         type("M", (), {"m_ny": 29})())
     assert not PlanarHexagonalMesh.odd_row_seam.fget(
         type("M", (), {"m_ny": 28})())
+
+
+def test_every_small_size_matches_oracle():
+    """Every nx, ny in 1..12 (odd and even rows, one-cell-wide meshes):
+    the product's builder against the oracle, bit for bit."""
+    for nx in range(1, 13):
+        for ny in range(1, 13):
+            tabs, px, py = product_tables(nx, ny, 1e4)
+            m = pyoracle.OracleMesh(nx, ny, 1e4, 1)
+            for k, v in tabs.items():
+                np.testing.assert_array_equal(v, m.tables[k],
+                                              err_msg=f"{nx}x{ny} {k}")
+            assert px == m.period_x and py == m.period_y
