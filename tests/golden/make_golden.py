@@ -122,10 +122,60 @@ def run_scenario(name: str, sc: dict, workdir: str) -> dict:
     return rec
 
 
+TABLES = ("nedges_on_cell", "edges_on_cell", "cells_on_cell",
+          "vertices_on_cell", "kite_index_on_cell", "nedges_on_edge",
+          "edges_on_edge", "cells_on_edge", "vertices_on_edge",
+          "edges_on_vertex", "cells_on_vertex", "area_cell", "x_cell",
+          "y_cell", "edge_sign_on_cell", "dc_edge", "dv_edge", "angle_edge",
+          "x_edge", "y_edge", "weights_on_edge", "area_triangle",
+          "x_vertex", "y_vertex", "kiteareas_on_vertex",
+          "edge_sign_on_vertex")
+
+
+def mesh_sweep(n: int = 12) -> None:
+    """Pins the oracle on every mesh of nx, ny in 1..n cells: the
+    reference's own tables and one tendency (every term on, 2 levels, one
+    tracer) against the oracle's, bit for bit.  Writes mesh_sweep.txt."""
+    pyoracle.build(with_reference=True)
+    bad = []
+    with tempfile.TemporaryDirectory() as wd:
+        for nx in range(1, n + 1):
+            for ny in range(1, n + 1):
+                sc = dict(nx=nx, ny=ny, dc=1e4, K=2, T=1, stepper="none",
+                          nsteps=0, dt=0.0, f0=1e-4, grav=9.81,
+                          visc_del2=1e3, visc_del4=1e9, eddy_diff2=1e3,
+                          eddy_diff4=1e9, seed=1000 * nx + ny)
+                rec = run_scenario(f"{nx}x{ny}", sc, wd)
+                om = pyoracle.OracleMesh(nx, ny, 1e4, 2)
+                for k in TABLES:
+                    if k in rec and not np.array_equal(rec[k], om.tables[k]):
+                        bad.append(f"{nx}x{ny} {k}")
+                md = pyoracle.OracleModel(om, f0=1e-4, grav=9.81,
+                                          visc_del2=1e3, visc_del4=1e9,
+                                          eddy_diff2=1e3, eddy_diff4=1e9,
+                                          ntracers=1)
+                got = md.compute_tendency(rec["in_h"], rec["in_vn"],
+                                          rec["in_tr"])
+                for k, g in zip(("tend_h", "tend_vn", "tend_tr"), got):
+                    if not np.array_equal(g, rec[k]):
+                        bad.append(f"{nx}x{ny} {k}")
+    text = (f"oracle against the reference build on every mesh of nx, ny in "
+            f"1..{n}: tables and one tendency (all terms, K = 2, T = 1)\n"
+            + (f"mismatches: {', '.join(bad)}\n" if bad else
+               f"{n * n} meshes, all bit-exact\n"))
+    with open(os.path.join(HERE, "mesh_sweep.txt"), "w") as f:
+        f.write(text)
+    print(text, end="")
+
+
 def main() -> None:
     """Regenerates every fixture and reference_tests.txt, or only the
-    scenarios named on the command line."""
+    scenarios named on the command line (``--mesh-sweep``: the sweep of
+    mesh_sweep())."""
     only = sys.argv[1:]
+    if only == ["--mesh-sweep"]:
+        mesh_sweep()
+        return
     pyoracle.build(with_reference=True)
     with tempfile.TemporaryDirectory() as wd:
         for name, sc in SCENARIOS.items():
