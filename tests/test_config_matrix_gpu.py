@@ -362,3 +362,45 @@ def test_checkpoint_and_resume_is_bitwise(kind, nstages, tmp_path):
     stepper(model2).step(R, 60.0, 20.0, 3)
     for g, w in zip(R.download(), want):
         np.testing.assert_array_equal(g, w)
+
+
+def test_every_small_mesh():
+    """Every mesh of nx, ny in 1..12 cells (odd rows, one-cell-wide meshes,
+    every term on, 2 levels, 2 tracers): the GPU tendency against the
+    oracle, <= 1e-12, and the adjoint tendency's dot product against the
+    tangent-linear model, <= 1e-12 of the sum of the products' magnitudes.
+    On one-cell-wide meshes an edge has the same cell on both sides and its
+    difference terms cancel, exactly in the tangent-linear model and to
+    round-off in the adjoint, so the dot product itself can be far below
+    its terms and is not the scale."""
+    for nx in range(1, 13):
+        for ny in range(1, 13):
+            mesh, params, model, omd = build(nx, ny, 2, ALL)
+            x = state(mesh, 2, 10 * nx + ny)
+            want = omd.compute_tendency(*x)
+            S = og.ShallowWaterState(mesh, params)
+            S.upload(*x)
+            Tn = og.ShallowWaterState(mesh, params)
+            model.compute_tendency(Tn, S, 0.0)
+            for g, w in zip(Tn.download(), want):
+                assert rel_diff(g, w) <= TOL, (nx, ny)
+            adj = og.Adjoint(model, 1)
+            dx = tuple(s * (uniform(7 * nx + ny, a.size).reshape(a.shape)
+                            - 0.5) for a, s in zip(x, (1.0, 0.01, 10.0)))
+            mu = tuple(uniform(9 * nx + ny + j, a.size).reshape(a.shape)
+                       - 0.5 for j, a in enumerate(x))
+            DX, MU = og.ShallowWaterState(mesh, params), \
+                og.ShallowWaterState(mesh, params)
+            DX.upload(*dx)
+            MU.upload(*mu)
+            JD, JT = og.ShallowWaterState(mesh, params), \
+                og.ShallowWaterState(mesh, params)
+            adj.tlm_tendency(S, DX, JD)
+            adj.adj_tendency(S, MU, JT)
+            jd, jt = JD.download(), JT.download()
+            lhs, rhs = dot(jd, mu), dot(dx, jt)
+            scale = max(sum(float(np.sum(np.abs(p * q)))
+                            for p, q in zip(jd, mu)),
+                        sum(float(np.sum(np.abs(p * q)))
+                            for p, q in zip(dx, jt)))
+            assert abs(lhs - rhs) <= TOL * scale, (nx, ny, lhs, rhs, scale)
