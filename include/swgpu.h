@@ -229,12 +229,21 @@ int swg_compute_tendency(swg_model model, swg_state tend, swg_state state,
  * model-owned buffers.  Inputs h [C][K], vn [E][K], tr [T][C][K] and outputs
  * h_tend, vn_tend, tr_tend are device pointers; tr/tr_tend may be NULL when
  * params->ntracers == 0.  It calls no cudaMalloc/cudaFree or other
- * allocating routine.  Meshes and parameter sets whose scratch exceeds the
- * maximum are rejected with SWG_ERR_ARG (64x64 cells x 64 levels with one
- * tracer and del2 viscosity fits).  The first call on each device looks up
- * the array's address with that device current; make that first call before
- * any stream capture.  All calls share the array: calls that overlap on the
- * GPU (unordered streams) race on it. */
+ * allocating routine.  The array itself is device memory that CUDA commits
+ * when it loads the library's device code into a context: under the default
+ * lazy module loading (CUDA_MODULE_LOADING=LAZY) that happens inside the
+ * first launch of one of this library's kernels in the context, which may be
+ * this call.  A caller that reserves the whole pool should therefore make a
+ * first call (or any other call of this library that launches a kernel) at
+ * start-up, before it reserves the pool.  Meshes and parameter sets whose
+ * scratch exceeds the maximum are rejected with SWG_ERR_ARG (64x64 cells x
+ * 64 levels with one tracer and del2 viscosity fits).  The first call in
+ * each CUDA context looks up the array's address with the device current
+ * and caches it under the context's unique ID, so calls in another context
+ * (non-primary, or re-created after cudaDeviceReset) look it up again; make
+ * that first call before any stream capture.  Its launches are never timed
+ * by swg_profile_enable (that would create events).  All calls share the
+ * array: calls that overlap on the GPU (unordered streams) race on it. */
 #define SWG_NOALLOC_SCRATCH_BYTES (64ull << 20)
 int swg_compute_tendency_noalloc(swg_mesh mesh, const swg_params *params,
                                  const double *h, const double *vn,

@@ -192,6 +192,14 @@ void launch_axpby(double *y, const double *x, const double *z, double alpha,
                   double beta, long long n, int kind, cudaStream_t st);
 // opt-in per-kernel CUDA-event timing (swg_profile_enable)
 bool profiling_enabled();
+// while alive, launches of the calling thread are not timed (no events are
+// created for them) even with profiling on
+struct ProfileOff {
+  ProfileOff();
+  ~ProfileOff();
+  ProfileOff(const ProfileOff &) = delete;
+  ProfileOff &operator=(const ProfileOff &) = delete;
+};
 int profile_enable(int on);
 int profile_read(int max_kernels, char *names, double *total_ms,
                  long long *launches, int *count);

@@ -180,13 +180,15 @@ struct Timed {
 };
 std::vector<Timed> g_timed;
 bool g_profile = false;
+// > 0 while a ProfileOff guard is alive on this thread: launches not timed
+thread_local int t_profile_off = 0;
 
 struct Scope {
   const char *name;
   cudaStream_t st;
   cudaEvent_t a = nullptr, b = nullptr;
   Scope(const char *n, cudaStream_t s) : name(n), st(s) {
-    if (g_profile && cudaEventCreate(&a) == cudaSuccess &&
+    if (g_profile && !t_profile_off && cudaEventCreate(&a) == cudaSuccess &&
         cudaEventCreate(&b) == cudaSuccess)
       cudaEventRecord(a, st);
   }
@@ -202,6 +204,9 @@ struct Scope {
 } // namespace
 
 bool profiling_enabled() { return g_profile; }
+
+ProfileOff::ProfileOff() { ++t_profile_off; }
+ProfileOff::~ProfileOff() { --t_profile_off; }
 
 int profile_enable(int on) {
   g_profile = on != 0;

@@ -9,19 +9,29 @@
 // keeps both in one fixed device array compiled into the library, and takes
 // the state and tendency arrays as device pointers from the caller.
 //
-// The array holds SWG_NOALLOC_SCRATCH_BYTES (64 MiB); every GPU that loads
-// the library holds it until the process exits.  Its device address is
-// looked up with cudaGetSymbolAddress on the first call on each device (with
-// that device current) and cached; in host code the array's name is only a
-// host-side stand-in, never a device address.  All calls share the array:
-// each call rewrites every scratch element it later reads, so nothing has to
-// start at zero, but calls that overlap on the GPU (different streams, no
-// ordering between them) race on it.
+// The array holds SWG_NOALLOC_SCRATCH_BYTES (64 MiB).  Its device memory is
+// committed when the library's device code is loaded into a context: at
+// context creation with eager module loading, or under CUDA's default lazy
+// loading at the first launch of one of this library's kernels in that
+// context.  It is held until the context is destroyed (normally process
+// exit).  In host code the array's name is only a host-side stand-in, never
+// a device address.  The address belongs to the CUDA context, not to the
+// device: it is looked up with cudaGetSymbolAddress, with the device
+// current, the first time a call runs in a context, and cached under that
+// context's unique ID (cuCtxGetId, never reused in a process).  A call in
+// another context (a non-primary one, or the primary context re-created
+// after cudaDeviceReset) therefore looks the address up again instead of
+// using a stale one.  All calls share the array: each call rewrites every
+// scratch element it later reads, so nothing has to start at zero, but
+// calls that overlap on the GPU (different streams, no ordering between
+// them) race on it.
 #include "swg_internal.h"
 
+#include <cuda.h> // driver types only; the entry points are looked up
+
 #include <algorithm>
-#include <atomic>
 #include <cstdio>
+#include <mutex>
 
 namespace swg {
 namespace {
@@ -31,7 +41,78 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-std::atomic<unsigned char *> g_scratch_addr[kMaxDevices];
+// Scratch address per device, valid for the context whose ID is ctx_id.
+struct ScratchAddr {
+  unsigned long long ctx_id = 0;
+  unsigned char *addr = nullptr;
+};
+ScratchAddr g_scratch_addr[kMaxDevices];
+std::mutex g_scratch_mu;
+
+// cuCtxGetCurrent / cuCtxGetId through the runtime's driver entry points,
+// so the library does not link libcuda itself.
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+
+// The unique ID of the calling thread's current context (making the
+// device's primary context current if none is), or 0 when the driver does
+// not offer cuCtxGetId.
+int current_context_id(int dev, unsigned long long *id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000,
+                                         cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000,
+                                         cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+    (void)cudaGetLastError();
+  });
+  *id = 0;
+  if (!get_current || !get_id)
+    return SWG_OK;
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS)
+    return fail(SWG_ERR_CUDA, "swg_compute_tendency_noalloc: cuCtxGetCurrent");
+  if (!ctx) { // no context bound to this thread yet: bind the primary one
+    cudaError_t err = cudaSetDevice(dev);
+    if (err != cudaSuccess)
+      return cuda_fail(err, "swg_compute_tendency_noalloc: cudaSetDevice");
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx)
+      return fail(SWG_ERR_CUDA,
+                  "swg_compute_tendency_noalloc: no current context");
+  }
+  if (get_id(ctx, id) != CUDA_SUCCESS)
+    return fail(SWG_ERR_CUDA, "swg_compute_tendency_noalloc: cuCtxGetId");
+  return SWG_OK;
+}
+
+// The scratch array's device address in the current context: cached per
+// (device, context ID); looked up again in a context not seen before.
+int scratch_address(int dev, unsigned char **out) {
+  unsigned long long id = 0;
+  TRY(current_context_id(dev, &id));
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  ScratchAddr &c = g_scratch_addr[dev];
+  if (id == 0 || c.ctx_id != id || !c.addr) {
+    void *ptr = nullptr;
+    cudaError_t err = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (err != cudaSuccess || !ptr)
+      return cuda_fail(err != cudaSuccess ? err : cudaErrorInvalidSymbol,
+                       "swg_compute_tendency_noalloc: cudaGetSymbolAddress");
+    c.addr = static_cast<unsigned char *>(ptr);
+    c.ctx_id = id; // 0 (no cuCtxGetId): never matches, looked up every call
+  }
+  *out = c.addr;
+  return SWG_OK;
+}
 
 // Parameter-scaled tables of a model, the same expressions swg_model_create
 // evaluates on the host (shallow_water_model.cpp:5-41 enables the terms).
@@ -146,7 +227,8 @@ extern "C" int swg_compute_tendency_noalloc(swg_mesh mesh,
                   "(64 MiB)", need, kScratchBytes);
     return fail(SWG_ERR_ARG, msg);
   }
-  // once per device: the array's device address, with that device current
+  // the array's device address in the current context, with the device
+  // current (looked up once per context)
   int dev = 0;
   cudaError_t err = cudaGetDevice(&dev);
   if (err != cudaSuccess)
@@ -154,16 +236,8 @@ extern "C" int swg_compute_tendency_noalloc(swg_mesh mesh,
   if (dev < 0 || dev >= kMaxDevices)
     return fail(SWG_ERR_ARG, "swg_compute_tendency_noalloc: device ordinal "
                              "above 63");
-  unsigned char *base = g_scratch_addr[dev].load();
-  if (!base) {
-    void *ptr = nullptr;
-    err = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (err != cudaSuccess || !ptr)
-      return cuda_fail(err != cudaSuccess ? err : cudaErrorInvalidSymbol,
-                       "swg_compute_tendency_noalloc: cudaGetSymbolAddress");
-    base = static_cast<unsigned char *>(ptr);
-    g_scratch_addr[dev].store(base);
-  }
+  unsigned char *base = nullptr;
+  TRY(scratch_address(dev, &base));
   layout(mesh, pv, base, tab, a);
   pv.f_vertex = tab[0];
   pv.gidc = tab[1];
@@ -189,7 +263,12 @@ extern "C" int swg_compute_tendency_noalloc(swg_mesh mesh,
   s.fvn.tend = vn_tend;
   s.ftr.tend = tr_tend;
   s.ep.mode = add_mode == SWG_ADD_REPLACE ? EPI_REPLACE : EPI_INCREMENT;
-  launch_tendency(m, pv, a, s, st);
+  {
+    // the per-kernel profiler (swg_profile_enable) creates an event pair per
+    // launch; this path creates no driver objects, so it is never timed
+    ProfileOff no_timing;
+    launch_tendency(m, pv, a, s, st);
+  }
   err = cudaGetLastError();
   return err == cudaSuccess
              ? SWG_OK

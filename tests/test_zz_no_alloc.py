@@ -3,7 +3,9 @@ cannot allocate device memory while they run.  It keeps its parameter tables
 and intermediate fields in a static 64 MiB device array instead of
 model-owned buffers, so here it is checked through the C ABI against the
 allocating entry point, swg_compute_tendency, on two calls in a row (the
-second reuses the array the first one wrote), and its size limit is checked.
+second reuses the array the first one wrote); its size limit is checked, and
+so is the reason it exists: a warm call at the largest documented size
+leaves the device's free memory unchanged.
 
 This file is named to be collected last so that a run stopping at its first
 failure has already run every other test."""
@@ -43,6 +45,14 @@ def _noalloc(mesh, params, state, tend, add_mode=0):
         C.c_void_p(tr) if T else None, C.c_void_p(th), C.c_void_p(tv),
         C.c_void_p(tt) if T else None, add_mode, None)
     return rc
+
+
+def _free_device_bytes():
+    """cudaMemGetInfo's free byte count of the current device."""
+    from omega_playground_gb300.shallow_water import _cudart
+    free, total = C.c_size_t(0), C.c_size_t(0)
+    assert _cudart().cudaMemGetInfo(C.byref(free), C.byref(total)) == 0
+    return free.value
 
 
 def _allocating(mesh, params, state):
@@ -143,3 +153,41 @@ def test_noalloc_enabled_sets(name):
     assert _noalloc(mesh, params, S, tend, 1) == 0
     for a, b in zip(tend.download(), ref):
         assert rel_diff(a, 2 * b) <= TOL, name
+
+
+def test_noalloc_allocates_nothing_and_largest_documented_size():
+    """The property the entry point exists for: a warm call on a mesh and
+    parameter set it has not seen before leaves the device's free memory
+    unchanged.  It runs at the size the header documents as fitting (64x64
+    cells x 64 levels, one tracer, del2 viscosity), twice in a row, and each
+    result equals swg_compute_tendency's."""
+    # warm-up on another configuration: loads the module (and with it the
+    # static array) and every kernel of the path
+    g = load_golden("rk4_all_terms")
+    mesh0, params0 = _setup(g["cfg"])
+    s0 = og.ShallowWaterState(mesh0, params0)
+    s0.upload(g["in_h"], g["in_vn"], g["in_tr"])
+    t0 = og.ShallowWaterState(mesh0, params0)
+    assert _noalloc(mesh0, params0, s0, t0) == 0
+    og.sync()
+    wl = WORKLOADS["rk4_64x64"]
+    assert (wl.nx, wl.ny, wl.nlayers, wl.ntracers) == (64, 64, 64, 1)
+    cfg = dict(nx=64, ny=64, dc=wl.dc, K=64, T=1, f0=wl.f0, grav=wl.grav,
+               visc_del2=1e3, visc_del4=0.0, eddy_diff2=0.0, eddy_diff4=0.0)
+    mesh, params = _setup(cfg)
+    state = og.ShallowWaterState(mesh, params)
+    state.upload(*initial_state(mesh, wl))
+    tend = og.ShallowWaterState(mesh, params)
+    og.sync()
+    outs = []
+    for call in range(2):
+        before = _free_device_bytes()
+        assert _noalloc(mesh, params, state, tend) == 0, \
+            _capi.lib().swg_last_error()
+        og.sync()
+        assert _free_device_bytes() == before, f"call {call} allocated"
+        outs.append(tend.download())
+    ref = _allocating(mesh, params, state)
+    for out in outs:
+        for a, b in zip(out, ref):
+            assert rel_diff(a, b) <= TOL
