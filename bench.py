@@ -298,13 +298,21 @@ def adjoint_ratio(stream, nsteps=0, nsnap=0):
     ev[5].record(stream)
     torch.cuda.synchronize()
     f_ms, b_ms = ev[2].elapsed_time(ev[3]), ev[4].elapsed_time(ev[5])
-    plain, taped = adj.info()
+    plain, taped, tadv = adj.info_ex()
+    snap_b, tape_b, total_b = adj.memory()
     grad = G.download(stream=sh)
     return {"workload": wl.name, "steps": wl.nsteps,
             "snapshots": nsnap, "plain_forward_ms": fwd_ms,
             "checkpointed_forward_ms": f_ms, "backward_ms": b_ms,
             "ratio": (f_ms + b_ms) / fwd_ms, "plain_advances": plain,
-            "taped_steps": taped, "loss": L,
+            "taped_steps": taped, "taped_advances": tadv,
+            "classic_binomial_plain_advances": og.checkpoint_cost(wl.nsteps,
+                                                                  nsnap),
+            "memory": {"snapshot_bytes": snap_b, "tape_bytes": tape_b,
+                       "tapes": 2,
+                       "tape_in_snapshots": round(tape_b / snap_b, 2),
+                       "total_bytes": total_b},
+            "loss": L,
             "grad_h_norm": float(np.sqrt(np.sum(grad[0] ** 2)))}
 
 

@@ -400,9 +400,21 @@ int swg_adj_batch_forward(int n, const swg_adjoint *adjs,
                           void *const *streams);
 int swg_adj_batch_backward(int n, const swg_adjoint *adjs,
                            const swg_state *lambdas, void *const *streams);
-/* plain (re-)advanced and taped steps of the last forward/backward pair */
+/* plain (re-)advanced and taped steps of the last forward/backward pair;
+ * every step is taped once, either from a restored or re-advanced state or
+ * as a taped advance (a step whose tape is kept while its result continues
+ * the advance).  No counterpart in the reference. */
 int swg_adj_info(swg_adjoint adj, long long *plain_steps,
                  long long *taped_steps);
+/* the same, plus how many of the taped steps were taped advances */
+int swg_adj_info_ex(swg_adjoint adj, long long *plain_steps,
+                    long long *taped_steps, long long *taped_advances);
+/* device bytes of one snapshot (a state), of one tape (the stage inputs,
+ * accumulator and intermediates of one step; the adjoint holds two), and
+ * of everything the adjoint holds besides its tables.  No counterpart in
+ * the reference. */
+int swg_adj_memory(swg_adjoint adj, long long *snapshot_bytes,
+                   long long *tape_bytes, long long *total_bytes);
 /* Gradient of the loss whose dL/dx_N was given to the last swg_adj_backward
  * with respect to the del2 viscosity, host arrays (either may be NULL):
  * per edge, d L / d(visc_del2 * mesh_scaling_del2[e]); per cell, for a
@@ -413,9 +425,26 @@ int swg_adj_info(swg_adjoint adj, long long *plain_steps,
  * SWG_ERR_STATE until a backward sweep has completed. */
 int swg_adj_grad_visc(swg_adjoint adj, double *grad_edge, double *grad_cell,
                       void *stream);
-/* plain advances of the optimal binomial schedule (host only; -1 for
- * nsteps outside [1, 10000] or nsnapshots < 1) */
+/* plain advances of the classic optimal binomial schedule with one tape
+ * (Griewank-Walther; host only; -1 for nsteps outside [1, 10000] or
+ * nsnapshots < 1).  The adjoint's own planner, which also tapes the last
+ * step of a re-advance, needs fewer: swg_adj_plan. */
 long long swg_checkpoint_cost(int nsteps, int nsnapshots);
+/* the schedule the adjoint runs for nsteps steps, nsnapshots snapshots and
+ * a stepper of nstages stages (4: RK4; 5 or 1: LSRK): plain advances and
+ * taped advances, as swg_adj_info_ex reports them after a forward/backward
+ * pair (host only).  No counterpart in the reference. */
+int swg_adj_plan(int nsteps, int nsnapshots, int nstages,
+                 long long *plain_steps, long long *taped_advances);
+/* the same schedule as a list of actions (host only): *count actions, the
+ * first max_actions of them written as (type, a, b) triples.  Types:
+ * 0 advance `cur` from step a by b plain steps, 1 store `cur` in snapshot
+ * a, 2 restore `cur` from snapshot a, 3 tape step a from `cur` into tape b
+ * and reverse it, 4 taped advance of step a into tape b (its result
+ * replaces `cur`), 5 reverse step a from tape b, 6 end of the forward sweep
+ * (x_N in `cur`). */
+int swg_adj_schedule(int nsteps, int nsnapshots, int nstages,
+                     int max_actions, int *actions, int *count);
 
 /* ------------------------------------------------------- diagnostics -----
  * replaces energy_integral / mass_integral / circulation_integral

@@ -9,7 +9,8 @@ C++ classes (see shallow_water.py); the C++ mirror is cxx/omega_gpu.hpp.
 from .shallow_water import (AddMode, Adjoint, Batch, LSRKStepper,  # noqa: F401
                             HostStepper, pinned_empty,
                             MPASMesh, adjoint_batch_backward,
-                            adjoint_batch_forward, checkpoint_cost,
+                            adjoint_batch_forward, adjoint_plan,
+                            checkpoint_cost,
                             PlanarHexagonalMesh, RK4Stepper,
                             ShallowWaterModel, ShallowWaterParams,
                             ShallowWaterState, TimeStepper,
@@ -20,7 +21,7 @@ from .shallow_water import (AddMode, Adjoint, Batch, LSRKStepper,  # noqa: F401
 from ._capi import SwgError, exported_symbols  # noqa: F401
 from . import workloads  # noqa: F401
 
-__all__ = ["AddMode", "Adjoint", "Batch", "checkpoint_cost", "HostStepper",
+__all__ = ["AddMode", "Adjoint", "Batch", "adjoint_plan", "checkpoint_cost", "HostStepper",
            "pinned_empty",
            "LinearShallowWaterModel", "LinearShallowWaterParams",
            "adjoint_batch_forward", "adjoint_batch_backward", "LSRKStepper", "MPASMesh", "PlanarHexagonalMesh",

@@ -159,7 +159,18 @@ _SIGS = {
     "swg_adj_backward": (C.c_int, [_vp, _vp, _vp]),
     "swg_adj_info": (C.c_int, [_vp, C.POINTER(C.c_longlong),
                                C.POINTER(C.c_longlong)]),
+    "swg_adj_info_ex": (C.c_int, [_vp, C.POINTER(C.c_longlong),
+                                  C.POINTER(C.c_longlong),
+                                  C.POINTER(C.c_longlong)]),
+    "swg_adj_memory": (C.c_int, [_vp, C.POINTER(C.c_longlong),
+                                 C.POINTER(C.c_longlong),
+                                 C.POINTER(C.c_longlong)]),
     "swg_checkpoint_cost": (C.c_longlong, [C.c_int, C.c_int]),
+    "swg_adj_plan": (C.c_int, [C.c_int, C.c_int, C.c_int,
+                               C.POINTER(C.c_longlong),
+                               C.POINTER(C.c_longlong)]),
+    "swg_adj_schedule": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int,
+                                   C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "swg_adj_grad_visc": (C.c_int, [_vp, _dp, _dp, _vp]),
     "swg_adj_batch_forward": (C.c_int, [C.c_int, C.POINTER(_vp),
                                         C.POINTER(_vp), C.c_double,

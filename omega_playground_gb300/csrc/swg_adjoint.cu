@@ -25,10 +25,12 @@
 // taped forward step, mu_3 = dt b3 lam, mu_s = dt b_s lam + dt a_s lamX_{s+1},
 // lamX_s = J(X_s)^T mu_s, and lam_i = lam_{i+1} + sum_s lamX_s.
 //
-// Checkpointing: the optimal binomial schedule (Griewank-Walther) for n
-// steps and s snapshots, computed by dynamic programming over (n, s); the
-// forward sweep stores the schedule's checkpoints, the backward sweep
-// restores, re-advances and tapes each step once, in reverse order.
+// Checkpointing: a binomial schedule (Griewank-Walther) for n steps and s
+// snapshots with two tapes, computed by dynamic programming over (n, s):
+// the forward sweep stores the schedule's checkpoints and tapes the last
+// steps; the backward sweep restores, re-advances and reverses each step
+// once, in reverse order, taping the last step of a re-advance on the way
+// when the planner finds that cheaper (see Planner).
 #include "swg_device.cuh"
 
 #include <algorithm>
@@ -449,10 +451,41 @@ unsigned nb(long long n) { return unsigned((n + ATPB - 1) / ATPB); }
 
 using namespace swg;
 
+// Schedule actions.  ADV (a = first step, b = count) advances `cur` with
+// plain steps; STORE / RESTORE (a = slot) copy `cur` to / from a snapshot;
+// TAPE_ADJ (a = step, b = tape) tapes the step from `cur` into tape b and
+// runs its adjoint; TADV (a = step, b = tape) is a taped advance: the step
+// is taped into tape b and its result replaces `cur`; ADJ (a = step,
+// b = tape) runs the adjoint of a step taped earlier; FWD_END ends the
+// forward sweep (x_N is in `cur`).
+enum ActType { A_ADV = 0, A_STORE, A_RESTORE, A_TAPE_ADJ, A_TADV, A_ADJ,
+               A_FWD_END };
 struct AdjAction {
-  int type; // 0 advance(i, n), 1 store(slot), 2 restore(slot), 3 tape+adjoint(i)
+  int type;
   int a, b;
 };
+
+// A captured graph replayed while dt stays the same.
+struct AdjGraph {
+  cudaGraphExec_t exec = nullptr;
+  double dt = 0;
+  long long launches = 0; // kernels per replay
+};
+
+// One step's tape: the stage inputs, the taped step's accumulator and the
+// intermediates of every stage, with the graphs that write and read it.
+struct TapeSlot {
+  swg_state X[5] = {}; // stage inputs; X[0] is the step's start state
+  swg_state acc = nullptr;
+  AuxView taux[5]{};
+  AdjGraph tape_adj; // tape without the step's result, then its adjoint
+  AdjGraph tadv;     // taped advance: X[0] <- cur, tape, result into cur
+  AdjGraph adj;      // adjoint of the taped step
+  // recorded on the caller's stream after each use of the tape by an
+  // adjoint, so that a taped advance on the advance stream waits for it
+  cudaEvent_t free_ev = nullptr;
+};
+constexpr int kTapes = 2;
 
 struct swg_adjoint_s {
   swg_model model;
@@ -466,13 +499,9 @@ struct swg_adjoint_s {
   // rka / rkb are its coefficients (as in swg_stepper_create)
   int kind = SWG_STEPPER_RK4, ns = 4;
   std::vector<double> rka, rkb;
-  swg_state cur = nullptr, next = nullptr, X[5] = {}, acc = nullptr,
-            lam = nullptr, lacc = nullptr, mu = nullptr, mu2 = nullptr,
-            lX = nullptr;
-  AuxView taux[5]{};              // intermediates of the taped stages
-  cudaGraphExec_t tape_graph = nullptr;
-  double tape_graph_dt = 0;
-  long long tape_graph_launches = 0;
+  swg_state cur = nullptr, lam = nullptr, lacc = nullptr, mu = nullptr,
+            mu2 = nullptr;
+  TapeSlot tp[kTapes];
   // tangent-linear model buffers
   AuxViewT<Dual> daux{};
   Dual *dS = nullptr, *dacc = nullptr, *dP0 = nullptr, *dP1 = nullptr,
@@ -482,12 +511,13 @@ struct swg_adjoint_s {
   size_t pos = 0;
   int nsteps = 0;
   double t0 = 0, dt = 0;
-  long long plain_steps = 0, taped_steps = 0;
-  int state = 0; // 0 idle, 1 forward done (first step taped)
+  long long plain_steps = 0, taped_steps = 0, taped_advances = 0;
+  int state = 0; // 0 idle, 1 forward done (the last steps taped)
   bool grad_ready = false; // a backward sweep has completed
-  // backward sweep: restores, stores and plain advances run on `adv`,
-  // concurrently with the caller's stream, which tapes and reverses each
-  // step; `ready` = x_i is in cur, `freed` = cur was copied to the tape
+  // backward sweep: restores, stores, plain and taped advances run on
+  // `adv`, concurrently with the caller's stream, which tapes and reverses
+  // the steps; `ready` = the advance stream's work so far is done (x_i in
+  // cur, taped advances written), `freed` = cur was copied to a tape
   cudaStream_t adv = nullptr;
   cudaEvent_t go = nullptr, ready = nullptr, freed = nullptr;
 };
@@ -709,14 +739,14 @@ template <class T> int alloc_aux_like(swg_adjoint ad, AuxViewT<T> &d) {
   return SWG_OK;
 }
 
-// tape of stage s: the model's intermediates plus what the adjoint passes
-// would otherwise recompute (1/h_vertex, 1/h, mean thickness, and for the
-// stages whose final passes run in the taped step, the PV sum S1)
-int alloc_tape(swg_adjoint ad, int s) {
+// stage s of tape slot b: the model's intermediates plus what the adjoint
+// passes would otherwise recompute (1/h_vertex, 1/h, mean thickness, and for
+// the stages whose final passes run in the taped step, the PV sum S1)
+int alloc_tape(swg_adjoint ad, int b, int s) {
   swg_model md = ad->model;
   const size_t C = md->mesh->ncells, E = md->mesh->nedges,
                V = md->mesh->nvertices, K = md->mesh->nlayers;
-  AuxView &t = ad->taux[s];
+  AuxView &t = ad->tp[b].taux[s];
   auto &A = ad->allocs;
   TRY(alloc_aux_like(ad, t));
   if (md->view.do_vn) {
@@ -823,58 +853,60 @@ void lincomb(swg_state y, swg_state x1, swg_state x2, double a, double b,
   ++g_launches;
 }
 
-// stage input of the tape: a disabled field keeps its start-of-step value
-void stage_ptrs(swg_adjoint ad, int s, const double **h, const double **vn,
-                const double **tr) {
+// stage input of a tape: a disabled field keeps its start-of-step value
+void stage_ptrs(const swg_adjoint ad, const TapeSlot &tp, int s,
+                const double **h, const double **vn, const double **tr) {
   const ModelView &p = ad->model->view;
-  *h = p.do_h ? ad->X[s]->h : ad->X[0]->h;
-  *vn = p.do_vn ? ad->X[s]->vn : ad->X[0]->vn;
-  *tr = ad->X[s]->tr;
+  *h = p.do_h ? tp.X[s]->h : tp.X[0]->h;
+  *vn = p.do_vn ? tp.X[s]->vn : tp.X[0]->vn;
+  *tr = tp.X[s]->tr;
 }
 
-// Taped low-storage RK step (lsrk.cpp:36-89) from X0: stage s forms
-// T = a_s T + F(X_s) in ad->acc and X_{s+1} = X_s + dt b_s T in a separate
+// Taped low-storage RK step (lsrk.cpp:36-89) from tp.X[0]: stage s forms
+// T = a_s T + F(X_s) in tp.acc and X_{s+1} = X_s + dt b_s T in a separate
 // buffer (a copy of X_s updated by the same epilogue as the in-place
 // stepper, so the values are the stepper's bit for bit).  The last stage
 // only records its intermediates unless `out` takes the step's result.
-int tape_step_lsrk(swg_adjoint ad, double dt, swg_state out, cudaStream_t st) {
+int tape_step_lsrk(swg_adjoint ad, TapeSlot &tp, double dt, swg_state out,
+                   cudaStream_t st) {
   swg_model md = ad->model;
   const ModelView &pv = md->view;
   const int ns = ad->ns;
   for (int s = 0; s < ns; ++s) {
     const double *h, *vn, *tr;
-    stage_ptrs(ad, s, &h, &vn, &tr);
-    swg_state o = s < ns - 1 ? ad->X[s + 1] : out;
+    stage_ptrs(ad, tp, s, &h, &vn, &tr);
+    swg_state o = s < ns - 1 ? tp.X[s + 1] : out;
     if (!o) {
-      launch_aux(md->mesh->view, pv, ad->taux[s], h, vn, tr, st, &md->fork);
+      launch_aux(md->mesh->view, pv, tp.taux[s], h, vn, tr, st, &md->fork);
       continue;
     }
-    TRY(swg_state_copy(o, ad->X[s], st));
+    TRY(swg_state_copy(o, tp.X[s], st));
     StageArgs a{};
     a.h = h;
     a.vn = vn;
     a.tr = tr;
-    a.fh = {ad->acc->h, nullptr, nullptr, o->h};
-    a.fvn = {ad->acc->vn, nullptr, nullptr, o->vn};
-    a.ftr = {ad->acc->tr, nullptr, nullptr, o->tr};
+    a.fh = {tp.acc->h, nullptr, nullptr, o->h};
+    a.fvn = {tp.acc->vn, nullptr, nullptr, o->vn};
+    a.ftr = {tp.acc->tr, nullptr, nullptr, o->tr};
     a.ep = {EPI_LSRK, ad->rka[s], dt * ad->rkb[s], 0.0};
-    launch_tendency(md->mesh->view, pv, ad->taux[s], a, st, &md->fork);
+    launch_tendency(md->mesh->view, pv, tp.taux[s], a, st, &md->fork);
   }
-  ++ad->taped_steps;
   cudaError_t err = cudaGetLastError();
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_adjoint: taped step");
 }
 
-// Taped RK4 step from X0 (the caller copies the step's start state there):
-// X1..X3 the stage inputs, and (when `out` is given) the step's result.
-int tape_step(swg_adjoint ad, double dt, swg_state out, cudaStream_t st) {
+// Taped RK4 step from tp.X[0] (the caller copies the step's start state
+// there): X1..X3 the stage inputs, and (when `out` is given) the step's
+// result.
+int tape_step(swg_adjoint ad, TapeSlot &tp, double dt, swg_state out,
+              cudaStream_t st) {
   if (ad->kind != SWG_STEPPER_RK4)
-    return tape_step_lsrk(ad, dt, out, st);
+    return tape_step_lsrk(ad, tp, dt, out, st);
   swg_model md = ad->model;
   const ModelView &pv = md->view;
   static const double rka[3] = {1. / 2, 1. / 2, 1};
   static const double rkb[4] = {1. / 6, 1. / 3, 1. / 3, 1. / 6};
-  swg_state S = ad->X[0];
+  swg_state S = tp.X[0];
   const int last = out ? 3 : 2;
   if (out) {
     // a field whose tendency is disabled ends the step as it began; the
@@ -894,30 +926,29 @@ int tape_step(swg_adjoint ad, double dt, swg_state out, cudaStream_t st) {
   for (int s = 0; s <= last; ++s) {
     StageArgs a{};
     const double *h, *vn, *tr;
-    stage_ptrs(ad, s, &h, &vn, &tr);
+    stage_ptrs(ad, tp, s, &h, &vn, &tr);
     a.h = h;
     a.vn = vn;
     a.tr = tr;
-    swg_state o = s < 3 ? ad->X[s + 1] : out;
-    a.fh = {nullptr, S->h, ad->acc->h, o->h};
-    a.fvn = {nullptr, S->vn, ad->acc->vn, o->vn};
-    a.ftr = {nullptr, S->tr, ad->acc->tr, o->tr};
+    swg_state o = s < 3 ? tp.X[s + 1] : out;
+    a.fh = {nullptr, S->h, tp.acc->h, o->h};
+    a.fvn = {nullptr, S->vn, tp.acc->vn, o->vn};
+    a.ftr = {nullptr, S->tr, tp.acc->tr, o->tr};
     const int mode = s == 0 ? EPI_RK4_FIRST : (s < 3 ? EPI_RK4_MID : EPI_RK4_LAST);
     a.ep = {mode, 0.0, dt * rkb[s], s < 3 ? dt * rka[s] : 0.0};
-    launch_tendency(md->mesh->view, pv, ad->taux[s], a, st, &md->fork);
+    launch_tendency(md->mesh->view, pv, tp.taux[s], a, st, &md->fork);
   }
   if (!out) { // intermediates of the last stage input
     const double *h, *vn, *tr;
-    stage_ptrs(ad, 3, &h, &vn, &tr);
-    launch_aux(md->mesh->view, pv, ad->taux[3], h, vn, tr, st, &md->fork);
+    stage_ptrs(ad, tp, 3, &h, &vn, &tr);
+    launch_aux(md->mesh->view, pv, tp.taux[3], h, vn, tr, st, &md->fork);
   }
-  ++ad->taped_steps;
   cudaError_t err = cudaGetLastError();
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_adjoint: taped step");
 }
 
-// lam <- adjoint of the taped step applied to lam.  The output passes of
-// stage s accumulate lamX_s into lacc and form mu_{s-1} directly
+// lam <- adjoint of the step taped in tp, applied to lam.  The output passes
+// of stage s accumulate lamX_s into lacc and form mu_{s-1} directly
 // (ping-pong mu buffers: the passes of stage s still read mu_s).
 //
 // Low-storage RK (ns stages): with lamX_s the adjoint of the stage input X_s
@@ -925,7 +956,8 @@ int tape_step(swg_adjoint ad, double dt, swg_state out, cudaStream_t st) {
 // lamX_s = lamX_{s+1} + J(X_s)^T mu_s and
 // mu_{s-1} = dt b_{s-1} lamX_s + a_s mu_s; the step's adjoint is lamX_0.
 // The output passes accumulate lamX in lacc and form mu_{s-1} from it.
-int adjoint_step(swg_adjoint ad, double dt, cudaStream_t st) {
+int adjoint_step(swg_adjoint ad, const TapeSlot &tp, double dt,
+                 cudaStream_t st) {
   static const double rk4a[3] = {1. / 2, 1. / 2, 1};
   static const double rk4b[4] = {1. / 6, 1. / 3, 1. / 3, 1. / 6};
   const bool lsrk = ad->kind != SWG_STEPPER_RK4;
@@ -942,7 +974,7 @@ int adjoint_step(swg_adjoint ad, double dt, cudaStream_t st) {
   for (int s = ns - 1; s >= 0; --s) {
     swg_state mu = mus[(ns - 1 - s) % 2], nmu = mus[(ns - s) % 2];
     AdjIO io{};
-    stage_ptrs(ad, s, &io.h, &io.vn, &io.tr);
+    stage_ptrs(ad, tp, s, &io.h, &io.vn, &io.tr);
     io.mh_ = mu->h;
     io.mvn = mu->vn;
     io.mtr = mu->tr;
@@ -961,7 +993,7 @@ int adjoint_step(swg_adjoint ad, double dt, cudaStream_t st) {
       io.gamma = lsrk ? rka[s] : 0.0;
       io.lsrk = lsrk;
     }
-    adj_passes(ad, ad->taux[s], io, st);
+    adj_passes(ad, tp.taux[s], io, st);
   }
   err = cudaMemcpyAsync(ad->lam->h, ad->lacc->h, n * 8,
                         cudaMemcpyDeviceToDevice, st);
@@ -970,141 +1002,282 @@ int adjoint_step(swg_adjoint ad, double dt, cudaStream_t st) {
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_adjoint: adjoint step");
 }
 
-// ---- binomial schedule
-// The planner's dynamic program costs O(nsteps^2 * snapshots) host work
-// (about a second at the step limit); a schedule that re-runs more than
+// ---- checkpoint schedule
+// The planner's dynamic programs cost O(nsteps^2 * snapshots) host work
+// (seconds at the step limit); a schedule that re-runs more than
 // kMaxReadvance plain steps per step is refused as a too small budget.
 constexpr int kMaxAdjointSteps = 10000;
 constexpr long long kMaxReadvance = 32;
 
-struct Planner {
-  int N, S;
-  std::vector<long long> cost; // (n, s) -> plain advances; n in [0,N], s in [0,S]
-  std::vector<int> split;
-  long long &C(int n, int s) { return cost[size_t(n) * (S + 1) + s]; }
-  int &M(int n, int s) { return split[size_t(n) * (S + 1) + s]; }
-  Planner(int n, int s) : N(n), S(s), cost(size_t(n + 1) * (s + 1), 0),
-                          split(size_t(n + 1) * (s + 1), 0) {
-    for (int nn = 1; nn <= N; ++nn) {
-      C(nn, 0) = (long long)nn * (nn - 1) / 2;
-      for (int ss = 1; ss <= S; ++ss) {
-        if (nn == 1) {
-          C(nn, ss) = 0;
-          continue;
-        }
-        long long best = -1;
-        int bm = 1;
-        for (int m = 1; m < nn; ++m) {
-          const long long c = m + C(nn - m, ss - 1) + C(m, ss);
-          if (best < 0 || c < best) {
-            best = c;
-            bm = m;
-          }
-        }
-        C(nn, ss) = best;
-        M(nn, ss) = bm;
+// The classic optimal binomial schedule (Griewank-Walther) with one tape:
+// plain advances cost(n, s) = min_m [m + cost(n - m, s - 1) + cost(m, s)],
+// cost(n, 0) = n (n - 1) / 2.  Reported by swg_checkpoint_cost as the
+// count the planner below improves on.
+long long classic_binomial_cost(int N, int S) {
+  std::vector<long long> c(size_t(N + 1) * (S + 1), 0);
+  auto C = [&](int n, int s) -> long long & { return c[size_t(n) * (S + 1) + s]; };
+  for (int n = 1; n <= N; ++n) {
+    C(n, 0) = (long long)n * (n - 1) / 2;
+    for (int s = 1; s <= S; ++s) {
+      if (n == 1)
+        continue;
+      long long best = -1;
+      for (int m = 1; m < n; ++m) {
+        const long long x = m + C(n - m, s - 1) + C(m, s);
+        if (best < 0 || x < best)
+          best = x;
       }
+      C(n, s) = best;
     }
   }
-  // reverse steps [i0, i0+n) with x_{i0} in `cur` and in slot `slot`;
-  // `s` further slots free (slot+1 ...)
-  void gen(std::vector<AdjAction> &out, int i0, int n, int s, int slot,
-           bool cur_ok) {
-    if (n == 1) {
-      if (!cur_ok)
-        out.push_back({2, slot, 0});
-      out.push_back({3, i0, 0});
-      return;
-    }
-    if (s == 0) {
-      for (int j = n - 1; j >= 0; --j) {
-        if (!cur_ok || j < n - 1)
-          out.push_back({2, slot, 0});
-        if (j > 0)
-          out.push_back({0, i0, j});
-        out.push_back({3, i0 + j, 0});
+  return C(N, S);
+}
+
+// Checkpoint schedule with two tapes.  Reversing a step needs its tape
+// (stage inputs and intermediates).  The classic schedule restores a
+// checkpoint, re-advances to x_i and tapes step i from it; but the last
+// step of that re-advance is step i - 1, the very next step to reverse.
+// Here it can run as a taped advance into the second tape, at about the
+// cost of a plain step, so the next reversal needs no restore, no
+// re-advance and no tape.  A dynamic program picks, for every range of
+// steps and snapshot budget, between that pair (advance to x_{i-1}, taped
+// advance of step i-1, tape of step i, both adjoints) and the binomial
+// split (advance m steps, store a checkpoint, reverse the right part with
+// one snapshot fewer, then the left part).  Costs are in hundredths of a
+// plain step: a taped advance 104 (the plain step plus the tape's extra
+// writes), a tape from a state (all but the last stage, plus the last
+// stage's intermediates, about 40 per cent of a stage) (100 (ns - 1) + 40)
+// / ns.  The adjoints cost the same under every schedule and are left out.
+//
+//   f(n, s): reverse steps [i0, i0 + n) with x_{i0} available (in `cur` or
+//            a snapshot) and s free snapshots;
+//   h(n, s): the same, starting the forward sweep: it also produces
+//            x_{i0+n}, whose last step is taped on the way (taped advances).
+struct Planner {
+  int N, S;
+  long long cADV = 100, cTADV = 104, cTAPE = 85;
+  std::vector<long long> f, h;
+  std::vector<int> fm, hm; // 0: the taped pair; m > 0: split after m steps
+  size_t at(int n, int s) const { return size_t(n) * (S + 1) + s; }
+  Planner(int n, int s, int ns)
+      : N(n), S(std::max(0, std::min(s, n - 1))) {
+    cTAPE = (100LL * (ns - 1) + 40) / ns;
+    const size_t sz = size_t(N + 1) * (S + 1);
+    f.assign(sz, 0);
+    h.assign(sz, 0);
+    fm.assign(sz, 0);
+    hm.assign(sz, 0);
+    for (int nn = 1; nn <= N; ++nn)
+      for (int ss = 0; ss <= S; ++ss) {
+        if (nn == 1) {
+          f[at(1, ss)] = cTAPE;
+          h[at(1, ss)] = cTADV;
+          continue;
+        }
+        const long long rest = f[at(nn - 2, ss)] + (nn - 2) * cADV + cTADV;
+        long long bf = rest + cTAPE, bh = rest + cTADV;
+        int mf = 0, mh = 0;
+        if (ss > 0)
+          for (int m = 1; m < nn; ++m) {
+            const long long base = m * cADV + f[at(m, ss)];
+            const long long cf = base + f[at(nn - m, ss - 1)];
+            const long long ch = base + h[at(nn - m, ss - 1)];
+            if (cf < bf) {
+              bf = cf;
+              mf = m;
+            }
+            if (ch < bh) {
+              bh = ch;
+              mh = m;
+            }
+          }
+        f[at(nn, ss)] = bf;
+        fm[at(nn, ss)] = mf;
+        h[at(nn, ss)] = bh;
+        hm[at(nn, ss)] = mh;
       }
+  }
+  // reverse [i0, i0 + n): x_{i0} in `cur` (cur_ok) or in snapshot `slot`;
+  // slots slot+1 ... slot+s are free.  Tape 0 takes steps taped from a
+  // state, tape 1 the taped advances of the pairs.
+  void gen_f(std::vector<AdjAction> &out, int i0, int n, int s, int slot,
+             bool cur_ok) const {
+    while (n > 0) {
+      if (!cur_ok)
+        out.push_back({A_RESTORE, slot, 0});
+      if (n == 1) {
+        out.push_back({A_TAPE_ADJ, i0, 0});
+        return;
+      }
+      const int m = fm[at(n, s)];
+      if (m == 0) {
+        if (n > 2)
+          out.push_back({A_ADV, i0, n - 2});
+        out.push_back({A_TADV, i0 + n - 2, 1});
+        out.push_back({A_TAPE_ADJ, i0 + n - 1, 0});
+        out.push_back({A_ADJ, i0 + n - 2, 1});
+        n -= 2;
+      } else {
+        out.push_back({A_ADV, i0, m});
+        out.push_back({A_STORE, slot + 1, 0});
+        gen_f(out, i0 + m, n - m, s - 1, slot + 1, true);
+        n = m;
+      }
+      cur_ok = false;
+    }
+  }
+  // the whole schedule from x_{i0} in `cur` and snapshot `slot`: the
+  // forward sweep up to A_FWD_END (x_{i0+n} in `cur`, the last steps
+  // taped), then the reversal
+  void gen_h(std::vector<AdjAction> &out, int i0, int n, int s,
+             int slot) const {
+    if (n == 1) {
+      out.push_back({A_TADV, i0, 0});
+      out.push_back({A_FWD_END, 0, 0});
+      out.push_back({A_ADJ, i0, 0});
       return;
     }
-    const int m = M(n, s);
-    if (!cur_ok)
-      out.push_back({2, slot, 0});
-    out.push_back({0, i0, m});
-    out.push_back({1, slot + 1, 0});
-    gen(out, i0 + m, n - m, s - 1, slot + 1, true);
-    gen(out, i0, m, s, slot, false);
+    const int m = hm[at(n, s)];
+    if (m == 0) {
+      if (n > 2)
+        out.push_back({A_ADV, i0, n - 2});
+      out.push_back({A_TADV, i0 + n - 2, 1});
+      out.push_back({A_TADV, i0 + n - 1, 0});
+      out.push_back({A_FWD_END, 0, 0});
+      out.push_back({A_ADJ, i0 + n - 1, 0});
+      out.push_back({A_ADJ, i0 + n - 2, 1});
+      gen_f(out, i0, n - 2, s, slot, false);
+      return;
+    }
+    out.push_back({A_ADV, i0, m});
+    out.push_back({A_STORE, slot + 1, 0});
+    gen_h(out, i0 + m, n - m, s - 1, slot + 1);
+    gen_f(out, i0, m, s, slot, false);
+  }
+  // the schedule of nsteps steps (the planner's N), snapshot 0 holding x_0
+  std::vector<AdjAction> schedule() const {
+    std::vector<AdjAction> out;
+    out.push_back({A_STORE, 0, 0});
+    gen_h(out, 0, N, S, 0);
+    return out;
   }
 };
 
-// One schedule action on stream st.  With `two` (backward sweep) the
-// restores, stores and advances go to ad->adv instead, and a tape+adjoint
-// action hands x_i over from it through the ready / freed events.
-int run_action(swg_adjoint ad, const AdjAction &a, cudaStream_t st, bool two) {
-  cudaStream_t q = two ? ad->adv : st;
-  switch (a.type) {
-  case 0:
-    ad->plain_steps += a.b;
-    return swg_step(ad->stepper, ad->cur, ad->t0 + a.a * ad->dt, ad->dt, a.b,
-                    1, q);
-  case 1:
-    return swg_state_copy(ad->snaps[a.a], ad->cur, q);
-  case 2:
-    return swg_state_copy(ad->cur, ad->snaps[a.a], q);
-  default:
-    break;
+void count_actions(const std::vector<AdjAction> &acts, long long *plain,
+                   long long *tadv) {
+  *plain = *tadv = 0;
+  for (const AdjAction &a : acts) {
+    if (a.type == A_ADV)
+      *plain += a.b;
+    else if (a.type == A_TADV)
+      ++*tadv;
   }
-  cudaError_t e = cudaSuccess;
-  if (two && ((e = cudaEventRecord(ad->ready, ad->adv)) != cudaSuccess ||
-              (e = cudaStreamWaitEvent(st, ad->ready, 0)) != cudaSuccess))
-    return cuda_fail(e, "swg_adjoint: stream handshake");
-  TRY(swg_state_copy(ad->X[0], ad->cur, st));
-  if (two && ((e = cudaEventRecord(ad->freed, st)) != cudaSuccess ||
-              (e = cudaStreamWaitEvent(ad->adv, ad->freed, 0)) != cudaSuccess))
-    return cuda_fail(e, "swg_adjoint: stream handshake");
-  // tape + adjoint of one step: the same launches every time (no forcing),
-  // replayed from a CUDA graph captured on first use
-  if (!ad->tape_graph || ad->tape_graph_dt != ad->dt) {
-    if (ad->tape_graph) {
-      cudaGraphExecDestroy(ad->tape_graph);
-      ad->tape_graph = nullptr;
+}
+
+// Captures `record` once (per dt) into g on a private stream and replays
+// it on st; when capture fails the launches run directly on st.
+template <class Fn>
+int replay(swg_adjoint ad, AdjGraph &g, cudaStream_t st, Fn record) {
+  if (!g.exec || g.dt != ad->dt) {
+    if (g.exec) {
+      cudaGraphExecDestroy(g.exec);
+      g.exec = nullptr;
     }
     cudaStream_t cs;
     cudaError_t err = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (err != cudaSuccess)
       return cuda_fail(err, "swg_adjoint: capture stream");
     const long long before = g_launches.load();
-    const long long taped = ad->taped_steps;
     err = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     int rc = SWG_OK;
-    if (err == cudaSuccess && (rc = tape_step(ad, ad->dt, nullptr, cs)) == SWG_OK)
-      rc = adjoint_step(ad, ad->dt, cs);
-    cudaGraph_t g = nullptr;
-    cudaError_t err2 = cudaStreamEndCapture(cs, &g);
-    ad->tape_graph_launches = g_launches.load() - before;
-    g_launches -= ad->tape_graph_launches;
-    ad->taped_steps = taped;
+    if (err == cudaSuccess)
+      rc = record(cs);
+    cudaGraph_t gr = nullptr;
+    cudaError_t err2 = cudaStreamEndCapture(cs, &gr);
+    g.launches = g_launches.load() - before;
+    g_launches -= g.launches;
     cudaStreamDestroy(cs);
     if (err != cudaSuccess || err2 != cudaSuccess || rc != SWG_OK) {
-      if (g)
-        cudaGraphDestroy(g);
+      if (gr)
+        cudaGraphDestroy(gr);
       (void)cudaGetLastError();
-      TRY(tape_step(ad, ad->dt, nullptr, st)); // direct launches
-      return adjoint_step(ad, ad->dt, st);
+      return record(st); // direct launches
     }
-    err = cudaGraphInstantiate(&ad->tape_graph, g, 0);
-    cudaGraphDestroy(g);
+    err = cudaGraphInstantiate(&g.exec, gr, 0);
+    cudaGraphDestroy(gr);
     if (err != cudaSuccess) {
-      ad->tape_graph = nullptr;
+      g.exec = nullptr;
       return cuda_fail(err, "swg_adjoint: graph instantiate");
     }
-    ad->tape_graph_dt = ad->dt;
+    g.dt = ad->dt;
   }
-  cudaError_t err = cudaGraphLaunch(ad->tape_graph, st);
+  cudaError_t err = cudaGraphLaunch(g.exec, st);
   if (err != cudaSuccess)
     return cuda_fail(err, "swg_adjoint: graph launch");
-  g_launches += ad->tape_graph_launches;
-  ++ad->taped_steps;
+  g_launches += g.launches;
   return SWG_OK;
+}
+
+// One schedule action on stream st.  With `two` (backward sweep) the
+// restores, stores and plain and taped advances go to ad->adv instead; the
+// adjoints run on st after the advance stream's work queued so far (event
+// `ready`), a tape from `cur` hands `cur` back through `freed`, and a taped
+// advance into a tape waits until the adjoint that last read that tape is
+// done (the tape's free_ev).
+int run_action(swg_adjoint ad, const AdjAction &a, cudaStream_t st, bool two) {
+  cudaStream_t q = two ? ad->adv : st;
+  cudaError_t e = cudaSuccess;
+  switch (a.type) {
+  case A_ADV:
+    ad->plain_steps += a.b;
+    return swg_step(ad->stepper, ad->cur, ad->t0 + a.a * ad->dt, ad->dt, a.b,
+                    1, q);
+  case A_STORE:
+    return swg_state_copy(ad->snaps[a.a], ad->cur, q);
+  case A_RESTORE:
+    return swg_state_copy(ad->cur, ad->snaps[a.a], q);
+  case A_TADV: {
+    TapeSlot &tp = ad->tp[a.b];
+    if (two && (e = cudaStreamWaitEvent(q, tp.free_ev, 0)) != cudaSuccess)
+      return cuda_fail(e, "swg_adjoint: stream handshake");
+    ++ad->taped_steps;
+    ++ad->taped_advances;
+    return replay(ad, tp.tadv, q, [&](cudaStream_t cs) {
+      TRY(swg_state_copy(tp.X[0], ad->cur, cs));
+      return tape_step(ad, tp, ad->dt, ad->cur, cs);
+    });
+  }
+  case A_TAPE_ADJ:
+  case A_ADJ:
+    break;
+  default:
+    return SWG_OK;
+  }
+  TapeSlot &tp = ad->tp[a.b];
+  if (two && ((e = cudaEventRecord(ad->ready, ad->adv)) != cudaSuccess ||
+              (e = cudaStreamWaitEvent(st, ad->ready, 0)) != cudaSuccess))
+    return cuda_fail(e, "swg_adjoint: stream handshake");
+  int rc;
+  if (a.type == A_TAPE_ADJ) {
+    TRY(swg_state_copy(tp.X[0], ad->cur, st));
+    if (two && ((e = cudaEventRecord(ad->freed, st)) != cudaSuccess ||
+                (e = cudaStreamWaitEvent(ad->adv, ad->freed, 0)) != cudaSuccess))
+      return cuda_fail(e, "swg_adjoint: stream handshake");
+    ++ad->taped_steps;
+    // tape + adjoint of one step: the same launches every time (no
+    // forcing), replayed from a graph captured on first use
+    rc = replay(ad, tp.tape_adj, st, [&](cudaStream_t cs) {
+      TRY(tape_step(ad, tp, ad->dt, nullptr, cs));
+      return adjoint_step(ad, tp, ad->dt, cs);
+    });
+  } else {
+    rc = replay(ad, tp.adj, st, [&](cudaStream_t cs) {
+      return adjoint_step(ad, tp, ad->dt, cs);
+    });
+  }
+  if (rc == SWG_OK && two && (e = cudaEventRecord(tp.free_ev, st)) != cudaSuccess)
+    return cuda_fail(e, "swg_adjoint: stream handshake");
+  return rc;
 }
 
 int check_model(swg_model md) {
@@ -1172,13 +1345,16 @@ extern "C" int swg_adjoint_create_stepper(swg_model md, int nsnapshots,
        (rc = zal(A, E * K, &w.Qmu)) ||
        (md->view.vel_del2 && (rc = zal(A, E * K, &w.gc2e)))))
     ;
-  swg_state *st[] = {&ad->cur, &ad->next, &ad->acc, &ad->lam, &ad->lacc,
-                     &ad->mu, &ad->mu2, &ad->lX};
+  swg_state *st[] = {&ad->cur, &ad->lam, &ad->lacc, &ad->mu, &ad->mu2};
   for (auto *p : st)
     if (rc == SWG_OK)
       rc = swg_state_create(md->mesh, T, p);
-  for (int s = 0; s < ad->ns && rc == SWG_OK; ++s) // stage inputs of the tape
-    rc = swg_state_create(md->mesh, T, &ad->X[s]);
+  for (int b = 0; b < kTapes; ++b) { // stage inputs and accumulator of a tape
+    for (int s = 0; s < ad->ns && rc == SWG_OK; ++s)
+      rc = swg_state_create(md->mesh, T, &ad->tp[b].X[s]);
+    if (rc == SWG_OK)
+      rc = swg_state_create(md->mesh, T, &ad->tp[b].acc);
+  }
   for (int s = 0; s < nsnapshots && rc == SWG_OK; ++s) {
     swg_state x = nullptr;
     rc = swg_state_create(md->mesh, T, &x);
@@ -1192,7 +1368,8 @@ extern "C" int swg_adjoint_create_stepper(swg_model md, int nsnapshots,
   }
   if (rc == SWG_OK) {
     cudaError_t e = cudaStreamCreateWithFlags(&ad->adv, cudaStreamNonBlocking);
-    for (cudaEvent_t *ev : {&ad->go, &ad->ready, &ad->freed})
+    for (cudaEvent_t *ev : {&ad->go, &ad->ready, &ad->freed,
+                            &ad->tp[0].free_ev, &ad->tp[1].free_ev})
       if (e == cudaSuccess)
         e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     if (e != cudaSuccess)
@@ -1204,8 +1381,9 @@ extern "C" int swg_adjoint_create_stepper(swg_model md, int nsnapshots,
                        (rc = zal(A, n, &ad->dacc)) || (rc = zal(A, n, &ad->dP0)) ||
                        (rc = zal(A, n, &ad->dP1)) || (rc = zal(A, n, &ad->dT))))
     ;
-  for (int s = 0; s < ad->ns && rc == SWG_OK; ++s)
-    rc = alloc_tape(ad, s);
+  for (int b = 0; b < kTapes; ++b)
+    for (int s = 0; s < ad->ns && rc == SWG_OK; ++s)
+      rc = alloc_tape(ad, b, s);
   if (rc != SWG_OK) {
     swg_adjoint_destroy(ad);
     return rc;
@@ -1218,16 +1396,22 @@ extern "C" int swg_adjoint_destroy(swg_adjoint ad) {
   if (!ad)
     return SWG_OK;
   swg_stepper_destroy(ad->stepper);
-  if (ad->tape_graph)
-    cudaGraphExecDestroy(ad->tape_graph);
+  for (TapeSlot &tp : ad->tp) {
+    for (AdjGraph *g : {&tp.tape_adj, &tp.tadv, &tp.adj})
+      if (g->exec)
+        cudaGraphExecDestroy(g->exec);
+    if (tp.free_ev)
+      cudaEventDestroy(tp.free_ev);
+    for (swg_state x : tp.X)
+      swg_state_destroy(x);
+    swg_state_destroy(tp.acc);
+  }
   for (cudaEvent_t e : {ad->go, ad->ready, ad->freed})
     if (e)
       cudaEventDestroy(e);
   if (ad->adv)
     cudaStreamDestroy(ad->adv);
-  swg_state st[] = {ad->cur, ad->next, ad->X[0], ad->X[1], ad->X[2], ad->X[3],
-                    ad->X[4],
-                    ad->acc, ad->lam, ad->lacc, ad->mu, ad->mu2, ad->lX};
+  swg_state st[] = {ad->cur, ad->lam, ad->lacc, ad->mu, ad->mu2};
   for (auto s : st)
     swg_state_destroy(s);
   for (auto s : ad->snaps)
@@ -1376,8 +1560,11 @@ int fwd_begin(swg_adjoint ad, swg_state state0, double t0, double dt,
   if (ad->model->terms_switched)
     return fail(SWG_ERR_STATE, "swg_adj_forward: a tendency term of the model "
                                "was switched after the adjoint was created");
-  Planner pl(nsteps, ad->nsnap - 1);
-  if (pl.C(nsteps, ad->nsnap - 1) > kMaxReadvance * (long long)nsteps)
+  Planner pl(nsteps, ad->nsnap - 1, ad->ns);
+  std::vector<AdjAction> acts = pl.schedule();
+  long long plain, tadv;
+  count_actions(acts, &plain, &tadv);
+  if (plain > kMaxReadvance * (long long)nsteps)
     return fail(SWG_ERR_BUDGET, "swg_adj_forward: too few snapshots: the "
                                 "schedule would re-run more than 32 plain "
                                 "steps per step; give the adjoint more "
@@ -1385,29 +1572,22 @@ int fwd_begin(swg_adjoint ad, swg_state state0, double t0, double dt,
   ad->t0 = t0;
   ad->dt = dt;
   ad->nsteps = nsteps;
-  ad->plain_steps = ad->taped_steps = 0;
-  ad->actions.clear();
-  ad->actions.push_back({1, 0, 0});
-  pl.gen(ad->actions, 0, nsteps, ad->nsnap - 1, 0, true);
+  ad->plain_steps = ad->taped_steps = ad->taped_advances = 0;
+  ad->actions.swap(acts);
   ad->pos = 0;
   ad->state = 0;
   return swg_state_copy(ad->cur, state0, st);
 }
 
-// the forward sweep runs the schedule up to its first tape+adjoint action
-// (step nsteps-1), then tapes that step, producing x_N
+// the forward sweep runs the schedule up to its end marker: x_N is then in
+// `cur` and the last steps are taped
 int fwd_next(swg_adjoint ad, swg_state final_out, cudaStream_t st, bool *done) {
-  const AdjAction &a = ad->actions[ad->pos];
-  if (a.type != 3) {
-    ++ad->pos;
+  const AdjAction &a = ad->actions[ad->pos++];
+  if (a.type != A_FWD_END) {
     *done = false;
     return run_action(ad, a, st, false);
   }
-  if (a.a != ad->nsteps - 1)
-    return fail(SWG_ERR_STATE, "swg_adj_forward: unexpected schedule");
-  TRY(swg_state_copy(ad->X[0], ad->cur, st));
-  TRY(tape_step(ad, ad->dt, ad->next, st));
-  TRY(swg_state_copy(final_out, ad->next, st));
+  TRY(swg_state_copy(final_out, ad->cur, st));
   ad->state = 1;
   *done = true;
   return SWG_OK;
@@ -1428,8 +1608,6 @@ int bwd_begin(swg_adjoint ad, swg_state lambda, cudaStream_t st) {
     if (err != cudaSuccess)
       return cuda_fail(err, "swg_adj_backward: reset parameter gradient");
   }
-  TRY(adjoint_step(ad, ad->dt, st)); // the last step is already taped
-  ++ad->pos;
   return SWG_OK;
 }
 
@@ -1564,6 +1742,60 @@ extern "C" int swg_adj_info(swg_adjoint ad, long long *plain_steps,
   return SWG_OK;
 }
 
+extern "C" int swg_adj_info_ex(swg_adjoint ad, long long *plain_steps,
+                               long long *taped_steps,
+                               long long *taped_advances) {
+  if (!ad)
+    return fail(SWG_ERR_ARG, "swg_adj_info_ex: NULL");
+  TRY(swg_adj_info(ad, plain_steps, taped_steps));
+  if (taped_advances)
+    *taped_advances = ad->taped_advances;
+  return SWG_OK;
+}
+
+// bytes of the arrays of an intermediate set (null members not counted)
+size_t aux_bytes(const AuxView &a, size_t C, size_t E, size_t V, size_t K,
+                 size_t T) {
+  size_t w = 0;
+  for (const double *p : {a.q, a.zeta, a.z4, a.rhv})
+    w += p ? V * K : 0;
+  for (const double *p : {a.div, a.ke, a.d4, a.rh})
+    w += p ? C * K : 0;
+  for (const double *p : {a.ntr, a.lap})
+    w += p ? T * C * K : 0;
+  for (const double *p : {a.F, a.G, a.Q, a.mh, a.u2, a.d2u, a.S1})
+    w += p ? E * K : 0;
+  if (a.d2u4 && a.d2u4 != a.d2u)
+    w += E * K;
+  return w * sizeof(double);
+}
+
+extern "C" int swg_adj_memory(swg_adjoint ad, long long *snapshot_bytes,
+                              long long *tape_bytes, long long *total_bytes) {
+  if (!ad)
+    return fail(SWG_ERR_ARG, "swg_adj_memory: NULL");
+  swg_model md = ad->model;
+  const size_t C = md->mesh->ncells, E = md->mesh->nedges,
+               V = md->mesh->nvertices, K = md->mesh->nlayers,
+               T = md->params.ntracers;
+  const size_t state = words(md) * sizeof(double);
+  size_t tape = 0;
+  for (int s = 0; s < ad->ns; ++s)
+    tape += aux_bytes(ad->tp[0].taux[s], C, E, V, K, T);
+  tape += size_t(ad->ns + 1) * state; // stage inputs and accumulator
+  if (snapshot_bytes)
+    *snapshot_bytes = (long long)state;
+  if (tape_bytes)
+    *tape_bytes = (long long)tape;
+  if (total_bytes) // snapshots, both tapes, the sweep's own states (cur,
+                   // lam, lacc, mu, mu2) and the adjoint work arrays
+    *total_bytes = (long long)(size_t(ad->nsnap + 5) * state + kTapes * tape +
+                               (2 * T * C + 4 * C + 3 * V + 5 * E) * K *
+                                   sizeof(double) +
+                               (ad->aw.gc2e ? E * K * sizeof(double) : 0));
+  return SWG_OK;
+}
+
 extern "C" int swg_adj_grad_visc(swg_adjoint ad, double *grad_edge,
                                  double *grad_cell, void *stream) {
   if (!ad)
@@ -1604,6 +1836,37 @@ extern "C" int swg_adj_grad_visc(swg_adjoint ad, double *grad_edge,
 extern "C" long long swg_checkpoint_cost(int nsteps, int nsnapshots) {
   if (nsteps < 1 || nsnapshots < 1 || nsteps > kMaxAdjointSteps)
     return -1;
-  Planner pl(nsteps, nsnapshots - 1);
-  return pl.C(nsteps, nsnapshots - 1);
+  return classic_binomial_cost(nsteps, nsnapshots - 1);
+}
+
+extern "C" int swg_adj_plan(int nsteps, int nsnapshots, int nstages,
+                            long long *plain_steps, long long *taped_advances) {
+  if (nsteps < 1 || nsnapshots < 1 || nsteps > kMaxAdjointSteps ||
+      !(nstages == 4 || nstages == 5 || nstages == 1))
+    return fail(SWG_ERR_ARG, "swg_adj_plan: bad argument");
+  long long p = 0, t = 0;
+  count_actions(Planner(nsteps, nsnapshots - 1, nstages).schedule(), &p, &t);
+  if (plain_steps)
+    *plain_steps = p;
+  if (taped_advances)
+    *taped_advances = t;
+  return SWG_OK;
+}
+
+extern "C" int swg_adj_schedule(int nsteps, int nsnapshots, int nstages,
+                                int max_actions, int *actions, int *count) {
+  if (nsteps < 1 || nsnapshots < 1 || nsteps > kMaxAdjointSteps ||
+      !(nstages == 4 || nstages == 5 || nstages == 1) || !count ||
+      max_actions < 0 || (max_actions > 0 && !actions))
+    return fail(SWG_ERR_ARG, "swg_adj_schedule: bad argument");
+  const std::vector<AdjAction> acts =
+      Planner(nsteps, nsnapshots - 1, nstages).schedule();
+  *count = int(acts.size());
+  const int n = std::min<int>(max_actions, int(acts.size()));
+  for (int i = 0; i < n; ++i) {
+    actions[3 * i] = acts[i].type;
+    actions[3 * i + 1] = acts[i].a;
+    actions[3 * i + 2] = acts[i].b;
+  }
+  return SWG_OK;
 }

@@ -633,6 +633,13 @@ struct CheckpointedAdjoint {
     swg_check(swg_adj_info(m_handle, &p, &t));
     return p;
   }
+  // steps of the last sweep pair taped as taped advances (the last step of
+  // a re-advance, kept in the second tape for the next reversal)
+  long long taped_advances() const {
+    long long p = 0, t = 0, a = 0;
+    swg_check(swg_adj_info_ex(m_handle, &p, &t, &a));
+    return a;
+  }
 };
 
 // ------------------------------------------------------------ diagnostics --

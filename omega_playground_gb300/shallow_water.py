@@ -737,9 +737,24 @@ class Adjoint:
         return ge, gc
 
     def info(self):
+        """(plain re-advanced steps, taped steps) of the last sweep pair."""
         a, b = C.c_longlong(), C.c_longlong()
         check(lib().swg_adj_info(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def info_ex(self):
+        """(plain steps, taped steps, taped advances among them)."""
+        a, b, c = C.c_longlong(), C.c_longlong(), C.c_longlong()
+        check(lib().swg_adj_info_ex(self._h, C.byref(a), C.byref(b),
+                                    C.byref(c)))
+        return a.value, b.value, c.value
+
+    def memory(self):
+        """Device bytes: (one snapshot, one tape, everything held)."""
+        a, b, c = C.c_longlong(), C.c_longlong(), C.c_longlong()
+        check(lib().swg_adj_memory(self._h, C.byref(a), C.byref(b),
+                                   C.byref(c)))
+        return a.value, b.value, c.value
 
     def __del__(self):
         if getattr(self, "_h", None) and _capi._lib is not None:
@@ -774,8 +789,18 @@ def adjoint_batch_backward(adjs, lambdas, streams=None):
 
 
 def checkpoint_cost(nsteps: int, nsnapshots: int) -> int:
-    """Plain forward steps of the optimal binomial checkpointing schedule."""
+    """Plain forward steps of the classic optimal binomial checkpointing
+    schedule with one tape (Griewank-Walther)."""
     return int(lib().swg_checkpoint_cost(int(nsteps), int(nsnapshots)))
+
+
+def adjoint_plan(nsteps: int, nsnapshots: int, nstages: int = 4):
+    """(plain advances, taped advances) of the schedule the adjoint runs
+    for nsteps steps and nsnapshots snapshots (nstages 4: RK4; 5, 1: LSRK)."""
+    a, b = C.c_longlong(), C.c_longlong()
+    check(lib().swg_adj_plan(int(nsteps), int(nsnapshots), int(nstages),
+                             C.byref(a), C.byref(b)))
+    return a.value, b.value
 
 
 def _diag(fn, state, model, stream=None):

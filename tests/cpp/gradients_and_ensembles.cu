@@ -92,8 +92,9 @@ bool dot_product_test() {
   const double lhs = dot(download(DX), lamN);
   const double rhs = dot(dx0, download(LAM));
   const double rel = std::fabs(lhs - rhs) / std::fmax(std::fabs(lhs), std::fabs(rhs));
-  std::printf("dot_product lhs=%.17e rhs=%.17e rel=%.3e plain_steps=%lld\n",
-              lhs, rhs, rel, adj.plain_steps());
+  std::printf("dot_product lhs=%.17e rhs=%.17e rel=%.3e plain_steps=%lld "
+              "taped_advances=%lld\n",
+              lhs, rhs, rel, adj.plain_steps(), adj.taped_advances());
   return rel <= 1e-12;
 }
 

@@ -128,6 +128,106 @@ def test_checkpoint_cost_matches_binomial_formula():
     assert lib.swg_checkpoint_cost(10, 0) == -1
 
 
+def _plan_restated(N, S, ns):
+    """The adjoint planner's dynamic program, restated (costs in hundredths
+    of a plain step): f(n, s) reverses n steps from an available state, h(n,
+    s) also produces the final state; 0 = the taped pair, m > 0 = split."""
+    S = max(0, min(S, N - 1))
+    cA, cT, cP = 100, 104, (100 * (ns - 1) + 40) // ns
+    f = [[0] * (S + 1) for _ in range(N + 1)]
+    h = [[0] * (S + 1) for _ in range(N + 1)]
+    fm = [[0] * (S + 1) for _ in range(N + 1)]
+    hm = [[0] * (S + 1) for _ in range(N + 1)]
+    for n in range(1, N + 1):
+        for s in range(S + 1):
+            if n == 1:
+                f[n][s], h[n][s] = cP, cT
+                continue
+            rest = f[n - 2][s] + (n - 2) * cA + cT
+            bf, bh, mf, mh = rest + cP, rest + cT, 0, 0
+            if s > 0:
+                for m in range(1, n):
+                    base = m * cA + f[m][s]
+                    if base + f[n - m][s - 1] < bf:
+                        bf, mf = base + f[n - m][s - 1], m
+                    if base + h[n - m][s - 1] < bh:
+                        bh, mh = base + h[n - m][s - 1], m
+            f[n][s], fm[n][s], h[n][s], hm[n][s] = bf, mf, bh, mh
+    return f, h, fm, hm, S
+
+
+def _schedule(N, nsnap, ns):
+    lib = _capi.lib()
+    count = C.c_int(0)
+    assert lib.swg_adj_schedule(N, nsnap, ns, 0, None, C.byref(count)) == 0
+    buf = (C.c_int * (3 * count.value))()
+    assert lib.swg_adj_schedule(N, nsnap, ns, count.value, buf,
+                                C.byref(count)) == 0
+    return [tuple(buf[3 * i:3 * i + 3]) for i in range(count.value)]
+
+
+def _simulate(acts, N, nsnap):
+    """Runs a schedule on positions only: every step is reversed once, in
+    order N-1 ... 0, from a tape of that step; a tape is never overwritten
+    before its step is reversed; snapshots stay in range."""
+    cur, snaps, tapes, ended, rev = 0, {}, {}, False, []
+    plain = tadv = 0
+    for t, a, b in acts:
+        if t == 0:
+            assert cur == a and b > 0 and not (ended and a + b > N)
+            cur += b
+            plain += b
+        elif t == 1:
+            assert 0 <= a < nsnap
+            snaps[a] = cur
+        elif t == 2:
+            cur = snaps[a]
+        elif t == 3:
+            assert ended and cur == a and tapes.get(b) is None
+            rev.append(a)
+        elif t == 4:
+            assert cur == a and tapes.get(b) is None
+            tapes[b] = a
+            cur += 1
+            tadv += 1
+        elif t == 5:
+            assert ended and tapes.get(b) == a
+            tapes[b] = None
+            rev.append(a)
+        else:
+            assert t == 6 and not ended and cur == N and not rev
+            ended = True
+    assert rev == list(range(N - 1, -1, -1))
+    return plain, tadv
+
+
+def test_adjoint_schedule_is_valid_and_optimal():
+    """The adjoint's checkpoint schedule (host-only planner, no GPU): it
+    reverses every step exactly once from that step's own tape with the
+    given snapshots, and its counts are the restated dynamic program's."""
+    import omega_playground_gb300 as og
+    for N in list(range(1, 26)) + [40, 77]:
+        for nsnap in (1, 2, 3, 5, 9):
+            for ns in (4, 5, 1):
+                acts = _schedule(N, nsnap, ns)
+                plain, tadv = _simulate(acts, N, nsnap)
+                assert og.adjoint_plan(N, nsnap, ns) == (plain, tadv)
+                f, h, fm, hm, S = _plan_restated(N, nsnap - 1, ns)
+                cP = (100 * (ns - 1) + 40) // ns
+                ntape = N - tadv
+                assert 100 * plain + 104 * tadv + cP * ntape == h[N][S], \
+                    (N, nsnap, ns)
+    # the benchmarked adjoint: 1000 RK4 steps, 32 snapshots
+    plain, tadv = og.adjoint_plan(1000, 32, 4)
+    assert (plain, tadv) == (1932, 440)
+    assert plain + tadv < og.checkpoint_cost(1000, 32) == 2405
+    assert _simulate(_schedule(1000, 32, 4), 1000, 32) == (plain, tadv)
+    lib = _capi.lib()
+    n = C.c_int(0)
+    assert lib.swg_adj_schedule(10001, 32, 4, 0, None, C.byref(n)) == 1
+    assert lib.swg_adj_schedule(10, 32, 3, 0, None, C.byref(n)) == 1
+
+
 def test_host_stepper_edge_layout():
     """Chunk layouts with small end chunks (host-state stepper autotuning)."""
     import omega_playground_gb300 as og

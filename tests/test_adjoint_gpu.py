@@ -111,9 +111,9 @@ def test_trajectory_dot_product_through_checkpointing(nsteps, nsnap, over):
     LAM = make_state(mesh, params, lamN)
     adj.backward(LAM)
     lam0 = LAM.download()
-    plain, taped = adj.info()
+    plain, taped, tadv = adj.info_ex()
     assert taped == nsteps
-    assert plain == og.checkpoint_cost(nsteps, nsnap)
+    assert (plain, tadv) == og.adjoint_plan(nsteps, nsnap, 4)
     DX = make_state(mesh, params, dx0)
     adj.tlm_apply(X0, DX, 0.0, wl.dt, nsteps)
     dxN = DX.download()
@@ -225,7 +225,9 @@ def test_dot_product_full_adjoint_workload():
     adj.forward(X0, 0.0, wl.dt, wl.nsteps, XN)
     LAM = make_state(mesh, params, lamN)
     adj.backward(LAM)
-    assert adj.info() == (og.checkpoint_cost(wl.nsteps, 32), wl.nsteps)
+    plain, tadv = og.adjoint_plan(wl.nsteps, 32, 4)
+    assert adj.info_ex() == (plain, wl.nsteps, tadv)
+    assert plain + tadv < og.checkpoint_cost(wl.nsteps, 32)
     DX = make_state(mesh, params, dx0)
     adj.tlm_apply(X0, DX, 0.0, wl.dt, wl.nsteps)
     lhs, rhs = dot(DX.download(), lamN), dot(dx0, LAM.download())
@@ -249,10 +251,10 @@ def test_checkpoint_budget_and_step_limit_are_errors():
     with pytest.raises(og.SwgError) as e:
         og.Adjoint(model, 32).forward(X0, 0.0, wl.dt, 10001, XN)
     assert e.value.code == 1
-    adj.forward(X0, 0.0, wl.dt, 20, XN)   # 190 plain steps: within budget
+    adj.forward(X0, 0.0, wl.dt, 20, XN)   # 90 plain steps: within budget
     LAM = make_state(mesh, params, rand_like([a.shape for a in x0], 5))
     adj.backward(LAM)
-    assert adj.info() == (og.checkpoint_cost(20, 1), 20)
+    assert adj.info_ex() == (90, 20, 11) and og.adjoint_plan(20, 1) == (90, 11)
 
 
 @pytest.mark.parametrize("nstages,nsteps,nsnap,over", [
@@ -278,8 +280,9 @@ def test_lsrk_trajectory_dot_product_through_checkpointing(nstages, nsteps,
     LAM = make_state(mesh, params, lamN)
     adj.backward(LAM)
     lam0 = LAM.download()
-    plain, taped = adj.info()
-    assert taped == nsteps and plain == og.checkpoint_cost(nsteps, nsnap)
+    plain, taped, tadv = adj.info_ex()
+    assert taped == nsteps
+    assert (plain, tadv) == og.adjoint_plan(nsteps, nsnap, nstages)
     DX = make_state(mesh, params, dx0)
     adj.tlm_apply(X0, DX, 0.0, wl.dt, nsteps)
     lhs, rhs = dot(DX.download(), lamN), dot(dx0, lam0)
