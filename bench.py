@@ -160,6 +160,39 @@ class ClockSampler:
 
 # ------------------------------------------------------- CPU baseline -----
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True,
+                             timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+def workload_config(wl, world, sample_nlayers):
+    """The `config` object both arms print (the same keys, so the two lines
+    can be compared key for key)."""
+    return {"workload": wl.name, "nx": wl.nx, "ny": wl.ny,
+            "nlayers": wl.nlayers, "ntracers": wl.ntracers,
+            "stepper": ("rk4" if wl.stepper == "rk4"
+                        else f"lsrk{wl.nstages}"), "dt": wl.dt,
+            "parallelism": f"replicas x{world}",
+            "l2": l2_note(8 * wl.ncells * wl.nlayers * (4 + wl.ntracers)),
+            "sample_nlayers": sample_nlayers}
+
+
 def oracle_sample(wl, nlayers_sample, steps, warmup):
     """Time the oracle (C restatement of the reference, OpenMP) on the
     workload's mesh and tracers with `nlayers_sample` levels."""
@@ -199,7 +232,7 @@ def cpu_baseline(wl, target_s=15.0):
     nsteps = max(1, min(20, int(target_s / max(times[0], 1e-6))))
     units, times, cores, w = oracle_sample(wl, nl, nsteps, 0)
     return {"value": units * len(times) / sum(times), "unit": UNIT,
-            "cores": cores, "kind": "port",
+            "cores": cores, "kind": "port", "cpu_model": cpu_model(),
             "sample": (f"{len(times)} {w.stepper}{w.nstages} step(s) of the "
                        f"{w.nx}x{w.ny} mesh, {w.ntracers} tracers, "
                        f"{w.nlayers} of {wl.nlayers} levels; oracle C "
@@ -223,13 +256,9 @@ def run_reference(args, wl):
         "ms_per_step": 1e3 * total / len(times), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded)",
-        "config": {"workload": wl.name, "nx": wl.nx, "ny": wl.ny,
-                   "nlayers": wl.nlayers, "ntracers": wl.ntracers,
-                   "stepper": ("rk4" if wl.stepper == "rk4"
-                               else f"lsrk{wl.nstages}"),
-                   "sample_nlayers": w.nlayers},
+        "config": workload_config(wl, args.gpus, w.nlayers),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores,
-                         "kind": "port",
+                         "kind": "port", "cpu_model": cpu_model(),
                          "sample": (f"each step: one {w.stepper}{w.nstages} "
                                     f"step of the {w.nx}x{w.ny} mesh, "
                                     f"{w.ntracers} tracers, {w.nlayers} of "
@@ -396,19 +425,32 @@ def run_ours(args, wl):
                 "stage": {"achieved": stage_bytes / (stage_ms / 1e3) / 1e9,
                           "alg_bytes": stage_bytes, "ms": stage_ms,
                           "frac": stage_bytes / (stage_ms / 1e3) / 1e9 / peak}}
-    # FP64 issue roof: GB300 issues 2 FP64 thread-instructions per SM per
-    # clock (ncu sm__sass_thread_inst_executed_op_dfma_pred_on.peak_sustained);
-    # instructions per cell-level of k_cell_final measured by ncu on the
+    # FP64 issue roof, measured here: DFMA / DADD / DMUL issue rates of this
+    # GPU (swg_fp64_issue_rate: every SM filled, 8 independent chains per
+    # thread, CUDA events) with the SM clock sampled while they run.  The
+    # instructions per cell-level of k_cell_final come from ncu on the
     # 256x256x64x8 case (DFMA 132 + DMUL 15 + DADD 8 = 155 with 8 tracers).
     fp64 = None
     if dom == "k_cell_final" and wl.ntracers == 8:
         sms = torch.cuda.get_device_properties(local).multi_processor_count
-        mhz = clk.get("sm_mhz") or 2070.0
-        peak_inst = 2.0 * sms * mhz * 1e6
+        pk_clocks = ClockSampler(uuid)
+        time.sleep(0.3)
+        rates = {op: og.fp64_issue_rate(op, 20000, stream=sh)
+                 for op in ("dfma", "dadd", "dmul")}
+        pk_clk = pk_clocks.stop()
+        pk_mhz = pk_clk.get("sm_mhz") or 0.0
+        peak_inst = rates["dfma"][0]
         got_inst = 155.0 * CK / (dom_ms / 1e3)
         fp64 = {"bound": "fp64", "kernel": dom, "achieved": got_inst / 1e9,
                 "peak": peak_inst / 1e9, "unit": "G FP64 inst/s",
-                "frac": got_inst / peak_inst, "inst_per_cell_level": 155}
+                "frac": got_inst / peak_inst, "inst_per_cell_level": 155,
+                "peak_source": "measured: swg_fp64_issue_rate (DFMA), this run",
+                "issue_rates": {
+                    op: {"G_inst_per_s": r / 1e9, "ms": round(ms, 3),
+                         "per_sm_per_clock": (r / (sms * pk_mhz * 1e6)
+                                              if pk_mhz else None)}
+                    for op, (r, ms) in rates.items()},
+                "peak_clocks": pk_clk}
     kernels = {k: {"ms_per_launch": v[0] / v[1], "launches_per_step": v[1],
                    "share": v[0] / sum(x[0] for x in prof.values())}
                for k, v in prof.items()}
@@ -491,13 +533,7 @@ def run_ours(args, wl):
             "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)",
-            "config": {"workload": wl.name, "nx": wl.nx, "ny": wl.ny,
-                       "nlayers": wl.nlayers, "ntracers": wl.ntracers,
-                       "stepper": ("rk4" if wl.stepper == "rk4"
-                                   else f"lsrk{wl.nstages}"), "dt": wl.dt,
-                       "parallelism": f"replicas x{world}",
-                       "l2": l2_note(8 * wl.ncells * wl.nlayers
-                                     * (4 + wl.ntracers))},
+            "config": workload_config(wl, world, wl.nlayers),
             "roofline": roofline, "fp64_roofline": fp64, "kernels": kernels,
             "cpu_baseline": cpu, "e2e": e2e, "adjoint": adjoint,
             "ensemble": ens, "adjoint_ensemble": adj_ens,

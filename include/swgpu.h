@@ -219,6 +219,33 @@ int swg_model_set_forcing(swg_model model, swg_forcing_fn fn, void *user);
 int swg_compute_tendency(swg_model model, swg_state tend, swg_state state,
                          double t, int add_mode, void *stream);
 
+/* The model's auxiliary state and per-field tendencies, as the reference
+ * splits compute_tendency (shallow_water_model.cpp:313-347).
+ * swg_model_compute_aux replaces m_aux_state.compute(h, vn, tr, f_vertex,
+ * mesh) (shallow_water_auxstate.cpp:12-50): device arrays of the model's
+ * layout.  Every tendency evaluation and step also leaves its last
+ * auxiliary state in the model.  The per-field calls replace
+ * compute_h_tendency / compute_vn_tendency / compute_tr_tendency
+ * (shallow_water_model.hpp:36-41, shallow_water_model.cpp:43-311): each reads
+ * the intermediates of the last auxiliary computation (mean thickness,
+ * vorticities, kinetic energy, divergence, normalised tracers) and the
+ * normal velocity vn it is given (and the velocity tendency also its h, for
+ * the SSH gradient), honours the term switches and add_mode (REPLACE zeroes
+ * the field first), and runs no additional_tendency hook.  As in the
+ * reference, the tracer call is not given h and does not read tr: the
+ * normalised tracers come from the auxiliary state.  The velocity tendency
+ * needs a model created with the velocity tendency enabled (SWG_ERR_STATE
+ * otherwise).  The linear model (swg_linear_model_create) keeps no
+ * auxiliary state: its h and vn calls read h and vn directly. */
+int swg_model_compute_aux(swg_model model, const double *h, const double *vn,
+                          const double *tr, void *stream);
+int swg_compute_h_tendency(swg_model model, double *h_tend, const double *h,
+                           const double *vn, int add_mode, void *stream);
+int swg_compute_vn_tendency(swg_model model, double *vn_tend, const double *h,
+                            const double *vn, int add_mode, void *stream);
+int swg_compute_tr_tendency(swg_model model, double *tr_tend, const double *tr,
+                            const double *vn, int add_mode, void *stream);
+
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory while they run (a host framework that owns the whole device pool,
  * or code that must avoid the synchronisation an allocation brings): the
@@ -445,6 +472,16 @@ int swg_adj_plan(int nsteps, int nsnapshots, int nstages,
  * (x_N in `cur`). */
 int swg_adj_schedule(int nsteps, int nsnapshots, int nstages,
                      int max_actions, int *actions, int *count);
+
+/* ----------------------------------------------------- measurement -----
+ * FP64 issue rate of the current GPU (no counterpart in the reference): op
+ * 0 DFMA, 1 DADD, 2 DMUL; every SM filled with resident threads, each
+ * running 8 independent chains for `iters` iterations, timed with CUDA
+ * events on `stream` (blocking).  *inst_per_s gets thread-instructions per
+ * second, *ms (may be NULL) the timed kernel's duration.  The solver's
+ * kernels are bound by this rate, not by HBM bandwidth. */
+int swg_fp64_issue_rate(int op, int iters, double *inst_per_s, double *ms,
+                        void *stream);
 
 /* ------------------------------------------------------- diagnostics -----
  * replaces energy_integral / mass_integral / circulation_integral

@@ -15,6 +15,7 @@ from .shallow_water import (AddMode, Adjoint, Batch, LSRKStepper,  # noqa: F401
                             ShallowWaterModel, ShallowWaterParams,
                             ShallowWaterState, TimeStepper,
                             circulation_integral, energy_integral,
+                            fp64_issue_rate,
                             kernel_launches, mass_integral,
                             LinearShallowWaterModel, LinearShallowWaterParams,
                             profile_enable, profile_read, sync)
@@ -27,6 +28,6 @@ __all__ = ["AddMode", "Adjoint", "Batch", "adjoint_plan", "checkpoint_cost", "Ho
            "adjoint_batch_forward", "adjoint_batch_backward", "LSRKStepper", "MPASMesh", "PlanarHexagonalMesh",
            "RK4Stepper", "ShallowWaterModel", "ShallowWaterParams",
            "ShallowWaterState", "TimeStepper", "circulation_integral",
-           "energy_integral", "mass_integral", "sync", "kernel_launches",
+           "energy_integral", "fp64_issue_rate", "mass_integral", "sync", "kernel_launches",
            "profile_enable", "profile_read",
            "SwgError", "exported_symbols", "workloads"]

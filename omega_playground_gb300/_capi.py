@@ -114,6 +114,10 @@ _SIGS = {
     "swg_model_set_forcing": (C.c_int, [_vp, FORCING_FN, _vp]),
     "swg_compute_tendency": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_int,
                                        _vp]),
+    "swg_model_compute_aux": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "swg_compute_h_tendency": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, _vp]),
+    "swg_compute_vn_tendency": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, _vp]),
+    "swg_compute_tr_tendency": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, _vp]),
     "swg_compute_tendency_noalloc": (C.c_int, [_vp, C.POINTER(Params), _vp,
                                                _vp, _vp, _vp, _vp, _vp,
                                                C.c_int, _vp]),
@@ -166,6 +170,7 @@ _SIGS = {
                                  C.POINTER(C.c_longlong),
                                  C.POINTER(C.c_longlong)]),
     "swg_checkpoint_cost": (C.c_longlong, [C.c_int, C.c_int]),
+    "swg_fp64_issue_rate": (C.c_int, [C.c_int, C.c_int, _dp, _dp, _vp]),
     "swg_adj_plan": (C.c_int, [C.c_int, C.c_int, C.c_int,
                                C.POINTER(C.c_longlong),
                                C.POINTER(C.c_longlong)]),

@@ -506,7 +506,6 @@ extern "C" int swg_model_create_ex(swg_mesh mesh, const swg_params *p,
   const bool vn = pv.do_vn;
   const bool vdiss = vn && (pv.vel_del2 || pv.vel_del4);
   const bool v4 = vn && pv.vel_del4;
-  const bool trd = T > 0 && (pv.tr_del2 || pv.tr_del4);
   struct Need {
     bool on;
     size_t n;
@@ -519,7 +518,9 @@ extern "C" int swg_model_create_ex(swg_mesh mesh, const swg_params *p,
       {T > 0, T * C * K, &a.ntr},
       {T > 0 && pv.tr_del4, T * C * K, &a.lap},
       {true, E * K, &a.F},      {vn, E * K, &a.G},
-      {vn, E * K, &a.Q},        {trd, E * K, &a.mh},
+      // the mean thickness is kept always: the per-field tendency calls
+      // read the last auxiliary state's (the reference's m_mean_h_edge)
+      {vn, E * K, &a.Q},        {true, E * K, &a.mh},
       {vdiss, E * K, &a.d2u},
       {v4 && mesh->view.dv4_differs, E * K, &a.d2u4},
   };
@@ -715,6 +716,77 @@ extern "C" int swg_compute_tendency(swg_model md, swg_state tend,
   const StageArgs s = tendency_args(
       tend, state, add_mode == SWG_ADD_REPLACE ? EPI_REPLACE : EPI_INCREMENT);
   return run_tendency(md, s, tend, state->h, state->vn, t, as_stream(stream));
+}
+
+// ------------------------------------------- auxiliary state, per field ---
+// The reference's model computes its auxiliary state (ShallowWaterAuxiliary-
+// State::compute, shallow_water_auxstate.cpp:12-50) and then each field's
+// tendency from it (compute_h_tendency / compute_vn_tendency /
+// compute_tr_tendency, shallow_water_model.cpp:43-311).  These entry points
+// expose the same split: the per-field calls read the intermediates of the
+// last auxiliary computation (by swg_model_compute_aux or by any tendency
+// evaluation or step on the model) together with their own h / vn
+// arguments, as the reference's do.
+
+extern "C" int swg_model_compute_aux(swg_model md, const double *h,
+                                     const double *vn, const double *tr,
+                                     void *stream) {
+  if (!md || !h || !vn || (md->params.ntracers > 0 && !tr))
+    return fail(SWG_ERR_ARG, "swg_model_compute_aux: bad argument");
+  if (md->view.linear)
+    return fail(SWG_ERR_ARG, "swg_model_compute_aux: the linear model keeps "
+                             "no auxiliary state");
+  NvtxRange range("auxstate");
+  launch_aux(md->mesh->view, md->view, md->aux, h, vn, tr, as_stream(stream),
+             &md->fork);
+  return check_launch("auxiliary state kernels");
+}
+
+static int field_tendency(swg_model md, int field, double *tend,
+                          const double *h, const double *vn, int add_mode,
+                          void *stream, const char *who) {
+  // h is read by the velocity tendency only (the SSH gradient)
+  if (!md || !tend || !vn || (field == 1 && !h))
+    return fail(SWG_ERR_ARG, std::string(who) + ": bad argument");
+  if (add_mode != SWG_ADD_REPLACE && add_mode != SWG_ADD_INCREMENT)
+    return fail(SWG_ERR_ARG, std::string(who) + ": bad add_mode");
+  if (field == 2 && md->view.linear)
+    return fail(SWG_ERR_ARG, std::string(who) + ": the linear model has no "
+                                                "tracers");
+  if (field == 1 && !md->view.do_vn && !md->view.linear)
+    return fail(SWG_ERR_STATE, std::string(who) +
+                                   ": the model was created with the "
+                                   "velocity tendency disabled, so it keeps "
+                                   "no velocity intermediates");
+  if (field == 2 && md->params.ntracers == 0)
+    return SWG_OK; // no tracers: nothing to compute
+  launch_field_tendency(md->mesh->view, md->view, md->aux, field, h, vn, tend,
+                        add_mode == SWG_ADD_REPLACE ? EPI_REPLACE
+                                                    : EPI_INCREMENT,
+                        as_stream(stream));
+  return check_launch(who);
+}
+
+extern "C" int swg_compute_h_tendency(swg_model md, double *h_tend,
+                                      const double *h, const double *vn,
+                                      int add_mode, void *stream) {
+  return field_tendency(md, 0, h_tend, h, vn, add_mode, stream,
+                        "swg_compute_h_tendency");
+}
+
+extern "C" int swg_compute_vn_tendency(swg_model md, double *vn_tend,
+                                       const double *h, const double *vn,
+                                       int add_mode, void *stream) {
+  return field_tendency(md, 1, vn_tend, h, vn, add_mode, stream,
+                        "swg_compute_vn_tendency");
+}
+
+extern "C" int swg_compute_tr_tendency(swg_model md, double *tr_tend,
+                                       const double *tr, const double *vn,
+                                       int add_mode, void *stream) {
+  (void)tr; // the reference reads the normalised tracers of the aux state
+  return field_tendency(md, 2, tr_tend, nullptr, vn, add_mode, stream,
+                        "swg_compute_tr_tendency");
 }
 
 // -------------------------------------------------------------- steppers ---

@@ -35,6 +35,11 @@ __device__ __forceinline__ Dual fma(Dual a, Dual b, Dual c) {
 
 // 1/x: hardware estimate refined by two Newton-Raphson steps
 // r <- r + r (1 - x r); each step squares the relative error of the estimate.
+// The estimate is the .ftz form: a subnormal input (|x| < 2^-1022) counts as
+// zero (result infinite) and a result below 2^-1022 flushes to zero, so the
+// function is for |x| in [2^-1022, 2^1022], far beyond any thickness.  On
+// the GPU it is within 1 ulp of the correctly rounded 1.0 / x over 1e-6 ..
+// 1e6 and random mantissas in [2^-40, 2^40] (tests/cpp/rcp_accuracy.cu).
 __device__ __forceinline__ double rcp_nr(double x) {
   double r;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
@@ -155,7 +160,7 @@ pt_edge1(const MeshView &m, const ModelView &p, const AuxViewT<T> &a,
   const T u = vn[i];
   const T F = mh * u;
   a.F[i] = F;
-  if (a.mh) // allocated for tracer diffusion, and in the adjoint's tape
+  if (a.mh) // kept by every nonlinear model and in the adjoint's tape
     a.mh[i] = mh;
   if (p.do_vn) {
     const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
@@ -284,8 +289,10 @@ __device__ __forceinline__ void pt_edge_final(const MeshView &m,
             s.h[size_t(c1) * K + k] - s.h[size_t(c0) * K + k], t);
   if (p.drag && k == p.drag_level) {
     // bottom drag -c_d sqrt(ke_0 + ke_1) vn / mean_h on the lowest level
-    // (the term commented out at shallow_water_hierarchical.cpp:479-486)
-    const T hm = 0.5 * (s.h[size_t(c0) * K + k] + s.h[size_t(c1) * K + k]);
+    // (the term commented out at shallow_water_hierarchical.cpp:479-486),
+    // with the auxiliary state's mean thickness (h_drag_edge = h_mean)
+    const T hm = a.mh ? a.mh[i]
+                      : 0.5 * (s.h[size_t(c0) * K + k] + s.h[size_t(c1) * K + k]);
     const T ks = a.ke[size_t(c0) * K + k] + a.ke[size_t(c1) * K + k];
     t = t + (-p.drag_coeff * sqrt(ks)) * s.vn[i] * rcp_nr(hm);
   }

@@ -188,6 +188,14 @@ void launch_tendency_dual(const MeshView &m, const ModelView &p,
 void launch_aux(const MeshView &m, const ModelView &p, const AuxView &a,
                 const double *h, const double *vn, const double *tr,
                 cudaStream_t st, const Fork *fk = nullptr);
+// one field of a tendency from the last auxiliary state in `a` and the
+// caller's h / vn (the reference's compute_h_tendency, compute_vn_tendency,
+// compute_tr_tendency): field 0 h, 1 vn, 2 tracers; mode EPI_REPLACE or
+// EPI_INCREMENT.  Rewrites the thickness flux F (and G) of `a`.
+void launch_field_tendency(const MeshView &m, const ModelView &p,
+                           const AuxView &a, int field, const double *h,
+                           const double *vn, double *tend, int mode,
+                           cudaStream_t st);
 void launch_axpby(double *y, const double *x, const double *z, double alpha,
                   double beta, long long n, int kind, cudaStream_t st);
 // opt-in per-kernel CUDA-event timing (swg_profile_enable)

@@ -109,6 +109,23 @@ __global__ void __launch_bounds__(TPB)
     pt_lin_cell<T>(m, p, s, i);
 }
 
+// Thickness flux of a per-field tendency call (compute_h/vn/tr_tendency):
+// F = mean_h vn from the last auxiliary state's mean thickness and the
+// caller's normal velocity (pv_flux_edge.hpp and thickness_hadv_cell.hpp
+// multiply the two per edge), and with G also F Q for the PV flux; the
+// same expressions as pt_edge1, so equal inputs give equal fluxes.
+template <bool G>
+__global__ void __launch_bounds__(TPB)
+    k_field_flux(MeshView m, AuxView a, const double *__restrict__ vn) {
+  const unsigned i = blockIdx.x * TPB + threadIdx.x;
+  if (i >= unsigned(m.nedges) * unsigned(m.nlayers))
+    return;
+  const double F = a.mh[i] * vn[i];
+  a.F[i] = F;
+  if (G)
+    a.G[i] = F * a.Q[i];
+}
+
 // Elementwise helpers for the unfused stepper path (forcing hook set).
 __global__ void k_axpby(double *__restrict__ y, const double *__restrict__ x,
                         const double *__restrict__ z, double alpha,
@@ -381,6 +398,62 @@ void launch_aux(const MeshView &m, const ModelView &p, const AuxView &a,
                 const double *h, const double *vn, const double *tr,
                 cudaStream_t st, const Fork *fk) {
   launch_aux_t<double>(m, p, a, h, vn, tr, st, fk);
+}
+
+void launch_field_tendency(const MeshView &m, const ModelView &p,
+                           const AuxView &a, int field, const double *h,
+                           const double *vn, double *tend, int mode,
+                           cudaStream_t st) {
+  const long long K = m.nlayers, CK = m.ncells * K, EK = m.nedges * K;
+  StageArgs s{};
+  s.h = h;
+  s.vn = vn;
+  s.ep.mode = mode;
+  ModelView q = p;
+  if (p.linear) { // the linear terms read h and vn themselves
+    if (field == 0) {
+      s.fh.tend = tend;
+      Scope sc("k_lin_cell", st);
+      k_lin_cell<double><<<nblocks(CK), TPB, 0, st>>>(m, q, s);
+    } else {
+      s.fvn.tend = tend;
+      Scope sc("k_lin_edge", st);
+      if (m.ne == 8)
+        k_lin_edge<8, double><<<nblocks(EK), TPB, 0, st>>>(m, q, s);
+      else
+        k_lin_edge<10, double><<<nblocks(EK), TPB, 0, st>>>(m, q, s);
+    }
+    return;
+  }
+  {
+    Scope sc("k_field_flux", st);
+    if (field == 1)
+      k_field_flux<true><<<nblocks(EK), TPB, 0, st>>>(m, a, vn);
+    else
+      k_field_flux<false><<<nblocks(EK), TPB, 0, st>>>(m, a, vn);
+  }
+  if (field == 1) {
+    s.fvn.tend = tend;
+    NvtxRange r("vn_tendency");
+    Scope sc("k_edge_final", st);
+    if (m.ne == 8)
+      k_edge_final<8, double><<<nblocks(EK), TPB, 0, st>>>(m, q, a, s);
+    else
+      k_edge_final<10, double><<<nblocks(EK), TPB, 0, st>>>(m, q, a, s);
+    return;
+  }
+  // the cell pass writes h when do_h is set and the tracers when ntracers
+  // > 0: one of the two per call
+  q.do_h = field == 0;
+  if (field == 0) {
+    q.ntracers = 0;
+    s.fh.tend = tend;
+  } else {
+    s.ftr.tend = tend;
+  }
+  NvtxRange r(field == 0 ? "h_tendency" : "tr_tendency");
+  Scope sc("k_cell_final", st);
+  k_cell_final<double><<<nblocks(CK), TPB, 0, st>>>(m, q, a, s);
 }
 
 int fork_create(Fork &f) {

@@ -35,6 +35,7 @@
 #include <stdexcept>
 #include <string>
 #include <type_traits>
+#include <typeinfo>
 #include <vector>
 
 namespace omega {
@@ -360,6 +361,37 @@ struct TendencyTerm {
       : m_enabled(model, term) {}
 };
 
+// Read-only view of the model's auxiliary state (the reference's
+// ShallowWaterAuxiliaryState, shallow_water_auxstate.hpp, with its member
+// groups): device views of the intermediates of the last auxiliary
+// computation, which compute() or any tendency evaluation or step leaves.
+// The GPU path keeps the mean thickness once (m_mean_h_edge and
+// m_flux_h_edge, equal in the reference, view the same array) and the two
+// vorticity terms summed: m_pv_vertex = norm_rvort_vertex +
+// norm_pvort_vertex, m_pv_edge = 2 (norm_rvort_edge + norm_pvort_edge).
+// A view the model's configuration does not compute is empty (null data).
+struct ShallowWaterAuxiliaryState {
+  swg_model m_model = nullptr;
+  struct {
+    RealConst2d m_mean_h_edge, m_flux_h_edge;
+  } m_thickness_aux;
+  struct {
+    RealConst2d m_rvort_vertex, m_pv_vertex, m_pv_edge;
+  } m_vorticity_aux;
+  struct {
+    RealConst2d m_ke_cell, m_vel_div_cell;
+  } m_kinetic_aux;
+  struct {
+    RealConst3d m_norm_tr_cell;
+  } m_tracer_aux;
+  // shallow_water_auxstate.cpp:12-50; f_vertex is the model's m_f_vertex
+  void compute(RealConst2d h_cell, RealConst2d vn_edge, RealConst3d tr_cell,
+               RealConst1d /*f_vertex*/, const void * /*mesh*/ = nullptr) const {
+    swg_check(swg_model_compute_aux(m_model, h_cell.data(), vn_edge.data(),
+                                    tr_cell.data(), nullptr));
+  }
+};
+
 struct ShallowWaterModel {
   ShallowWaterParams m_params;
   MPASMesh *m_mesh;
@@ -377,6 +409,8 @@ struct ShallowWaterModel {
   // Coriolis parameter per vertex (shallow_water_model.hpp:32), f0 after
   // construction; a user kernel may write it, later evaluations read it
   Real1d m_f_vertex;
+  // the auxiliary state of the last evaluation (shallow_water_model.hpp:18)
+  ShallowWaterAuxiliaryState m_aux_state;
 
   // `options`: the linear variant or the opt-in bottom drag
   // (swg_model_options in swgpu.h); the default is the reference's model,
@@ -395,9 +429,12 @@ struct ShallowWaterModel {
     swg_check(swg_model_aux(m_handle, "f_vertex", &fv, &nfv));
     m_f_vertex.m_data = const_cast<double *>(fv);
     m_f_vertex.m_ext[0] = size_t(nfv);
-    // The hook stays registered until the base no-op runs once; then the
-    // steppers switch to the fused kernels (models that override
-    // additional_tendency keep the unfused, hooked sequence).
+    bind_aux_state();
+    // The hook is registered here, where the dynamic type is not known yet.
+    // settle_hook() drops it without any GPU work for the library's own
+    // model classes (steppers, compute_tendency and resolve_hook call it);
+    // for a user's derived class it stays until the base no-op runs once
+    // (an override keeps the unfused, hooked sequence).
     swg_check(swg_model_set_forcing(m_handle, &ShallowWaterModel::trampoline,
                                     this));
   }
@@ -418,17 +455,49 @@ struct ShallowWaterModel {
   void compute_tendency(const ShallowWaterState &tend,
                         const ShallowWaterState &state, Real t,
                         AddMode add_mode = AddMode::replace) const {
+    settle_hook();
     swg_check(swg_compute_tendency(
         m_handle, tend.handle(), state.handle(), t,
         add_mode == AddMode::replace ? SWG_ADD_REPLACE : SWG_ADD_INCREMENT,
         nullptr));
   }
 
+  // shallow_water_model.hpp:36-41: one field's tendency from the auxiliary
+  // state of the last evaluation (m_aux_state) and the given views; the
+  // tracer tendency reads the normalised tracers of the auxiliary state
+  // (tr_cell is not read, and no h is given, as in the reference)
+  void compute_h_tendency(Real2d h_tend_cell, RealConst2d h_cell,
+                          RealConst2d vn_edge, AddMode add_mode) const {
+    swg_check(swg_compute_h_tendency(m_handle, h_tend_cell.data(),
+                                     h_cell.data(), vn_edge.data(),
+                                     mode(add_mode), nullptr));
+  }
+  void compute_vn_tendency(Real2d vn_tend_edge, RealConst2d h_cell,
+                           RealConst2d vn_edge, AddMode add_mode) const {
+    swg_check(swg_compute_vn_tendency(m_handle, vn_tend_edge.data(),
+                                      h_cell.data(), vn_edge.data(),
+                                      mode(add_mode), nullptr));
+  }
+  void compute_tr_tendency(Real3d tr_tend_cell, RealConst3d tr_cell,
+                           RealConst2d vn_edge, AddMode add_mode) const {
+    swg_check(swg_compute_tr_tendency(m_handle, tr_tend_cell.data(),
+                                      tr_cell.data(), vn_edge.data(),
+                                      mode(add_mode), nullptr));
+  }
+
+  // Drops the hook registered at construction when additional_tendency
+  // cannot be overridden: the object is exactly a ShallowWaterModel or a
+  // LinearShallowWaterModel (a user's derived class may override it and
+  // keeps the hook).  Costs no GPU work; the steppers, the tendency call and
+  // resolve_hook() run it first.
+  void settle_hook() const;
+
   // Settles whether additional_tendency is overridden: one tendency
   // evaluation on a scratch state (h = vn = 1) runs the hook once; the base
   // no-op then unregisters itself.  The ensemble and adjoint classes call it
   // because the library refuses models that still carry a hook.
   void resolve_hook() const {
+    settle_hook();
     if (m_default_hook)
       return;
     ShallowWaterState tend(m_mesh, m_params), state(m_mesh, m_params);
@@ -439,6 +508,42 @@ struct ShallowWaterModel {
 
 private:
   mutable bool m_default_hook = false;
+
+  static int mode(AddMode m) {
+    return m == AddMode::replace ? SWG_ADD_REPLACE : SWG_ADD_INCREMENT;
+  }
+  // m_aux_state's views of the model's intermediate arrays
+  void bind_aux_state() {
+    ShallowWaterAuxiliaryState &a = m_aux_state;
+    a.m_model = m_handle;
+    const MPASMesh *me = m_mesh;
+    auto bind2 = [&](const char *name, RealConst2d &v, Int rows) {
+      const double *p = nullptr;
+      long long n = 0;
+      if (swg_model_aux(m_handle, name, &p, &n) != SWG_OK)
+        return; // not computed by this configuration: an empty view
+      v.m_data = p;
+      v.m_ext[0] = rows;
+      v.m_ext[1] = me->m_nlayers;
+    };
+    bind2("mean_h_edge", a.m_thickness_aux.m_mean_h_edge, me->m_nedges);
+    a.m_thickness_aux.m_flux_h_edge = a.m_thickness_aux.m_mean_h_edge;
+    bind2("rvort_vertex", a.m_vorticity_aux.m_rvort_vertex, me->m_nvertices);
+    bind2("q_vertex", a.m_vorticity_aux.m_pv_vertex, me->m_nvertices);
+    bind2("pv_edge", a.m_vorticity_aux.m_pv_edge, me->m_nedges);
+    bind2("ke_cell", a.m_kinetic_aux.m_ke_cell, me->m_ncells);
+    bind2("vel_div_cell", a.m_kinetic_aux.m_vel_div_cell, me->m_ncells);
+    const double *p = nullptr;
+    long long n = 0;
+    if (m_params.m_ntracers > 0 &&
+        swg_model_aux(m_handle, "norm_tr_cell", &p, &n) == SWG_OK) {
+      RealConst3d &t = a.m_tracer_aux.m_norm_tr_cell;
+      t.m_data = p;
+      t.m_ext[0] = m_params.m_ntracers;
+      t.m_ext[1] = me->m_ncells;
+      t.m_ext[2] = me->m_nlayers;
+    }
+  }
 
   static void trampoline(void *user, double *h_tend, double *vn_tend,
                          const double *h, const double *vn, double t,
@@ -484,6 +589,14 @@ struct LinearShallowWaterModel : ShallowWaterModel {
   Real m_h0;
 };
 
+inline void ShallowWaterModel::settle_hook() const {
+  if (m_default_hook || (typeid(*this) != typeid(ShallowWaterModel) &&
+                         typeid(*this) != typeid(LinearShallowWaterModel)))
+    return;
+  m_default_hook = true;
+  swg_check(swg_model_set_forcing(m_handle, nullptr, nullptr));
+}
+
 // --------------------------------------------------------------- steppers --
 
 struct TimeStepper {
@@ -500,6 +613,7 @@ struct TimeStepper {
   }
   TimeStepper(ShallowWaterModel &shallow_water, int kind, int nstages)
       : m_shallow_water(&shallow_water) {
+    shallow_water.settle_hook(); // the model is fully constructed here
     swg_check(swg_stepper_create(shallow_water.m_handle, kind, nstages,
                                  &m_handle));
   }

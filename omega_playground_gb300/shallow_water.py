@@ -364,6 +364,45 @@ class ShallowWaterModel:
         check(lib().swg_compute_tendency(self._h, tend.handle, state.handle,
                                          float(t), int(add_mode), _s(stream)))
 
+    def compute_aux(self, h, vn, tr=None, stream=None):
+        """m_aux_state.compute(h, vn, tr, f_vertex, mesh)
+        (shallow_water_auxstate.cpp:12-50) on device arrays: a
+        ShallowWaterState's fields (state.device_ptrs()), torch tensors or
+        raw device pointers; f_vertex is the model's own m_f_vertex."""
+        check(lib().swg_model_compute_aux(self._h, _dev(h), _dev(vn),
+                                          _dev(tr), _s(stream)))
+
+    def compute_h_tendency(self, h_tend, h, vn, add_mode=AddMode.replace,
+                           stream=None):
+        """shallow_water_model.hpp:36-37: the thickness tendency from the
+        last auxiliary state (its mean thickness) and vn."""
+        check(lib().swg_compute_h_tendency(self._h, _dev(h_tend), _dev(h),
+                                           _dev(vn), int(add_mode),
+                                           _s(stream)))
+
+    def compute_vn_tendency(self, vn_tend, h, vn, add_mode=AddMode.replace,
+                            stream=None):
+        """shallow_water_model.hpp:38-39: the normal-velocity tendency from
+        the last auxiliary state, vn (PV flux) and h (SSH gradient)."""
+        check(lib().swg_compute_vn_tendency(self._h, _dev(vn_tend), _dev(h),
+                                            _dev(vn), int(add_mode),
+                                            _s(stream)))
+
+    def compute_tr_tendency(self, tr_tend, tr, vn, add_mode=AddMode.replace,
+                            stream=None):
+        """shallow_water_model.hpp:40-41: the tracer tendencies from the
+        last auxiliary state (normalised tracers, mean thickness) and vn;
+        tr is not read, as in the reference."""
+        check(lib().swg_compute_tr_tendency(self._h, _dev(tr_tend), _dev(tr),
+                                            _dev(vn), int(add_mode),
+                                            _s(stream)))
+
+    @property
+    def m_aux_state(self):
+        """Read-only view of the auxiliary state of the last evaluation:
+        reference-named members holding host copies (see AuxStateView)."""
+        return AuxStateView(self)
+
     def aux(self, name: str) -> np.ndarray:
         """Copy of a named intermediate of the last tendency evaluation."""
         p, n = _dp(), C.c_longlong()
@@ -404,6 +443,72 @@ class ShallowWaterModel:
         if getattr(self, "_h", None) and _capi._lib is not None:
             _capi._lib.swg_model_destroy(self._h)
             self._h = None
+
+
+def _dev(x):
+    """Device address of x: None, an int pointer, a torch tensor or an
+    object with __cuda_array_interface__."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return C.c_void_p(x)
+    if hasattr(x, "data_ptr"):
+        return C.c_void_p(x.data_ptr())
+    if hasattr(x, "__cuda_array_interface__"):
+        return C.c_void_p(x.__cuda_array_interface__["data"][0])
+    raise TypeError(f"not a device array: {type(x).__name__}")
+
+
+class AuxStateView:
+    """The reference's ShallowWaterAuxiliaryState member groups
+    (shallow_water_auxstate.hpp) over the model's intermediates, read when
+    accessed (host copies).  The mean thickness is kept once
+    (m_mean_h_edge is m_flux_h_edge); the vorticity terms are kept summed:
+    m_pv_vertex = norm_rvort_vertex + norm_pvort_vertex and m_pv_edge =
+    2 (norm_rvort_edge + norm_pvort_edge).  A member the configuration does
+    not compute is None."""
+
+    _GROUPS = {
+        "m_thickness_aux": {"m_mean_h_edge": "mean_h_edge",
+                            "m_flux_h_edge": "mean_h_edge"},
+        "m_vorticity_aux": {"m_rvort_vertex": "rvort_vertex",
+                            "m_pv_vertex": "q_vertex",
+                            "m_pv_edge": "pv_edge"},
+        "m_kinetic_aux": {"m_ke_cell": "ke_cell",
+                          "m_vel_div_cell": "vel_div_cell"},
+        "m_tracer_aux": {"m_norm_tr_cell": "norm_tr_cell"},
+    }
+
+    def __init__(self, model):
+        self._model = model
+
+    def compute(self, h, vn, tr=None, f_vertex=None, mesh=None, stream=None):
+        """shallow_water_auxstate.cpp:12-50 (f_vertex: the model's own)."""
+        self._model.compute_aux(h, vn, tr, stream)
+
+    def __getattr__(self, group):
+        names = AuxStateView._GROUPS.get(group)
+        if names is None:
+            raise AttributeError(group)
+        model = self._model
+        me = model.m_mesh
+        rows = {"edge": me.m_nedges, "vertex": me.m_nvertices,
+                "cell": me.m_ncells}
+
+        class _Group:
+            pass
+        g = _Group()
+        for member, name in names.items():
+            try:
+                a = model.aux(name)
+            except _capi.SwgError:
+                a = None
+            if a is not None:
+                n = rows[name.rsplit("_", 1)[1]]
+                a = a.reshape(-1, n, me.m_nlayers) if name == "norm_tr_cell" \
+                    else a.reshape(n, me.m_nlayers)
+            setattr(g, member, a)
+        return g
 
 
 _cudart_lib = None
@@ -801,6 +906,16 @@ def adjoint_plan(nsteps: int, nsnapshots: int, nstages: int = 4):
     check(lib().swg_adj_plan(int(nsteps), int(nsnapshots), int(nstages),
                              C.byref(a), C.byref(b)))
     return a.value, b.value
+
+
+def fp64_issue_rate(op: str = "dfma", iters: int = 20000, stream=None):
+    """(thread-instructions/s, kernel ms) of FP64 `op` ('dfma', 'dadd',
+    'dmul') on the current GPU, every SM filled (blocking)."""
+    code = {"dfma": 0, "dadd": 1, "dmul": 2}[op]
+    r, ms = C.c_double(), C.c_double()
+    check(lib().swg_fp64_issue_rate(code, int(iters), C.byref(r), C.byref(ms),
+                                    _s(stream)))
+    return r.value, ms.value
 
 
 def _diag(fn, state, model, stream=None):

@@ -100,6 +100,10 @@ def lib():
         L.or_model_aux.restype = _dp
         L.or_compute_tendency.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp,
                                           _dp, _dp, C.c_double, C.c_int]
+        L.or_aux_compute.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        L.or_h_tendency.argtypes = [C.c_void_p, _dp, _dp, C.c_int]
+        L.or_vn_tendency.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_int]
+        L.or_tr_tendency.argtypes = [C.c_void_p, _dp, _dp, C.c_int]
         L.or_step.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp,
                               C.c_double, C.c_double, C.c_int]
         L.or_step.restype = C.c_int
@@ -223,6 +227,29 @@ class OracleModel:
         lib().or_compute_tendency(self._h, _dptr(th), _dptr(tv), _dptr(tt),
                                   _dptr(h), _dptr(vn), _dptr(tr), t, add_mode)
         return th, tv, tt
+
+    def compute_aux(self, h, vn, tr):
+        """m_aux_state.compute (shallow_water_auxstate.cpp:12-50)."""
+        tr = tr if tr is not None else np.zeros(self.shapes()[2])
+        lib().or_aux_compute(self._h, _dptr(h), _dptr(vn), _dptr(tr))
+
+    def compute_h_tendency(self, h_tend, vn, add_mode=0):
+        """compute_h_tendency (shallow_water_model.cpp:43-84) from the last
+        auxiliary state and vn; h_tend in place."""
+        lib().or_h_tendency(self._h, _dptr(h_tend), _dptr(vn), add_mode)
+        return h_tend
+
+    def compute_vn_tendency(self, vn_tend, h, vn, add_mode=0):
+        """compute_vn_tendency (shallow_water_model.cpp:86-219)."""
+        lib().or_vn_tendency(self._h, _dptr(vn_tend), _dptr(h), _dptr(vn),
+                             add_mode)
+        return vn_tend
+
+    def compute_tr_tendency(self, tr_tend, vn, add_mode=0):
+        """compute_tr_tendency (shallow_water_model.cpp:221-311): the
+        normalised tracers come from the auxiliary state."""
+        lib().or_tr_tendency(self._h, _dptr(tr_tend), _dptr(vn), add_mode)
+        return tr_tend
 
     def step(self, h, vn, tr, t0, dt, nsteps, kind="lsrk", nstages=5):
         """In place on (h, vn, tr); kind 'rk4' or 'lsrk'."""

@@ -350,8 +350,8 @@ double *or_model_aux(or_model *md, const char *name, size_t *n) {
 }
 
 /* ShallowWaterAuxiliaryState::compute (shallow_water_auxstate.cpp:12-50). */
-static void aux_compute(or_model *md, const double *h, const double *vn,
-                        const double *tr) {
+void or_aux_compute(or_model *md, const double *h, const double *vn,
+                    const double *tr) {
   const or_mesh *m = &md->m;
   const int K = m->nlayers, C = m->ncells, E = m->nedges, V = m->nvertices;
   const int T = md->p.ntracers;
@@ -424,8 +424,8 @@ static void aux_compute(or_model *md, const double *h, const double *vn,
 /* ShallowWaterModel::compute_h_tendency (shallow_water_model.cpp:71-84,
  * default inner-if kernel) with ThicknessHorzAdvOnCell
  * (thickness_hadv_cell.hpp:59-83); the flux thickness is m_flux_h_edge. */
-static void h_tendency(or_model *md, double *h_tend, const double *vn,
-                       int add_mode) {
+void or_h_tendency(or_model *md, double *h_tend, const double *vn,
+                   int add_mode) {
   const or_mesh *m = &md->m;
   const int K = m->nlayers, C = m->ncells;
 #pragma omp parallel for schedule(static)
@@ -450,8 +450,8 @@ static void h_tendency(or_model *md, double *h_tend, const double *vn,
 }
 
 /* ShallowWaterModel::compute_vn_tendency (shallow_water_model.cpp:88-219). */
-static void vn_tendency(or_model *md, double *vn_tend, const double *h,
-                        const double *vn, int add_mode) {
+void or_vn_tendency(or_model *md, double *vn_tend, const double *h,
+                    const double *vn, int add_mode) {
   const or_mesh *m = &md->m;
   const or_params *p = &md->p;
   const int K = m->nlayers, C = m->ncells, E = m->nedges, V = m->nvertices;
@@ -588,8 +588,8 @@ static void vn_tendency(or_model *md, double *vn_tend, const double *h,
 /* ShallowWaterModel::compute_tr_tendency (shallow_water_model.cpp:221-311).
  * The reference passes m_mean_h_edge as the flux thickness and
  * m_flux_h_edge as the mean thickness (:225-228); both hold the same values. */
-static void tr_tendency(or_model *md, double *tr_tend, const double *vn,
-                        int add_mode) {
+void or_tr_tendency(or_model *md, double *tr_tend, const double *vn,
+                    int add_mode) {
   const or_mesh *m = &md->m;
   const or_params *p = &md->p;
   const int K = m->nlayers, C = m->ncells, T = p->ntracers;
@@ -746,13 +746,13 @@ void or_compute_tendency(or_model *md, double *h_tend, double *vn_tend,
     linear_tendency(md, h_tend, vn_tend, h, vn, add_mode);
     return;
   }
-  aux_compute(md, h, vn, tr);
+  or_aux_compute(md, h, vn, tr);
   if (!md->p.disable_h_tendency)
-    h_tendency(md, h_tend, vn, add_mode);
+    or_h_tendency(md, h_tend, vn, add_mode);
   if (!md->p.disable_vn_tendency)
-    vn_tendency(md, vn_tend, h, vn, add_mode);
+    or_vn_tendency(md, vn_tend, h, vn, add_mode);
   if (md->p.ntracers > 0)
-    tr_tendency(md, tr_tend, vn, add_mode);
+    or_tr_tendency(md, tr_tend, vn, add_mode);
 }
 
 /* ------------------------------------------------------------ steppers --- */

@@ -90,6 +90,21 @@ void or_compute_tendency(or_model *md, double *h_tend, double *vn_tend,
                          double *tr_tend, const double *h, const double *vn,
                          const double *tr, double t, int add_mode);
 
+/* The split compute_tendency of the reference: the auxiliary state
+ * (ShallowWaterAuxiliaryState::compute, shallow_water_auxstate.cpp:12-50)
+ * and the per-field tendencies from it (compute_h_tendency,
+ * compute_vn_tendency, compute_tr_tendency: shallow_water_model.cpp:43-311),
+ * which read the aux state of the last or_aux_compute / or_compute_tendency
+ * and their own arguments.  Nonlinear model only. */
+void or_aux_compute(or_model *md, const double *h, const double *vn,
+                    const double *tr);
+void or_h_tendency(or_model *md, double *h_tend, const double *vn,
+                   int add_mode);
+void or_vn_tendency(or_model *md, double *vn_tend, const double *h,
+                    const double *vn, int add_mode);
+void or_tr_tendency(or_model *md, double *tr_tend, const double *vn,
+                    int add_mode);
+
 /* nsteps steps of RK4Stepper (kind 0) or LSRKStepper (kind 1, nstages 5 or
  * 1) starting at t0, in place on (h, vn, tr).  Stepper scratch persists in
  * the model across calls, like the reference's stepper members. */

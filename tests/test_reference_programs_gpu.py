@@ -125,3 +125,42 @@ def test_cpp_model_variants():
     equal."""
     out = run("model_variants")
     assert "PASS" in out and out.count("twin 1") == 2, out
+
+
+def test_cpp_aux_state_and_field_tendencies():
+    """The C++ drop-in's m_aux_state and compute_h/vn/tr_tendency: after
+    compute_tendency the three per-field methods reproduce it bit for bit,
+    increment adds it again, m_aux_state.compute of another state gives
+    that state's mean thickness exactly, and a plain model's first step
+    launches the fused graph (its hook is dropped when the stepper is
+    built)."""
+    out = run("field_tendencies")
+    assert "PASS" in out, out
+    assert "bit for bit 1" in out and "again 1" in out, out
+
+
+def test_rcp_nr_within_one_ulp_of_division():
+    """The kernels' Newton-Raphson reciprocal (rcp.approx.ftz.f64 plus two
+    Newton steps, swg_device.cuh) against CUDA's IEEE 1.0 / x on the device:
+    log-spaced 1e-6 .. 1e6 of both signs, random mantissas in every binade of
+    [2^-40, 2^40] and thin-layer thicknesses 1e-3 .. 1e1.  Bound: 1 ulp of the
+    correctly rounded quotient (measured maximum printed)."""
+    import re
+    out = run("rcp_accuracy")
+    m = re.search(r"samples (\d+) max_ulp (\d+)", out)
+    assert m, out
+    assert int(m.group(1)) > 600000
+    assert int(m.group(2)) <= 1, out
+
+
+def test_fp64_issue_rate_is_measured():
+    """swg_fp64_issue_rate returns a positive DFMA / DADD / DMUL rate below
+    the architectural ceiling of 2 FP64 thread-instructions per SM per clock
+    at the GPU's maximum clock."""
+    import omega_playground_gb300 as og
+    import torch
+    props = torch.cuda.get_device_properties(0)
+    ceiling = 2.0 * props.multi_processor_count * 2.2e9
+    for op in ("dfma", "dadd", "dmul"):
+        rate, ms = og.fp64_issue_rate(op, 4000)
+        assert 0 < rate < ceiling and ms > 0, (op, rate)

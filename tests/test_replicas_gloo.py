@@ -126,3 +126,7 @@ def test_reference_arm_json_line(capsys, monkeypatch):
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"],
                            "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert line["config"]["workload"] == wl.name
+    # the same config keys as the GPU arm's line (the workload, stepper,
+    # dt, parallelism, L2 note and the sampled level count)
+    assert line["config"] == bench.workload_config(wl, 1, wl.nlayers)
+    assert cb["cpu_model"]
