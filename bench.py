@@ -426,7 +426,7 @@ def run_ours(args, wl):
                           "alg_bytes": stage_bytes, "ms": stage_ms,
                           "frac": stage_bytes / (stage_ms / 1e3) / 1e9 / peak}}
     # FP64 issue roof, measured here: DFMA / DADD / DMUL issue rates of this
-    # GPU (swg_fp64_issue_rate: every SM filled, 8 independent chains per
+    # GPU (swg_fp64_issue_rate: every SM filled, 4 independent chains per
     # thread, CUDA events) with the SM clock sampled while they run.  The
     # instructions per cell-level of k_cell_final come from ncu on the
     # 256x256x64x8 case (DFMA 132 + DMUL 15 + DADD 8 = 155 with 8 tracers).
@@ -435,7 +435,7 @@ def run_ours(args, wl):
         sms = torch.cuda.get_device_properties(local).multi_processor_count
         pk_clocks = ClockSampler(uuid)
         time.sleep(0.3)
-        rates = {op: og.fp64_issue_rate(op, 20000, stream=sh)
+        rates = {op: og.fp64_issue_rate(op, 40000, stream=sh)
                  for op in ("dfma", "dadd", "dmul")}
         pk_clk = pk_clocks.stop()
         pk_mhz = pk_clk.get("sm_mhz") or 0.0

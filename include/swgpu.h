@@ -476,7 +476,7 @@ int swg_adj_schedule(int nsteps, int nsnapshots, int nstages,
 /* ----------------------------------------------------- measurement -----
  * FP64 issue rate of the current GPU (no counterpart in the reference): op
  * 0 DFMA, 1 DADD, 2 DMUL; every SM filled with resident threads, each
- * running 8 independent chains for `iters` iterations, timed with CUDA
+ * running 4 independent chains for `iters` iterations, timed with CUDA
  * events on `stream` (blocking).  *inst_per_s gets thread-instructions per
  * second, *ms (may be NULL) the timed kernel's duration.  The solver's
  * kernels are bound by this rate, not by HBM bandwidth. */
