@@ -353,6 +353,7 @@ def run_ours(args, wl):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     import omega_playground_gb300 as og
+    from omega_playground_gb300.shallow_water import gpu_numa_node
 
     mesh = og.PlanarHexagonalMesh(wl.nx, wl.ny, wl.dc, wl.nlayers)
     params = wl.params()
@@ -474,13 +475,40 @@ def run_ours(args, wl):
         nbytes_in = hh.nbytes + vv.nbytes + tt.nbytes
         hs.step(hh, vv, tt, 0.0, wl.dt, 1, stream=sh)  # captures the graphs
         ups = world * wl.ncells * wl.nlayers * wl.nstages * args.e2e_steps
+
+        def link_rates():
+            """Host link rates of these page-locked arrays: whole-state
+            upload and download (CUDA events, best of 3)."""
+            up, down = [], []
+            for _ in range(3):
+                barrier()
+                e0.record(stream)
+                state.upload(hh, vv, tt, stream=sh)
+                e1.record(stream)
+                barrier()
+                up.append(e0.elapsed_time(e1))
+                e0.record(stream)
+                state.download(stream=sh, out=(hh, vv, tt))
+                e1.record(stream)
+                barrier()
+                down.append(e0.elapsed_time(e1))
+            return {"h2d_gbs": round(nbytes_in / min(up) / 1e6, 1),
+                    "d2h_gbs": round(nbytes_in / min(down) / 1e6, 1)}
+        link_before = link_rates()
+        e2e_clocks = ClockSampler(uuid)
+        time.sleep(0.3)
         barrier()
+        call_ms = []
         e0.record(stream)
         for s in range(args.e2e_steps):
+            t_call = time.perf_counter()
             hs.step(hh, vv, tt, s * wl.dt, wl.dt, 1, stream=sh)
+            call_ms.append((time.perf_counter() - t_call) * 1e3)
         e1.record(stream)
         barrier()
         e2e_ms = e0.elapsed_time(e1)
+        e2e_clk = e2e_clocks.stop()
+        link_after = link_rates()
         hh[...], vv[...], tt[...] = h0, vn0, tr0
         barrier()
         e0.record(stream)
@@ -497,8 +525,18 @@ def run_ours(args, wl):
                "ms_per_step": e2e_ms / args.e2e_steps,
                "api": "swg_host_step (HostStepper), page-locked host arrays",
                "level_chunks": hs.chunks,
+               "call_ms": {"min": round(min(call_ms), 2),
+                           "median": round(float(np.median(call_ms)), 2),
+                           "max": round(max(call_ms), 2),
+                           "each": [round(x, 2) for x in call_ms]},
                "chunk_tuning_ms_per_step": tuning and {
                    k: round(v, 2) for k, v in tuning.items()},
+               "chunk_tuning_statistic": "median of 5 one-step calls",
+               "host_link": {"before": link_before, "after": link_after,
+                             "bytes_each_way": nbytes_in,
+                             "numa": dict(zip(("gpu_node", "host_nodes"),
+                                              gpu_numa_node()))},
+               "clocks": e2e_clk,
                "serial_upload_step_download": {
                    "value": ups / (serial_ms / 1e3),
                    "ms_per_step": serial_ms / args.e2e_steps}}

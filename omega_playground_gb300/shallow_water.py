@@ -521,6 +521,8 @@ def _cudart():
         _cudart_lib = C.CDLL("libcudart.so.13")
         _cudart_lib.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t,
                                            C.c_int]
+        _cudart_lib.cudaDeviceGetPCIBusId.argtypes = [C.c_char_p, C.c_int,
+                                                      C.c_int]
     return _cudart_lib
 
 
@@ -590,13 +592,72 @@ class LSRKStepper(TimeStepper):
         super().__init__(shallow_water, nstages)
 
 
+def gpu_numa_node(device: int | None = None):
+    """(NUMA node of the current GPU's PCI function, number of host NUMA
+    nodes with CPUs); the node is None where the system does not say."""
+    import glob
+    import os
+    nodes = [n for n in glob.glob("/sys/devices/system/node/node[0-9]*")
+             if open(os.path.join(n, "cpulist")).read().strip()]
+    node = None
+    try:
+        cudart = _cudart()
+        dev = C.c_int(0)
+        if device is None:
+            cudart.cudaGetDevice(C.byref(dev))
+        else:
+            dev.value = int(device)
+        bus = C.create_string_buffer(64)
+        if cudart.cudaDeviceGetPCIBusId(bus, 64, dev) == 0:
+            path = ("/sys/bus/pci/devices/" + bus.value.decode().lower()
+                    + "/numa_node")
+            v = int(open(path).read().strip())
+            node = v if v >= 0 else None
+    except Exception:
+        node = None
+    if node is None and len(nodes) == 1:
+        node = int(nodes[0].rsplit("node", 1)[1])
+    return node, len(nodes)
+
+
+def _node_cpus(node: int):
+    cpus = set()
+    text = open(f"/sys/devices/system/node/node{node}/cpulist").read().strip()
+    for part in text.split(","):
+        if part:
+            a, _, b = part.partition("-")
+            cpus |= set(range(int(a), int(b or a) + 1))
+    return cpus
+
+
 def pinned_empty(shape) -> np.ndarray:
     """An uninitialised float64 array in page-locked host memory
-    (swg_host_alloc), freed when the last array viewing it goes away."""
+    (swg_host_alloc), freed when the last array viewing it goes away.  On a
+    host with several NUMA nodes the calling thread runs on the CPUs of the
+    GPU's node while the memory is allocated and locked, so its pages come
+    from the memory nearest the GPU (the thread's CPU set is restored
+    afterwards; no GPU setting changes)."""
+    import os
     shape = tuple(int(n) for n in np.atleast_1d(shape))
     n = int(np.prod(shape))
     p = C.c_void_p()
-    check(lib().swg_host_alloc(max(n, 1) * 8, C.byref(p)))
+    node, nnodes = gpu_numa_node()
+    saved = None
+    if node is not None and nnodes > 1 and hasattr(os, "sched_setaffinity"):
+        try:
+            saved = os.sched_getaffinity(0)
+            near = _node_cpus(node) & saved
+            if near:
+                os.sched_setaffinity(0, near)
+            else:
+                saved = None
+        except OSError:
+            saved = None
+    try:
+        check(lib().swg_host_alloc(max(n, 1) * 8, C.byref(p)))
+    finally:
+        if saved is not None:
+            os.sched_setaffinity(0, saved)
     buf = (C.c_double * max(n, 1)).from_address(p.value)
     buf._owner = _PinnedBlock(p.value)
     return np.frombuffer(buf, np.float64, n).reshape(shape)
@@ -651,7 +712,7 @@ class HostStepper:
     @classmethod
     def autotuned(cls, model: ShallowWaterModel, stepper: str = "lsrk",
                   nstages: int = 5, state=None, dt: float = 1.0,
-                  candidates=None, reps: int = 3):
+                  candidates=None, reps: int = 5):
         """The stepper whose chunk layout steps fastest on this machine,
         and {layout: ms per step}.  A candidate is a level chunk (int, 0:
         one chunk) or a list of chunk sizes; the default tries one chunk,
@@ -659,9 +720,10 @@ class HostStepper:
         4 or 8 levels.  Each candidate is timed (host wall clock, the call
         being synchronous) over `reps` one-step calls after one untimed
         call, on page-locked copies of `state` = (h, vn, tr) host arrays,
-        which are left unchanged; a candidate's figure is its fastest call,
-        so that a call slowed by other traffic on the host link does not
-        decide.  The fastest layout depends on the host link."""
+        which are left unchanged; a candidate's figure is the median of its
+        calls, the figure back-to-back calls reach (the fastest single call
+        overstates it when the host link is shared).  The fastest layout
+        depends on the host link."""
         import time
         K = model.m_mesh.m_nlayers
         if candidates is None:
@@ -693,7 +755,7 @@ class HostStepper:
                 t0 = time.perf_counter()
                 hs.step(*arrs, 0.0, dt, 1)
                 times.append((time.perf_counter() - t0) * 1e3)
-            table[key] = min(times)  # the layout's capability, not link noise
+            table[key] = float(np.median(times))
             if best is None or table[key] < table[best[0]]:
                 best = (key, hs)
         return best[1], table
