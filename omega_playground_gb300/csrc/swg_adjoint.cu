@@ -73,39 +73,47 @@ struct AdjIO {
   const double *h, *vn, *tr;    // state X
   const double *mh_, *mvn, *mtr; // mu (adjoint of the tendency)
   double *lh, *lvn, *ltr;        // lambda = J^T mu (written unless null)
-  // fused stage bookkeeping (each may be null): acc += lambda, and the next
-  // stage's mu: RK4  mu_next = alpha * lam + beta * lambda;
-  //             LSRK mu_next = alpha * acc (after the update) + gamma * mu
+  // fused stage bookkeeping (each may be null): acc = acc_in + lambda, and
+  // the next stage's mu (mode): 0 RK4  mu_next = alpha * lam + beta * lambda;
+  //                             1 LSRK mu_next = alpha * acc + gamma * mu;
+  //                             2 next step: mu_next = alpha * acc
+  // (acc after the update).  acc_in is acc itself except where a step's
+  // first stage reads lam and its last stage writes lam, which saves the
+  // copies between the two.
+  const double *acc_in_h, *acc_in_vn, *acc_in_tr;
   double *acc_h, *acc_vn, *acc_tr;
   double *nmu_h, *nmu_vn, *nmu_tr;
   const double *lam_h, *lam_vn, *lam_tr;
   double alpha, beta, gamma;
-  int lsrk;
+  int mode;
 };
 
-__device__ __forceinline__ void emit(const AdjIO &io, double *out, double *acc,
+__device__ __forceinline__ void emit(const AdjIO &io, double *out,
+                                     const double *acc_in, double *acc,
                                      double *nmu, const double *lam,
                                      const double *mu, size_t i, double x) {
   if (out)
     out[i] = x;
   double a = 0;
   if (acc) {
-    a = acc[i] + x;
+    a = acc_in[i] + x;
     acc[i] = a;
   }
   if (nmu)
-    nmu[i] = io.lsrk ? fma(io.alpha, a, io.gamma * mu[i])
-                     : fma(io.alpha, lam[i], io.beta * x);
+    nmu[i] = io.mode == 2   ? io.alpha * a
+             : io.mode == 1 ? fma(io.alpha, a, io.gamma * mu[i])
+                            : fma(io.alpha, lam[i], io.beta * x);
 }
 
 // --- pass 1: transposed edge stencils of the velocity tendency (cells and
 // vertices), and Q mu_vn per edge for the transposed PV flux; the first V*K
-// threads take vertices, the next C*K cells, the last E*K edges.
+// threads take vertices, the next C*K cells, the last E*K edges (the grid
+// starts at `base`: V*K when the vertex part, velocity del4, is off).
 __global__ void __launch_bounds__(ATPB)
     ka_vel(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
-           AdjIO io) {
+           AdjIO io, unsigned base) {
   const int K = m.nlayers;
-  unsigned i = blockIdx.x * ATPB + threadIdx.x;
+  unsigned i = base + blockIdx.x * ATPB + threadIdx.x;
   const unsigned VK = unsigned(m.nvertices) * K, CK = unsigned(m.ncells) * K;
   if (i >= VK + CK) {
     i -= VK + CK;
@@ -238,7 +246,7 @@ __global__ void __launch_bounds__(ATPB)
       for (int j = 0; j < MAXE; ++j)
         ln = fma(mnb[j], lL[size_t(nb[j]) * K + k], ln);
     }
-    emit(io, io.ltr, io.acc_tr, io.nmu_tr, io.lam_tr, io.mtr, t,
+    emit(io, io.ltr, io.acc_in_tr, io.acc_tr, io.nmu_tr, io.lam_tr, io.mtr, t,
          ln * r);
     hsum = fma(ln, a.ntr[t], hsum);
   }
@@ -329,14 +337,29 @@ __global__ void __launch_bounds__(ATPB)
   w.lvnp[i] = fma(mh, lF, w.lvnp[i]);
 }
 
-// --- pass 5: vertices: PV q = (zeta + f) / h_v, vorticity.
+// --- pass 5: vertices: PV q = (zeta + f) / h_v, vorticity; and, in the
+// C*K threads after the V*K vertex threads (launched with velocity
+// dissipation on), the cells' velocity-divergence adjoint, which reads only
+// the edge pass's output.  Splitting it from the cell pass lets the cell
+// and edge output passes run concurrently.
 __global__ void __launch_bounds__(ATPB)
     ka_vertex(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
               AdjIO io) {
   const int K = m.nlayers;
-  const unsigned i = blockIdx.x * ATPB + threadIdx.x;
-  if (i >= unsigned(m.nvertices) * K)
+  unsigned i = blockIdx.x * ATPB + threadIdx.x;
+  const unsigned VK = unsigned(m.nvertices) * K;
+  if (i >= VK) {
+    i -= VK;
+    if (i >= unsigned(m.ncells) * K)
+      return;
+    const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
+    double ld = 0;
+    for (int j = 0; j < MAXE; ++j)
+      ld = fma(__ldg(v.divadj + 6 * c + j),
+               w.ld2u[size_t(__ldg(m.ec + 6 * c + j)) * K + k], ld);
+    w.ldiv[i] = ld;
     return;
+  }
   const int vx = int(i / unsigned(K)), k = int(i - unsigned(vx) * K);
   const int e0 = __ldg(m.ev + 3 * vx), e1 = __ldg(m.ev + 3 * vx + 1),
             e2 = __ldg(m.ev + 3 * vx + 2);
@@ -362,7 +385,7 @@ __global__ void __launch_bounds__(ATPB)
   w.lhv[i] = -(a.q[i] * r * lq);
 }
 
-// --- pass 6: cells: thickness adjoint, velocity divergence adjoint.
+// --- pass 6: cells: thickness adjoint.
 __global__ void __launch_bounds__(ATPB)
     ka_cell(MeshView m, ModelView p, AdjView v, AdjWork w, AdjIO io) {
   const int K = m.nlayers;
@@ -370,24 +393,19 @@ __global__ void __launch_bounds__(ATPB)
   if (i >= unsigned(m.ncells) * K)
     return;
   const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
-  double lh = 0, ld = 0;
+  double lh = 0;
   for (int j = 0; j < MAXE; ++j) {
     const int e = __ldg(m.ec + 6 * c + j);
     lh = fma(__ldg(v.hm_c + 6 * c + j), w.lmh[size_t(e) * K + k], lh);
-    if (p.do_vn) {
+    if (p.do_vn)
       lh = fma(__ldg(v.ckvh + 6 * c + j),
                w.lhv[size_t(__ldg(v.cvtx + 6 * c + j)) * K + k], lh);
-      if (p.vel_del2 | p.vel_del4)
-        ld = fma(__ldg(v.divadj + 6 * c + j), w.ld2u[size_t(e) * K + k], ld);
-    }
   }
   if (p.do_vn)
     lh = fma(p.grav, w.lke[i], lh); // SSH gradient: g times the KE term
   if (p.ntracers > 0)
     lh += w.lhtr[i];
-  emit(io, io.lh, io.acc_h, io.nmu_h, io.lam_h, io.mh_, i, lh);
-  if (p.do_vn && (p.vel_del2 | p.vel_del4))
-    w.ldiv[i] = ld;
+  emit(io, io.lh, io.acc_in_h, io.acc_h, io.nmu_h, io.lam_h, io.mh_, i, lh);
 }
 
 // --- pass 7: edges: normal velocity adjoint.
@@ -409,7 +427,8 @@ __global__ void __launch_bounds__(ATPB)
       l = fma(__ldg(v.ccd_e2 + 2 * e + 1), w.ldiv[size_t(c1) * K + k], l);
     }
   }
-  emit(io, io.lvn, io.acc_vn, io.nmu_vn, io.lam_vn, io.mvn, i, l);
+  emit(io, io.lvn, io.acc_in_vn, io.acc_vn, io.nmu_vn, io.lam_vn, io.mvn, i,
+       l);
 }
 
 // y = alpha x1 + beta x2 (x2 may be null); dual pack / unpack
@@ -774,7 +793,9 @@ void adj_passes(swg_adjoint ad, const AuxView &aux, const AdjIO &io,
   const Fork *fk = &md->fork;
   const bool trd = p.ntracers > 0 && (p.tr_del2 | p.tr_del4);
   auto vel = [&](cudaStream_t q) {
-    ka_vel<<<nb(VK + CK + EK), ATPB, 0, q>>>(m, p, aux, v, w, io);
+    const long long base = p.vel_del4 ? 0 : VK; // vertex part: del4 only
+    ka_vel<<<nb(VK + CK + EK - base), ATPB, 0, q>>>(m, p, aux, v, w, io,
+                                                    unsigned(base));
     ++g_launches;
   };
   auto tr1 = [&](cudaStream_t q) {
@@ -820,12 +841,18 @@ void adj_passes(swg_adjoint ad, const AuxView &aux, const AdjIO &io,
     }
     edge(st);
   }
-  if (p.do_vn) {
-    ka_vertex<<<nb(VK), ATPB, 0, st>>>(m, p, aux, v, w, io);
+  if (p.do_vn) { // vertices, then (velocity dissipation) the cells' ldiv
+    const bool vdiss = p.vel_del2 | p.vel_del4;
+    ka_vertex<<<nb(VK + (vdiss ? CK : 0)), ATPB, 0, st>>>(m, p, aux, v, w,
+                                                          io);
     ++g_launches;
   }
-  ka_cell<<<nb(CK), ATPB, 0, st>>>(m, p, v, w, io);
-  ka_vn<<<nb(EK), ATPB, 0, st>>>(m, p, v, w, io);
+  // the two output passes read disjoint work arrays and write disjoint
+  // outputs (h: lh and its stage bookkeeping; vn: the same for vn)
+  fork_join(
+      fk, st,
+      [&](cudaStream_t q) { ka_vn<<<nb(EK), ATPB, 0, q>>>(m, p, v, w, io); },
+      [&](cudaStream_t q) { ka_cell<<<nb(CK), ATPB, 0, q>>>(m, p, v, w, io); });
   g_launches += 2;
 }
 
@@ -948,28 +975,35 @@ int tape_step(swg_adjoint ad, TapeSlot &tp, double dt, swg_state out,
 }
 
 // lam <- adjoint of the step taped in tp, applied to lam.  The output passes
-// of stage s accumulate lamX_s into lacc and form mu_{s-1} directly
-// (ping-pong mu buffers: the passes of stage s still read mu_s).
+// of stage s accumulate lamX_s and form mu_{s-1} directly (ping-pong mu
+// buffers: the passes of stage s still read mu_s).  The first reversed
+// stage adds to lam and writes lacc, the last adds to lacc and writes lam,
+// so no copy between them is needed.  With an even stage count (RK4) the
+// last stage also forms the next step's first mu, dt b_{ns-1} lam, in the
+// buffer that step reads first (bwd_begin forms the first one); with an
+// odd count a separate pass forms it at the start of every step.
 //
 // Low-storage RK (ns stages): with lamX_s the adjoint of the stage input X_s
 // and mu_s that of T_s, mu_{ns-1} = dt b_{ns-1} lam,
 // lamX_s = lamX_{s+1} + J(X_s)^T mu_s and
 // mu_{s-1} = dt b_{s-1} lamX_s + a_s mu_s; the step's adjoint is lamX_0.
 // The output passes accumulate lamX in lacc and form mu_{s-1} from it.
+const double *step_rkb(const swg_adjoint ad) {
+  static const double rk4b[4] = {1. / 6, 1. / 3, 1. / 3, 1. / 6};
+  return ad->kind != SWG_STEPPER_RK4 ? ad->rkb.data() : rk4b;
+}
+
 int adjoint_step(swg_adjoint ad, const TapeSlot &tp, double dt,
                  cudaStream_t st) {
   static const double rk4a[3] = {1. / 2, 1. / 2, 1};
-  static const double rk4b[4] = {1. / 6, 1. / 3, 1. / 3, 1. / 6};
   const bool lsrk = ad->kind != SWG_STEPPER_RK4;
   const int ns = ad->ns;
+  const bool even = ns % 2 == 0;
   const double *rka = lsrk ? ad->rka.data() : rk4a;
-  const double *rkb = lsrk ? ad->rkb.data() : rk4b;
+  const double *rkb = step_rkb(ad);
   const long long n = (long long)words(ad->model);
-  cudaError_t err = cudaMemcpyAsync(ad->lacc->h, ad->lam->h, n * 8,
-                                    cudaMemcpyDeviceToDevice, st);
-  if (err != cudaSuccess)
-    return cuda_fail(err, "swg_adjoint: copy");
-  lincomb(ad->mu, ad->lam, nullptr, dt * rkb[ns - 1], 0.0, n, st);
+  if (!even)
+    lincomb(ad->mu, ad->lam, nullptr, dt * rkb[ns - 1], 0.0, n, st);
   swg_state mus[2] = {ad->mu, ad->mu2};
   for (int s = ns - 1; s >= 0; --s) {
     swg_state mu = mus[(ns - 1 - s) % 2], nmu = mus[(ns - s) % 2];
@@ -978,27 +1012,34 @@ int adjoint_step(swg_adjoint ad, const TapeSlot &tp, double dt,
     io.mh_ = mu->h;
     io.mvn = mu->vn;
     io.mtr = mu->tr;
-    io.acc_h = ad->lacc->h;
-    io.acc_vn = ad->lacc->vn;
-    io.acc_tr = ad->lacc->tr;
-    if (s > 0) {
+    swg_state in = s == ns - 1 ? ad->lam : ad->lacc;
+    swg_state out = s == 0 ? ad->lam : ad->lacc;
+    io.acc_in_h = in->h;
+    io.acc_in_vn = in->vn;
+    io.acc_in_tr = in->tr;
+    io.acc_h = out->h;
+    io.acc_vn = out->vn;
+    io.acc_tr = out->tr;
+    if (s > 0 || even) {
       io.nmu_h = nmu->h;
       io.nmu_vn = nmu->vn;
       io.nmu_tr = nmu->tr;
+    }
+    if (s > 0) {
       io.lam_h = ad->lam->h;
       io.lam_vn = ad->lam->vn;
       io.lam_tr = ad->lam->tr;
       io.alpha = dt * rkb[s - 1];
       io.beta = lsrk ? 0.0 : dt * rka[s - 1];
       io.gamma = lsrk ? rka[s] : 0.0;
-      io.lsrk = lsrk;
+      io.mode = lsrk ? 1 : 0;
+    } else if (even) { // the next step's first mu (its stage ns-1 reads mus[0])
+      io.alpha = dt * rkb[ns - 1];
+      io.mode = 2;
     }
     adj_passes(ad, tp.taux[s], io, st);
   }
-  err = cudaMemcpyAsync(ad->lam->h, ad->lacc->h, n * 8,
-                        cudaMemcpyDeviceToDevice, st);
-  if (err == cudaSuccess)
-    err = cudaGetLastError();
+  cudaError_t err = cudaGetLastError();
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_adjoint: adjoint step");
 }
 
@@ -1601,6 +1642,9 @@ int bwd_begin(swg_adjoint ad, swg_state lambda, cudaStream_t st) {
   if (e != cudaSuccess)
     return cuda_fail(e, "swg_adj_backward: stream handshake");
   TRY(swg_state_copy(ad->lam, lambda, st));
+  if (ad->ns % 2 == 0) // the first step's first mu (later steps form theirs)
+    lincomb(ad->mu, ad->lam, nullptr, ad->dt * step_rkb(ad)[ad->ns - 1], 0.0,
+            (long long)words(ad->model), st);
   if (ad->aw.gc2e) {
     cudaError_t err = cudaMemsetAsync(
         ad->aw.gc2e, 0,
