@@ -383,11 +383,12 @@ int swg_batch_selftest_timeout(swg_batch batch, double limit_ms,
 
 /* ------------------------------------------ adjoint and tangent-linear ----
  * Differentiation of the RK4 or low-storage RK step (no counterpart in the
- * reference).  An
- * adjoint object is tied to a model (no forcing hook, edge_mask all ones,
- * dv >= dc/4) and owns `nsnapshots` state checkpoints for the binomial
- * checkpointing schedule, the stage tape of one step and the adjoint work
- * arrays.  Tendency level, in the style of an autograd Function's jvp/vjp:
+ * reference).  An adjoint object is tied to a model (any MPAS tables, edge
+ * mask, mesh scaling and dv < dc/4 included; not a model with a forcing
+ * hook, the linear model or the drag) and owns `nsnapshots` state
+ * checkpoints for the binomial checkpointing schedule, two step tapes and
+ * the adjoint work arrays.  Tendency level, in the style of an autograd
+ * Function's jvp/vjp:
  *   swg_tlm_tendency: dtend = J(x) dx        (exact forward-mode derivative)
  *   swg_adj_tendency: lambda = J(x)^T mu     (hand-written reverse mode)
  * Trajectory level (the adjoint's stepper, dt fixed):
@@ -395,9 +396,10 @@ int swg_batch_selftest_timeout(swg_batch batch, double limit_ms,
  *   swg_adj_forward: runs nsteps steps from state0 storing checkpoints,
  *                    writes x_N to final_out;
  *   swg_adj_backward: lambda (in: dL/dx_N) <- dL/dx_0.
- * The adjoint differentiates the terms the model had when it was created:
- * while a term is switched (swg_model_set_term_enabled) every call below
- * returns SWG_ERR_STATE. */
+ * Every call differentiates the model's terms as they are switched
+ * (swg_model_set_term_enabled) when it runs; swg_adj_backward refuses
+ * (SWG_ERR_STATE) a term set that differs from the one its forward sweep
+ * ran with. */
 int swg_adjoint_create(swg_model model, int nsnapshots, swg_adjoint *out);
 /* the same for another stepper: SWG_STEPPER_RK4 (nstages ignored) or
  * SWG_STEPPER_LSRK with nstages 5 or 1 (lsrk.cpp:16-33, 36-89) */

@@ -58,6 +58,7 @@ struct AdjView {
   int nt;
   // vertices [V][3]
   const double *z4adj, *zetaadj;
+  const double *zetaadj4; // with 1/max(dv, dc/4) (meshes where it differs)
 };
 
 struct AdjWork {
@@ -66,6 +67,9 @@ struct AdjWork {
   double *lz4, *lzeta, *lhv;            // [V][K]
   double *lQ, *lmh, *lvnp, *ld2u;       // [E][K]
   double *Qmu;                          // [E][K] Q mu_vn of the stage
+  // [E][K] adjoint of the del4 chain's first Laplacian, kept apart from the
+  // del2 one (ld2u) where 1/max(dv, dc/4) differs from 1/dv; else null
+  double *ld2u4;
   double *gc2e; // [E][K] accumulated dL/d(visc_del2 * mesh_scaling_del2), or null
 };
 
@@ -117,33 +121,42 @@ __global__ void __launch_bounds__(ATPB)
   const unsigned VK = unsigned(m.nvertices) * K, CK = unsigned(m.ncells) * K;
   if (i >= VK + CK) {
     i -= VK + CK;
-    if (i < unsigned(m.nedges) * K)
+    if (i < unsigned(m.nedges) * K && !p.off_pv)
       w.Qmu[i] = a.Q[i] * io.mvn[i];
     return;
   }
+  // the del4 term is masked per edge and level (mask * c4e): its
+  // transposes gather mask * mu
   if (i < VK) {
     if (!p.vel_del4)
       return;
     const int vx = int(i / unsigned(K)), k = int(i - unsigned(vx) * K);
     double z = 0;
-    for (int j = 0; j < 3; ++j)
-      z = fma(__ldg(v.z4adj + 3 * vx + j),
-              io.mvn[size_t(__ldg(m.ev + 3 * vx + j)) * K + k], z);
+    for (int j = 0; j < 3; ++j) {
+      const size_t ie = size_t(__ldg(m.ev + 3 * vx + j)) * K + k;
+      const double mu = m.mask ? io.mvn[ie] * m.mask[ie] : io.mvn[ie];
+      z = fma(__ldg(v.z4adj + 3 * vx + j), mu, z);
+    }
     w.lz4[i] = z;
     return;
   }
   i -= VK;
   const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
   // the SSH gradient's transpose is g times the kinetic-energy gradient's
-  // (both are -(x_1 - x_0)/dc per edge), applied where lke is read
+  // (both are -(x_1 - x_0)/dc per edge), applied where lke is read: lke
+  // serves either term
+  const bool ke_on = !p.off_ke || !p.off_ssh;
   double ke = 0, d4 = 0;
   for (int j = 0; j < MAXE; ++j) {
-    const double mu = io.mvn[size_t(__ldg(m.ec + 6 * c + j)) * K + k];
-    ke = fma(__ldg(v.keadj + 6 * c + j), mu, ke);
+    const size_t ie = size_t(__ldg(m.ec + 6 * c + j)) * K + k;
+    const double mu = io.mvn[ie];
+    if (ke_on)
+      ke = fma(__ldg(v.keadj + 6 * c + j), mu, ke);
     if (p.vel_del4)
-      d4 = fma(__ldg(v.d4adj + 6 * c + j), mu, d4);
+      d4 = fma(__ldg(v.d4adj + 6 * c + j), m.mask ? mu * m.mask[ie] : mu, d4);
   }
-  w.lke[i] = ke;
+  if (ke_on)
+    w.lke[i] = ke;
   if (p.vel_del4)
     w.ld4[i] = d4;
 }
@@ -184,12 +197,16 @@ __global__ void __launch_bounds__(ATPB)
   const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
   double wnb[MAXE], wc = 0;
   int nb[MAXE];
+  const bool adv = !p.off_tr_hadv; // tracer advection switched on
   for (int j = 0; j < MAXE; ++j) {
     const int e = __ldg(m.ec + 6 * c + j);
     nb[j] = __ldg(m.nbc + 6 * c + j);
-    const double F = a.F[size_t(e) * K + k];
-    double x = __ldg(v.ccdh_nb + 6 * c + j) * F;
-    wc = fma(__ldg(m.ccdh + 6 * c + j), F, wc);
+    double x = 0;
+    if (adv) {
+      const double F = a.F[size_t(e) * K + k];
+      x = __ldg(v.ccdh_nb + 6 * c + j) * F;
+      wc = fma(__ldg(m.ccdh + 6 * c + j), F, wc);
+    }
     if (D2) {
       const double mh = mean_h(m, a, io.h, e, k);
       x = fma(__ldg(v.kd2_nb + 6 * c + j), mh, x);
@@ -272,55 +289,72 @@ __global__ void __launch_bounds__(ATPB)
   const double F = a.F[i], u = io.vn[i];
   double lF = 0, lmh = 0;
   if (p.do_vn) {
-    // PV flux: t_e = Q_e S1_e + S2_e, S1 = sum w F_j, S2 = sum w G_j
-    double lG = 0, lFq = 0;
-    for (int t = 0; t < v.nt; ++t) {
-      const size_t is = size_t(__ldg(v.eoeT + v.nt * e + t)) * K + k;
-      const double ws = __ldg(v.woeT + v.nt * e + t);
-      lG = fma(ws, io.mvn[is], lG);
-      lFq = fma(ws, w.Qmu[is], lFq);
-    }
-    double S1;
-    if (a.S1) {
-      S1 = a.S1[i];
+    const double mu = io.mvn[i];
+    if (!p.off_pv) {
+      // PV flux: t_e = Q_e S1_e + S2_e, S1 = sum w F_j, S2 = sum w G_j
+      double lG = 0, lFq = 0;
+      for (int t = 0; t < v.nt; ++t) {
+        const size_t is = size_t(__ldg(v.eoeT + v.nt * e + t)) * K + k;
+        const double ws = __ldg(v.woeT + v.nt * e + t);
+        lG = fma(ws, io.mvn[is], lG);
+        lFq = fma(ws, w.Qmu[is], lFq);
+      }
+      double S1;
+      if (a.S1) {
+        S1 = a.S1[i];
+      } else {
+        S1 = 0;
+        for (int j = 0; j < NE; ++j)
+          S1 = fma(__ldg(m.woe + NE * e + j),
+                   a.F[size_t(__ldg(m.eoe + NE * e + j)) * K + k], S1);
+      }
+      w.lQ[i] = fma(S1, mu, F * lG);
+      lF = fma(a.Q[i], lG, lFq);
     } else {
-      S1 = 0;
-      for (int j = 0; j < NE; ++j)
-        S1 = fma(__ldg(m.woe + NE * e + j),
-                 a.F[size_t(__ldg(m.eoe + NE * e + j)) * K + k], S1);
+      w.lQ[i] = 0.0;
     }
-    const double Q = a.Q[i], mu = io.mvn[i];
-    w.lQ[i] = fma(S1, mu, F * lG);
-    lF = fma(Q, lG, lFq);
     // kinetic energy from vn^2 (the factor 2 of d(vn^2) is in cke2_e2)
-    const double lu2 = fma(__ldg(v.cke2_e2 + 2 * e), w.lke[i0],
-                           __ldg(v.cke2_e2 + 2 * e + 1) * w.lke[i1]);
-    w.lvnp[i] = u * lu2; // mean-h term added below
+    if (!p.off_ke) {
+      const double lu2 = fma(__ldg(v.cke2_e2 + 2 * e), w.lke[i0],
+                             __ldg(v.cke2_e2 + 2 * e + 1) * w.lke[i1]);
+      w.lvnp[i] = u * lu2; // mean-h term added below
+    } else {
+      w.lvnp[i] = 0.0;
+    }
     if (p.vel_del2 | p.vel_del4) {
       const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
-      double d = p.vel_del2 ? __ldg(p.c2e + e) * mu : 0.0;
+      const double mk = m.mask ? m.mask[i] : 1.0; // the dissipation's mask
+      double d = p.vel_del2 ? __ldg(p.c2e + e) * (mu * mk) : 0.0;
       if (p.vel_del2 && w.gc2e) // parameter gradient of the del2 coefficient
-        w.gc2e[i] = fma(mu, a.d2u[i], w.gc2e[i]);
+        w.gc2e[i] = fma(mu * mk, a.d2u[i], w.gc2e[i]);
+      double d4 = 0; // the del4 chain's first Laplacian
       if (p.vel_del4) {
-        d = fma(__ldg(v.cvr_e2 + 2 * e), w.lz4[size_t(v0) * K + k], d);
-        d = fma(__ldg(v.cvr_e2 + 2 * e + 1), w.lz4[size_t(v1) * K + k], d);
-        d = fma(__ldg(v.ccd_e2 + 2 * e), w.ld4[i0], d);
-        d = fma(__ldg(v.ccd_e2 + 2 * e + 1), w.ld4[i1], d);
+        d4 = __ldg(v.cvr_e2 + 2 * e) * w.lz4[size_t(v0) * K + k];
+        d4 = fma(__ldg(v.cvr_e2 + 2 * e + 1), w.lz4[size_t(v1) * K + k], d4);
+        d4 = fma(__ldg(v.ccd_e2 + 2 * e), w.ld4[i0], d4);
+        d4 = fma(__ldg(v.ccd_e2 + 2 * e + 1), w.ld4[i1], d4);
       }
-      w.ld2u[i] = d;
+      if (w.ld2u4) { // 1/max(dv, dc/4) differs: kept apart
+        w.ld2u[i] = d;
+        w.ld2u4[i] = d4;
+      } else {
+        w.ld2u[i] = d + d4;
+      }
     }
   } else {
     w.lvnp[i] = 0.0;
   }
   const double g0 = __ldg(v.ccdh_e2 + 2 * e), g1 = __ldg(v.ccdh_e2 + 2 * e + 1);
-  if (p.do_h)
+  if (p.do_h && !p.off_hadv)
     lF = fma(__ldg(v.ccdh2_e2 + 2 * e), io.mh_[i0],
              fma(__ldg(v.ccdh2_e2 + 2 * e + 1), io.mh_[i1], lF));
+  const bool adv = !p.off_tr_hadv;
   for (int l = 0; l < p.ntracers; ++l) {
     const size_t b = size_t(l) * CK;
     const double n0 = a.ntr[b + i0], n1 = a.ntr[b + i1];
     const double m0 = io.mtr[b + i0], m1 = io.mtr[b + i1];
-    lF = fma(n0 + n1, fma(g0, m0, g1 * m1), lF);
+    if (adv)
+      lF = fma(n0 + n1, fma(g0, m0, g1 * m1), lF);
     if (TRD) {
       const double dn = n1 - n0;
       if (p.tr_del2)
@@ -354,9 +388,11 @@ __global__ void __launch_bounds__(ATPB)
       return;
     const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
     double ld = 0;
-    for (int j = 0; j < MAXE; ++j)
+    for (int j = 0; j < MAXE; ++j) {
+      const size_t ie = size_t(__ldg(m.ec + 6 * c + j)) * K + k;
       ld = fma(__ldg(v.divadj + 6 * c + j),
-               w.ld2u[size_t(__ldg(m.ec + 6 * c + j)) * K + k], ld);
+               w.ld2u4 ? w.ld2u[ie] + w.ld2u4[ie] : w.ld2u[ie], ld);
+    }
     w.ldiv[i] = ld;
     return;
   }
@@ -370,6 +406,10 @@ __global__ void __launch_bounds__(ATPB)
     lz = __ldg(v.zetaadj + 3 * vx) * w.ld2u[size_t(e0) * K + k];
     lz = fma(__ldg(v.zetaadj + 3 * vx + 1), w.ld2u[size_t(e1) * K + k], lz);
     lz = fma(__ldg(v.zetaadj + 3 * vx + 2), w.ld2u[size_t(e2) * K + k], lz);
+    if (w.ld2u4) // the del4 chain's part, with 1/max(dv, dc/4)
+      for (int j = 0; j < 3; ++j)
+        lz = fma(__ldg(v.zetaadj4 + 3 * vx + j),
+                 w.ld2u4[size_t(__ldg(m.ev + 3 * vx + j)) * K + k], lz);
   }
   double r; // 1/h_vertex: the forward's value (taped, or recomputed)
   if (a.rhv) {
@@ -401,7 +441,7 @@ __global__ void __launch_bounds__(ATPB)
       lh = fma(__ldg(v.ckvh + 6 * c + j),
                w.lhv[size_t(__ldg(v.cvtx + 6 * c + j)) * K + k], lh);
   }
-  if (p.do_vn)
+  if (p.do_vn && !p.off_ssh)
     lh = fma(p.grav, w.lke[i], lh); // SSH gradient: g times the KE term
   if (p.ntracers > 0)
     lh += w.lhtr[i];
@@ -488,7 +528,8 @@ struct AdjAction {
 struct AdjGraph {
   cudaGraphExec_t exec = nullptr;
   double dt = 0;
-  long long launches = 0; // kernels per replay
+  unsigned long long version = 0; // the model's term version captured
+  long long launches = 0;         // kernels per replay
 };
 
 // One step's tape: the stage inputs, the taped step's accumulator and the
@@ -531,6 +572,7 @@ struct swg_adjoint_s {
   int nsteps = 0;
   double t0 = 0, dt = 0;
   long long plain_steps = 0, taped_steps = 0, taped_advances = 0;
+  unsigned fwd_terms = 0; // the model's term set at the last forward sweep
   int state = 0; // 0 idle, 1 forward done (the last steps taped)
   bool grad_ready = false; // a backward sweep has completed
   // backward sweep: restores, stores, plain and taped advances run on
@@ -608,6 +650,7 @@ int build_tables(swg_adjoint ad) {
       r4_nb(6 * C, 0), keadj(6 * C, 0), d4adj(6 * C, 0),
       divadj(6 * C, 0), ckvh(6 * C, 0);
   std::vector<int> cvtx(6 * C, 0);
+  std::vector<double> zetaadj4(3 * V);
   std::vector<double> ccd_e2(2 * E), ccdh_e2(2 * E), cke_e2(2 * E),
       ckq_e2(2 * E), kd2_e2(2 * E), cvr_e2(2 * E), z4adj(3 * V), zetaadj(3 * V),
       ccdh2_e2(2 * E), cke2_e2(2 * E), hm_c(6 * C, 0);
@@ -685,6 +728,7 @@ int build_tables(swg_adjoint ad) {
       const double sg = side == 0 ? -1.0 : 1.0;
       z4adj[3 * v + j] = -(sg * (-(P.visc_del4 * me->scale4_h[e])) * me->inv_dv_h[e]);
       zetaadj[3 * v + j] = -(sg * me->inv_dv_h[e]);
+      zetaadj4[3 * v + j] = -(sg * me->inv_dv4_h[e]);
     }
   // transposed edges-on-edge
   const int NE = me->view.ne;
@@ -726,7 +770,8 @@ int build_tables(swg_adjoint ad) {
       (rc = up(A, eoeT, &a.eoeT)) || (rc = up(A, woeT, &a.woeT)) ||
       (rc = up(A, z4adj, &a.z4adj)) || (rc = up(A, zetaadj, &a.zetaadj)) ||
       (rc = up(A, hm_c, &a.hm_c)) || (rc = up(A, ccdh2_e2, &a.ccdh2_e2)) ||
-      (rc = up(A, cke2_e2, &a.cke2_e2)))
+      (rc = up(A, cke2_e2, &a.cke2_e2)) ||
+      (me->view.dv4_differs && (rc = up(A, zetaadj4, &a.zetaadj4))))
     return rc;
   a.nt = nt;
   return SWG_OK;
@@ -755,6 +800,8 @@ template <class T> int alloc_aux_like(swg_adjoint ad, AuxViewT<T> &d) {
     if (x.on)
       TRY(zal(A, x.n, x.p));
   d.d2u4 = d.d2u;
+  if (a.d2u4 && a.d2u4 != a.d2u) // 1/max(dv, dc/4) differs from 1/dv
+    TRY(zal(A, E * K, &d.d2u4));
   return SWG_OK;
 }
 
@@ -1219,7 +1266,7 @@ void count_actions(const std::vector<AdjAction> &acts, long long *plain,
 // it on st; when capture fails the launches run directly on st.
 template <class Fn>
 int replay(swg_adjoint ad, AdjGraph &g, cudaStream_t st, Fn record) {
-  if (!g.exec || g.dt != ad->dt) {
+  if (!g.exec || g.dt != ad->dt || g.version != ad->model->version) {
     if (g.exec) {
       cudaGraphExecDestroy(g.exec);
       g.exec = nullptr;
@@ -1251,6 +1298,7 @@ int replay(swg_adjoint ad, AdjGraph &g, cudaStream_t st, Fn record) {
       return cuda_fail(err, "swg_adjoint: graph instantiate");
     }
     g.dt = ad->dt;
+    g.version = ad->model->version;
   }
   cudaError_t err = cudaGraphLaunch(g.exec, st);
   if (err != cudaSuccess)
@@ -1321,24 +1369,28 @@ int run_action(swg_adjoint ad, const AdjAction &a, cudaStream_t st, bool two) {
   return rc;
 }
 
+// The model's tendency-term switches as a bit set: a backward sweep must
+// see the set its forward sweep ran with (its re-advances and tapes would
+// differ otherwise).
+unsigned term_set(swg_model md) {
+  const ModelView &p = md->view;
+  const int f[] = {p.off_hadv, p.off_pv, p.off_ke, p.off_ssh, p.off_tr_hadv,
+                   p.vel_del2, p.vel_del4, p.tr_del2, p.tr_del4};
+  unsigned s = 0;
+  for (int i = 0; i < 9; ++i)
+    s |= unsigned(f[i] != 0) << i;
+  return s;
+}
+
 int check_model(swg_model md) {
   if (!md)
     return fail(SWG_ERR_ARG, "swg_adjoint: NULL model");
   if (md->forcing)
     return fail(SWG_ERR_ARG, "swg_adjoint: models with an additional_tendency "
                              "hook are not differentiated");
-  if (md->mesh->view.mask)
-    return fail(SWG_ERR_ARG, "swg_adjoint: edge_mask other than ones is not "
-                             "supported");
   if (md->view.linear || md->view.drag)
     return fail(SWG_ERR_ARG, "swg_adjoint: the linear model and the bottom "
                              "drag are not differentiated");
-  if (md->terms_switched)
-    return fail(SWG_ERR_ARG, "swg_adjoint: models with switched tendency "
-                             "terms are not differentiated");
-  if (md->mesh->view.dv4_differs)
-    return fail(SWG_ERR_ARG, "swg_adjoint: meshes with dv < dc/4 are not "
-                             "supported");
   return SWG_OK;
 }
 
@@ -1384,7 +1436,9 @@ extern "C" int swg_adjoint_create_stepper(swg_model md, int nsnapshots,
        (rc = zal(A, E * K, &w.lQ)) || (rc = zal(A, E * K, &w.lmh)) ||
        (rc = zal(A, E * K, &w.lvnp)) || (rc = zal(A, E * K, &w.ld2u)) ||
        (rc = zal(A, E * K, &w.Qmu)) ||
-       (md->view.vel_del2 && (rc = zal(A, E * K, &w.gc2e)))))
+       (md->view.vel_del2 && (rc = zal(A, E * K, &w.gc2e))) ||
+       (md->view.vel_del4 && md->mesh->view.dv4_differs &&
+        (rc = zal(A, E * K, &w.ld2u4)))))
     ;
   swg_state *st[] = {&ad->cur, &ad->lam, &ad->lacc, &ad->mu, &ad->mu2};
   for (auto *p : st)
@@ -1482,10 +1536,6 @@ extern "C" int swg_adj_tendency(swg_adjoint ad, swg_state x, swg_state mu,
   if (!ad || !same_layout(ad, x) || !same_layout(ad, mu) ||
       !same_layout(ad, lambda_out))
     return fail(SWG_ERR_ARG, "swg_adj_tendency: bad argument");
-  if (ad->model->terms_switched)
-    return fail(SWG_ERR_STATE, "swg_adj_tendency: a tendency term of the "
-                               "model was switched after the adjoint was "
-                               "created");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   adj_tendency(ad, x->h, x->vn, x->tr, mu, lambda_out, st);
   cudaError_t err = cudaGetLastError();
@@ -1497,10 +1547,6 @@ extern "C" int swg_tlm_tendency(swg_adjoint ad, swg_state x, swg_state dx,
   if (!ad || !same_layout(ad, x) || !same_layout(ad, dx) ||
       !same_layout(ad, dtend_out))
     return fail(SWG_ERR_ARG, "swg_tlm_tendency: bad argument");
-  if (ad->model->terms_switched)
-    return fail(SWG_ERR_STATE, "swg_tlm_tendency: a tendency term of the "
-                               "model was switched after the adjoint was "
-                               "created");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   swg_model md = ad->model;
   const long long n = (long long)words(md);
@@ -1530,9 +1576,6 @@ extern "C" int swg_tlm_apply(swg_adjoint ad, swg_state x0, swg_state dx,
   (void)t0;
   if (!ad || !same_layout(ad, x0) || !same_layout(ad, dx) || nsteps < 0)
     return fail(SWG_ERR_ARG, "swg_tlm_apply: bad argument");
-  if (ad->model->terms_switched)
-    return fail(SWG_ERR_STATE, "swg_tlm_apply: a tendency term of the model "
-                               "was switched after the adjoint was created");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   swg_model md = ad->model;
   const ModelView &pv = md->view;
@@ -1598,9 +1641,6 @@ int fwd_begin(swg_adjoint ad, swg_state state0, double t0, double dt,
   if (nsteps > kMaxAdjointSteps)
     return fail(SWG_ERR_ARG, "swg_adj_forward: more steps than the schedule "
                              "planner takes (10000); split the trajectory");
-  if (ad->model->terms_switched)
-    return fail(SWG_ERR_STATE, "swg_adj_forward: a tendency term of the model "
-                               "was switched after the adjoint was created");
   Planner pl(nsteps, ad->nsnap - 1, ad->ns);
   std::vector<AdjAction> acts = pl.schedule();
   long long plain, tadv;
@@ -1613,6 +1653,7 @@ int fwd_begin(swg_adjoint ad, swg_state state0, double t0, double dt,
   ad->t0 = t0;
   ad->dt = dt;
   ad->nsteps = nsteps;
+  ad->fwd_terms = term_set(ad->model);
   ad->plain_steps = ad->taped_steps = ad->taped_advances = 0;
   ad->actions.swap(acts);
   ad->pos = 0;
@@ -1694,7 +1735,7 @@ extern "C" int swg_adj_backward(swg_adjoint ad, swg_state lambda,
     return fail(SWG_ERR_ARG, "swg_adj_backward: bad argument");
   if (ad->state != 1)
     return fail(SWG_ERR_STATE, "swg_adj_backward: call swg_adj_forward first");
-  if (ad->model->terms_switched) // the re-advances would differ from the tape
+  if (term_set(ad->model) != ad->fwd_terms) // re-advances would differ
     return fail(SWG_ERR_STATE, "swg_adj_backward: a tendency term of the "
                                "model was switched after swg_adj_forward");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -1748,7 +1789,7 @@ extern "C" int swg_adj_batch_backward(int n, const swg_adjoint *adjs,
   for (int m = 0; m < n; ++m)
     if (!adjs[m] || !same_layout(adjs[m], lambdas[m]) || adjs[m]->state != 1)
       return fail(SWG_ERR_ARG, "swg_adj_batch_backward: member not ready");
-    else if (adjs[m]->model->terms_switched)
+    else if (term_set(adjs[m]->model) != adjs[m]->fwd_terms)
       return fail(SWG_ERR_STATE, "swg_adj_batch_backward: a tendency term of "
                                  "a member's model was switched after the "
                                  "forward sweep");

@@ -252,6 +252,7 @@ extern "C" int swg_mesh_create(const swg_mesh_desc *d, swg_mesh *out) {
   m->cke_h = cke;
   m->ccdh_h = ccdh;
   m->inv_dv_h = inv_dv;
+  m->inv_dv4_h = inv_dv4;
   m->woe_h = woe;
   bool mask_ones = true;
   if (d->edge_mask)

@@ -229,6 +229,7 @@ struct swg_mesh_s {
   // host copies of the derived tables (the adjoint builds transposes)
   std::vector<int> ev_h, cv_h, nbc_h, ce_h, ve_h, eoe_h;
   std::vector<double> cvr_h, kvh_h, ccd_h, cke_h, ccdh_h, inv_dv_h, woe_h;
+  std::vector<double> inv_dv4_h; // 1 / max(dv, dc / 4)
 };
 
 struct swg_state_s {

@@ -148,16 +148,24 @@ def test_general_mesh_diagnostics_with_max_levels():
         np.sum(om.area_cell[:, None] * h))) > 1e-6 * abs(omd.mass(h))
 
 
+@pytest.mark.parametrize("full", [False, True])
 @pytest.mark.parametrize("stepper,nstages", [("rk4", 4), ("lsrk", 5)])
-def test_general_mesh_adjoint_dot_products(stepper, nstages):
+def test_general_mesh_adjoint_dot_products(stepper, nstages, full):
     """The adjoint on perturbed tables (random geometry, 10 nonzero TRiSK
-    weights, shortened edges-on-edge lists, random del2/del4 scaling):
-    tendency and 5-step trajectory dot products against the tangent-linear
-    model <= 1e-12; tables that no consistent mesh has are rejected."""
+    weights, shortened edges-on-edge lists, random del2/del4 scaling; with
+    `full` also a 0/1 edge mask on 20 % of the edge levels and dv < dc/4 on
+    5 % of the edges, where the del4 chain's first Laplacian uses
+    1/max(dv, dc/4)): tendency and 5-step trajectory dot products against
+    the tangent-linear model <= 1e-12; tables that no consistent mesh has
+    are rejected."""
     cut = general_mesh(10, 8, 4, 7373, adjoint_ready=True, cut_cells=True)
     with pytest.raises(og.SwgError, match="neighbour"):
         og.Adjoint(models(*cut, 2)[2], 2)
-    om, gm = general_mesh(10, 8, 4, 7373, adjoint_ready=True)
+    om, gm = general_mesh(10, 8, 4, 7373, adjoint_ready=not full,
+                          cut_cells=False)
+    if full:
+        assert not np.all(om.tables["edge_mask"] == 1.0)
+        assert np.any(om.tables["dv_edge"] < 0.25 * om.tables["dc_edge"])
     T = 2
     _, gp, model = models(om, gm, T)
     adj = og.Adjoint(model, 2, stepper, nstages)
