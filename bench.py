@@ -559,6 +559,8 @@ def run_ours(args, wl):
                    "batched_forward_ms": a["batched_forward_ms"],
                    "adjoint_forward_sweep_ms": a["adjoint_forward_sweep_ms"],
                    "adjoint_backward_sweep_ms": a["adjoint_backward_sweep_ms"],
+                   "groups": a["groups"], "gpu_launches": a["gpu_launches"],
+                   "stream_interleaved_ms": a["stream_interleaved_ms"],
                    "batched_over_sequential_speedup":
                        a["batched_over_sequential_speedup"]}
     cpu = None
@@ -669,9 +671,11 @@ def adjoint_ensemble_line():
     """Batched adjoints: 32 members (nx from {32, 64, 96, 128}, 16-64 levels,
     2 tracers, RK4, 300 steps, per-cell log-normal viscosity), gradient of
     the region loss w.r.t. the initial state and the viscosity field, each
-    member with its own checkpoint budget and stream.  Timed against the
-    batched plain forward of the same members and against the members'
-    adjoints run one after another."""
+    member with its own checkpoint budget, run as one batched ensemble
+    (og.AdjointEnsemble: one launch per pass over the members of each
+    lockstep group).  Timed against the batched plain forward of the same
+    members; the stream-interleaved form (one stream per member) and the
+    members' adjoints run one after another are reported beside it."""
     import torch
     import omega_playground_gb300 as og
     from omega_playground_gb300.workloads import (adjoint_ensemble,
@@ -730,10 +734,19 @@ def adjoint_ensemble_line():
         a.upload(*m["x0"])
         X0.append(a)
         XN.append(og.ShallowWaterState(m["mesh"], m["params"]))
-    streams = [torch.cuda.Stream() for _ in mem]
-    sh = [s.cuda_stream for s in streams]
-    f_ms = timed(lambda: og.adjoint_batch_forward(adjs, X0, 0.0, dt, nsteps,
-                                                  XN, sh))
+    # the batched ensemble: every schedule action one launch per pass over
+    # the members of a lockstep group (one group per snapshot budget)
+    ens = og.AdjointEnsemble(adjs)
+    ens.forward(X0, 0.0, dt, 2, XN)                    # warm-up, tables
+    Gw = []
+    for m in mem:
+        G = og.ShallowWaterState(m["mesh"], m["params"])
+        G.fill(0.0)
+        Gw.append(G)
+    ens.backward(Gw)
+    torch.cuda.synchronize()
+    l0 = og.kernel_launches()
+    f_ms = timed(lambda: ens.forward(X0, 0.0, dt, nsteps, XN))
     Gs, loss = [], 0.0
     for m, xn in zip(mem, XN):
         L, g = loss_and_grad(*xn.download(), m["region"])
@@ -741,8 +754,20 @@ def adjoint_ensemble_line():
         G = og.ShallowWaterState(m["mesh"], m["params"])
         G.upload(*g)
         Gs.append(G)
-    b_ms = timed(lambda: og.adjoint_batch_backward(adjs, Gs, sh))
+    grads = [g.download() for g in Gs]
+    b_ms = timed(lambda: ens.backward(Gs))
+    launches = og.kernel_launches() - l0
     gvisc = [a.grad_visc()[1] for a in adjs]
+    # the same adjoints, one stream per member (stream-interleaved actions)
+    for G, g in zip(Gs, grads):
+        G.upload(*g)
+    streams = [torch.cuda.Stream() for _ in mem]
+    sh = [s.cuda_stream for s in streams]
+    l1 = og.kernel_launches()
+    s_ms = timed(lambda: og.adjoint_batch_forward(adjs, X0, 0.0, dt, nsteps,
+                                                  XN, sh))
+    s_ms += timed(lambda: og.adjoint_batch_backward(adjs, Gs, sh))
+    stream_launches = og.kernel_launches() - l1
     # the same adjoints one member at a time (default stream)
     seq_ms = 0.0
     for m in mem:
@@ -768,6 +793,9 @@ def adjoint_ensemble_line():
             "batched_forward_ms": fwd_ms, "batch_config": best_cfg,
             "adjoint_forward_sweep_ms": f_ms,
             "adjoint_backward_sweep_ms": b_ms,
+            "groups": ens.groups()[0], "gpu_launches": launches,
+            "stream_interleaved_ms": s_ms,
+            "stream_interleaved_launches": stream_launches,
             "sequential_member_adjoints_ms": seq_ms,
             "batched_over_sequential_speedup": seq_ms / (f_ms + b_ms),
             "forward_updates_per_s": units / (fwd_ms / 1e3), "loss": loss,

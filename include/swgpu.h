@@ -56,6 +56,7 @@ typedef struct swg_stepper_s *swg_stepper;
 typedef struct swg_batch_s *swg_batch;
 typedef struct swg_adjoint_s *swg_adjoint;
 typedef struct swg_host_stepper_s *swg_host_stepper;
+typedef struct swg_adj_ensemble_s *swg_adj_ensemble;
 
 /* Message of the calling thread's last failed call ("" if none). */
 const char *swg_last_error(void);
@@ -429,6 +430,31 @@ int swg_adj_batch_forward(int n, const swg_adjoint *adjs,
                           void *const *streams);
 int swg_adj_batch_backward(int n, const swg_adjoint *adjs,
                            const swg_state *lambdas, void *const *streams);
+/* Batched adjoint ensemble (no counterpart in the reference): the members'
+ * adjoints (distinct adjoints and models; uneven sizes, each with its own
+ * snapshot budget) advanced together, every action of the checkpoint
+ * schedule one batched launch per pass over the members.  Members with the
+ * same schedule (step count, snapshot budget, stepper) and the same kernel
+ * switches (edges-on-edge width, tracer diffusion) form a group that runs
+ * in lockstep: plain advances as a batch of the members' states, taped
+ * steps as batched tendency passes into the members' tapes, and the adjoint
+ * of a step as batched adjoint passes.  Groups run on streams of their own;
+ * `stream` orders the ensemble after earlier work on it and later work
+ * after it.  Results equal each member's swg_adj_forward / swg_adj_backward
+ * bit for bit, and swg_adj_info / swg_adj_grad_visc of a member report its
+ * part.  The ensemble keeps device tables of its members: create it once
+ * and reuse it. */
+int swg_adj_ensemble_create(int n, const swg_adjoint *adjs,
+                            swg_adj_ensemble *out);
+int swg_adj_ensemble_destroy(swg_adj_ensemble ens);
+int swg_adj_ensemble_forward(swg_adj_ensemble ens, const swg_state *states0,
+                             double t0, double dt, int nsteps,
+                             const swg_state *finals, void *stream);
+int swg_adj_ensemble_backward(swg_adj_ensemble ens, const swg_state *lambdas,
+                              void *stream);
+/* number of groups, and (if group_of is not NULL) each member's group */
+int swg_adj_ensemble_groups(swg_adj_ensemble ens, int *ngroups,
+                            int *group_of);
 /* plain (re-)advanced and taped steps of the last forward/backward pair;
  * every step is taped once, either from a restored or re-advanced state or
  * as a taped advance (a step whose tape is kept while its result continues

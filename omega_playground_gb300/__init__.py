@@ -6,7 +6,7 @@ updates on the doubly periodic planar hexagonal MPAS mesh, behind the C ABI
 in include/swgpu.h.  This package is the Python mirror of the reference's
 C++ classes (see shallow_water.py); the C++ mirror is cxx/omega_gpu.hpp.
 """
-from .shallow_water import (AddMode, Adjoint, Batch, LSRKStepper,  # noqa: F401
+from .shallow_water import (AddMode, Adjoint, AdjointEnsemble, Batch, LSRKStepper,  # noqa: F401
                             HostStepper, pinned_empty,
                             MPASMesh, adjoint_batch_backward,
                             adjoint_batch_forward, adjoint_plan,
@@ -22,7 +22,7 @@ from .shallow_water import (AddMode, Adjoint, Batch, LSRKStepper,  # noqa: F401
 from ._capi import SwgError, exported_symbols  # noqa: F401
 from . import workloads  # noqa: F401
 
-__all__ = ["AddMode", "Adjoint", "Batch", "adjoint_plan", "checkpoint_cost", "HostStepper",
+__all__ = ["AddMode", "Adjoint", "AdjointEnsemble", "Batch", "adjoint_plan", "checkpoint_cost", "HostStepper",
            "pinned_empty",
            "LinearShallowWaterModel", "LinearShallowWaterParams",
            "adjoint_batch_forward", "adjoint_batch_backward", "LSRKStepper", "MPASMesh", "PlanarHexagonalMesh",

@@ -183,6 +183,15 @@ _SIGS = {
                                         C.POINTER(_vp)]),
     "swg_adj_batch_backward": (C.c_int, [C.c_int, C.POINTER(_vp),
                                          C.POINTER(_vp), C.POINTER(_vp)]),
+    "swg_adj_ensemble_create": (C.c_int, [C.c_int, C.POINTER(_vp),
+                                          C.POINTER(_vp)]),
+    "swg_adj_ensemble_destroy": (C.c_int, [_vp]),
+    "swg_adj_ensemble_forward": (C.c_int, [_vp, C.POINTER(_vp), C.c_double,
+                                           C.c_double, C.c_int,
+                                           C.POINTER(_vp), _vp]),
+    "swg_adj_ensemble_backward": (C.c_int, [_vp, C.POINTER(_vp), _vp]),
+    "swg_adj_ensemble_groups": (C.c_int, [_vp, C.POINTER(C.c_int),
+                                          C.POINTER(C.c_int)]),
     "swg_diag_mass": (C.c_int, [_vp, _vp, _dp, _vp]),
     "swg_diag_energy": (C.c_int, [_vp, _vp, _dp, _vp]),
     "swg_diag_circulation": (C.c_int, [_vp, _vp, _dp, _vp]),

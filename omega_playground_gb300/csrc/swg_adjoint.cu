@@ -31,7 +31,7 @@
 // steps; the backward sweep restores, re-advances and reverses each step
 // once, in reverse order, taping the last step of a re-advance on the way
 // when the planner finds that cheaper (see Planner).
-#include "swg_device.cuh"
+#include "swg_adjoint.cuh"
 
 #include <algorithm>
 #include <cstring>
@@ -40,435 +40,45 @@
 namespace swg {
 namespace {
 
-constexpr int ATPB = 256;
-
-struct AdjView {
-  // cells [C][6]
-  const double *ccdh_nb, *ckq_nb, *kd2_nb, *r4_nb; // neighbour's coefficient
-  const double *keadj, *d4adj, *divadj;    // transposed edge terms
-  const int *cvtx;                                 // vertices of the cell
-  const double *ckvh;                              // their kite weight for c
-  const double *hm_c;                              // 0.5 on edges, 0 on padding
-  // edges [E][2]: coefficients of cells (c0, c1) / vertices (v0, v1) for e
-  const double *ccd_e2, *ccdh_e2, *cke_e2, *ckq_e2, *kd2_e2, *cvr_e2;
-  const double *ccdh2_e2, *cke2_e2;                // 2 ccdh_e2, 2 cke_e2
-  // transposed edges-on-edge [E][nt] with weights / 4
-  const int *eoeT;
-  const double *woeT;
-  int nt;
-  // vertices [V][3]
-  const double *z4adj, *zetaadj;
-  const double *zetaadj4; // with 1/max(dv, dc/4) (meshes where it differs)
-};
-
-struct AdjWork {
-  double *lL, *ln;                      // [T][C][K]
-  double *lke, *ld4, *lhtr, *ldiv; // [C][K]
-  double *lz4, *lzeta, *lhv;            // [V][K]
-  double *lQ, *lmh, *lvnp, *ld2u;       // [E][K]
-  double *Qmu;                          // [E][K] Q mu_vn of the stage
-  // [E][K] adjoint of the del4 chain's first Laplacian, kept apart from the
-  // del2 one (ld2u) where 1/max(dv, dc/4) differs from 1/dv; else null
-  double *ld2u4;
-  double *gc2e; // [E][K] accumulated dL/d(visc_del2 * mesh_scaling_del2), or null
-};
-
-struct AdjIO {
-  const double *h, *vn, *tr;    // state X
-  const double *mh_, *mvn, *mtr; // mu (adjoint of the tendency)
-  double *lh, *lvn, *ltr;        // lambda = J^T mu (written unless null)
-  // fused stage bookkeeping (each may be null): acc = acc_in + lambda, and
-  // the next stage's mu (mode): 0 RK4  mu_next = alpha * lam + beta * lambda;
-  //                             1 LSRK mu_next = alpha * acc + gamma * mu;
-  //                             2 next step: mu_next = alpha * acc
-  // (acc after the update).  acc_in is acc itself except where a step's
-  // first stage reads lam and its last stage writes lam, which saves the
-  // copies between the two.
-  const double *acc_in_h, *acc_in_vn, *acc_in_tr;
-  double *acc_h, *acc_vn, *acc_tr;
-  double *nmu_h, *nmu_vn, *nmu_tr;
-  const double *lam_h, *lam_vn, *lam_tr;
-  double alpha, beta, gamma;
-  int mode;
-};
-
-__device__ __forceinline__ void emit(const AdjIO &io, double *out,
-                                     const double *acc_in, double *acc,
-                                     double *nmu, const double *lam,
-                                     const double *mu, size_t i, double x) {
-  if (out)
-    out[i] = x;
-  double a = 0;
-  if (acc) {
-    a = acc_in[i] + x;
-    acc[i] = a;
-  }
-  if (nmu)
-    nmu[i] = io.mode == 2   ? io.alpha * a
-             : io.mode == 1 ? fma(io.alpha, a, io.gamma * mu[i])
-                            : fma(io.alpha, lam[i], io.beta * x);
-}
-
-// --- pass 1: transposed edge stencils of the velocity tendency (cells and
-// vertices), and Q mu_vn per edge for the transposed PV flux; the first V*K
-// threads take vertices, the next C*K cells, the last E*K edges (the grid
-// starts at `base`: V*K when the vertex part, velocity del4, is off).
+// Single-instance launches of the passes (swg_adjoint.cuh): one thread per
+// element of the pass's domain, starting at `base`.
 __global__ void __launch_bounds__(ATPB)
     ka_vel(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
            AdjIO io, unsigned base) {
-  const int K = m.nlayers;
-  unsigned i = base + blockIdx.x * ATPB + threadIdx.x;
-  const unsigned VK = unsigned(m.nvertices) * K, CK = unsigned(m.ncells) * K;
-  if (i >= VK + CK) {
-    i -= VK + CK;
-    if (i < unsigned(m.nedges) * K && !p.off_pv)
-      w.Qmu[i] = a.Q[i] * io.mvn[i];
-    return;
-  }
-  // the del4 term is masked per edge and level (mask * c4e): its
-  // transposes gather mask * mu
-  if (i < VK) {
-    if (!p.vel_del4)
-      return;
-    const int vx = int(i / unsigned(K)), k = int(i - unsigned(vx) * K);
-    double z = 0;
-    for (int j = 0; j < 3; ++j) {
-      const size_t ie = size_t(__ldg(m.ev + 3 * vx + j)) * K + k;
-      const double mu = m.mask ? io.mvn[ie] * m.mask[ie] : io.mvn[ie];
-      z = fma(__ldg(v.z4adj + 3 * vx + j), mu, z);
-    }
-    w.lz4[i] = z;
-    return;
-  }
-  i -= VK;
-  const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
-  // the SSH gradient's transpose is g times the kinetic-energy gradient's
-  // (both are -(x_1 - x_0)/dc per edge), applied where lke is read: lke
-  // serves either term
-  const bool ke_on = !p.off_ke || !p.off_ssh;
-  double ke = 0, d4 = 0;
-  for (int j = 0; j < MAXE; ++j) {
-    const size_t ie = size_t(__ldg(m.ec + 6 * c + j)) * K + k;
-    const double mu = io.mvn[ie];
-    if (ke_on)
-      ke = fma(__ldg(v.keadj + 6 * c + j), mu, ke);
-    if (p.vel_del4)
-      d4 = fma(__ldg(v.d4adj + 6 * c + j), m.mask ? mu * m.mask[ie] : mu, d4);
-  }
-  if (ke_on)
-    w.lke[i] = ke;
-  if (p.vel_del4)
-    w.ld4[i] = d4;
+  pa_vel(m, p, a, v, w, io, base + blockIdx.x * ATPB + threadIdx.x);
 }
-
-// mean thickness of edge e (the forward's value: taped, or recomputed)
-__device__ __forceinline__ double mean_h(const MeshView &m, const AuxView &a,
-                                         const double *h, int e, int k) {
-  const int K = m.nlayers;
-  if (a.mh)
-    return a.mh[size_t(e) * K + k];
-  return 0.5 * (h[size_t(__ldg(m.ce + 2 * e)) * K + k] +
-                h[size_t(__ldg(m.ce + 2 * e + 1)) * K + k]);
-}
-
-// the forward's Newton reciprocal of x
-__device__ __forceinline__ double fwd_rcp(double x) {
-  double r;
-  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
-  double e = fma(-x, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-x, r, 1.0);
-  return fma(r, e, r);
-}
-
-// --- pass 2: tracer tendency transposed to the normalised tracers (partial)
-// and to the tracer Laplacian.  D2, D4: tracer del2 / del4 on, as
-// compile-time switches (with runtime flags the diffusion arrays stayed in
-// registers and lowered the occupancy of the diffusion-free case).
 template <bool D2, bool D4>
 __global__ void __launch_bounds__(ATPB)
     ka_tr1(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
            AdjIO io) {
-  const int K = m.nlayers;
-  const unsigned i = blockIdx.x * ATPB + threadIdx.x;
-  const unsigned CK = unsigned(m.ncells) * K;
-  if (i >= CK)
-    return;
-  const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
-  double wnb[MAXE], wc = 0;
-  int nb[MAXE];
-  const bool adv = !p.off_tr_hadv; // tracer advection switched on
-  for (int j = 0; j < MAXE; ++j) {
-    const int e = __ldg(m.ec + 6 * c + j);
-    nb[j] = __ldg(m.nbc + 6 * c + j);
-    double x = 0;
-    if (adv) {
-      const double F = a.F[size_t(e) * K + k];
-      x = __ldg(v.ccdh_nb + 6 * c + j) * F;
-      wc = fma(__ldg(m.ccdh + 6 * c + j), F, wc);
-    }
-    if (D2) {
-      const double mh = mean_h(m, a, io.h, e, k);
-      x = fma(__ldg(v.kd2_nb + 6 * c + j), mh, x);
-      wc = fma(-__ldg(p.kd2 + 6 * c + j), mh, wc);
-    }
-    wnb[j] = x;
-  }
-  for (int l = 0; l < p.ntracers; ++l) {
-    const double *mu = io.mtr + size_t(l) * CK;
-    double acc = wc * mu[i];
-    for (int j = 0; j < MAXE; ++j)
-      acc = fma(wnb[j], mu[size_t(nb[j]) * K + k], acc);
-    w.ln[size_t(l) * CK + i] = acc;
-    if (D4) {
-      double L = -__ldg(p.r4sum + c) * mu[i];
-      for (int j = 0; j < MAXE; ++j)
-        L = fma(__ldg(v.r4_nb + 6 * c + j), mu[size_t(nb[j]) * K + k], L);
-      w.lL[size_t(l) * CK + i] = L;
-    }
-  }
+  pa_tr1<D2, D4>(m, p, a, v, w, io, blockIdx.x * ATPB + threadIdx.x);
 }
-
-// --- pass 3: through the tracer Laplacian and n = tr / h to the tracers;
-// the h part of n = tr / h is kept for pass 6.  D4: tracer del4 on.
 template <bool D4>
 __global__ void __launch_bounds__(ATPB)
     ka_tr2(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
            AdjIO io) {
-  const int K = m.nlayers;
-  const unsigned i = blockIdx.x * ATPB + threadIdx.x;
-  const unsigned CK = unsigned(m.ncells) * K;
-  if (i >= CK)
-    return;
-  const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
-  double mnb[MAXE], M = 0;
-  int nb[MAXE];
-  if (D4)
-    for (int j = 0; j < MAXE; ++j) {
-      const int e = __ldg(m.ec + 6 * c + j);
-      const double mh = mean_h(m, a, io.h, e, k);
-      nb[j] = __ldg(m.nbc + 6 * c + j);
-      mnb[j] = __ldg(v.ckq_nb + 6 * c + j) * mh;
-      M = fma(__ldg(m.ckq + 6 * c + j), mh, M);
-    }
-  // 1/h: the forward's own reciprocal (taped, or recomputed)
-  const double r = a.rh ? a.rh[i] : fwd_rcp(io.h[i]);
-  double hsum = 0;
-  for (int l = 0; l < p.ntracers; ++l) {
-    const size_t t = size_t(l) * CK + i;
-    double ln = w.ln[t];
-    if (D4) {
-      const double *lL = w.lL + size_t(l) * CK;
-      ln = fma(-M, lL[i], ln);
-      for (int j = 0; j < MAXE; ++j)
-        ln = fma(mnb[j], lL[size_t(nb[j]) * K + k], ln);
-    }
-    emit(io, io.ltr, io.acc_in_tr, io.acc_tr, io.nmu_tr, io.lam_tr, io.mtr, t,
-         ln * r);
-    hsum = fma(ln, a.ntr[t], hsum);
-  }
-  w.lhtr[i] = -(r * hsum);
+  pa_tr2<D4>(m, p, a, v, w, io, blockIdx.x * ATPB + threadIdx.x);
 }
-
-// --- pass 4: edges: PV flux (transposed edges-on-edge), thickness flux,
-// mean thickness, kinetic energy, edge Laplacian.  TRD: tracer diffusion
-// on (a compile-time switch: with a runtime flag the compiler evaluated the
-// diffusion products speculatively, 9 wasted FP64 instructions per edge).
 template <int NE, bool TRD>
 __global__ void __launch_bounds__(ATPB)
     ka_edge(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
             AdjIO io) {
-  const int K = m.nlayers;
-  const unsigned i = blockIdx.x * ATPB + threadIdx.x;
-  if (i >= unsigned(m.nedges) * K)
-    return;
-  const unsigned CK = unsigned(m.ncells) * K;
-  const int e = int(i / unsigned(K)), k = int(i - unsigned(e) * K);
-  const int c0 = __ldg(m.ce + 2 * e), c1 = __ldg(m.ce + 2 * e + 1);
-  const size_t i0 = size_t(c0) * K + k, i1 = size_t(c1) * K + k;
-  const double F = a.F[i], u = io.vn[i];
-  double lF = 0, lmh = 0;
-  if (p.do_vn) {
-    const double mu = io.mvn[i];
-    if (!p.off_pv) {
-      // PV flux: t_e = Q_e S1_e + S2_e, S1 = sum w F_j, S2 = sum w G_j
-      double lG = 0, lFq = 0;
-      for (int t = 0; t < v.nt; ++t) {
-        const size_t is = size_t(__ldg(v.eoeT + v.nt * e + t)) * K + k;
-        const double ws = __ldg(v.woeT + v.nt * e + t);
-        lG = fma(ws, io.mvn[is], lG);
-        lFq = fma(ws, w.Qmu[is], lFq);
-      }
-      double S1;
-      if (a.S1) {
-        S1 = a.S1[i];
-      } else {
-        S1 = 0;
-        for (int j = 0; j < NE; ++j)
-          S1 = fma(__ldg(m.woe + NE * e + j),
-                   a.F[size_t(__ldg(m.eoe + NE * e + j)) * K + k], S1);
-      }
-      w.lQ[i] = fma(S1, mu, F * lG);
-      lF = fma(a.Q[i], lG, lFq);
-    } else {
-      w.lQ[i] = 0.0;
-    }
-    // kinetic energy from vn^2 (the factor 2 of d(vn^2) is in cke2_e2)
-    if (!p.off_ke) {
-      const double lu2 = fma(__ldg(v.cke2_e2 + 2 * e), w.lke[i0],
-                             __ldg(v.cke2_e2 + 2 * e + 1) * w.lke[i1]);
-      w.lvnp[i] = u * lu2; // mean-h term added below
-    } else {
-      w.lvnp[i] = 0.0;
-    }
-    if (p.vel_del2 | p.vel_del4) {
-      const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
-      const double mk = m.mask ? m.mask[i] : 1.0; // the dissipation's mask
-      double d = p.vel_del2 ? __ldg(p.c2e + e) * (mu * mk) : 0.0;
-      if (p.vel_del2 && w.gc2e) // parameter gradient of the del2 coefficient
-        w.gc2e[i] = fma(mu * mk, a.d2u[i], w.gc2e[i]);
-      double d4 = 0; // the del4 chain's first Laplacian
-      if (p.vel_del4) {
-        d4 = __ldg(v.cvr_e2 + 2 * e) * w.lz4[size_t(v0) * K + k];
-        d4 = fma(__ldg(v.cvr_e2 + 2 * e + 1), w.lz4[size_t(v1) * K + k], d4);
-        d4 = fma(__ldg(v.ccd_e2 + 2 * e), w.ld4[i0], d4);
-        d4 = fma(__ldg(v.ccd_e2 + 2 * e + 1), w.ld4[i1], d4);
-      }
-      if (w.ld2u4) { // 1/max(dv, dc/4) differs: kept apart
-        w.ld2u[i] = d;
-        w.ld2u4[i] = d4;
-      } else {
-        w.ld2u[i] = d + d4;
-      }
-    }
-  } else {
-    w.lvnp[i] = 0.0;
-  }
-  const double g0 = __ldg(v.ccdh_e2 + 2 * e), g1 = __ldg(v.ccdh_e2 + 2 * e + 1);
-  if (p.do_h && !p.off_hadv)
-    lF = fma(__ldg(v.ccdh2_e2 + 2 * e), io.mh_[i0],
-             fma(__ldg(v.ccdh2_e2 + 2 * e + 1), io.mh_[i1], lF));
-  const bool adv = !p.off_tr_hadv;
-  for (int l = 0; l < p.ntracers; ++l) {
-    const size_t b = size_t(l) * CK;
-    const double n0 = a.ntr[b + i0], n1 = a.ntr[b + i1];
-    const double m0 = io.mtr[b + i0], m1 = io.mtr[b + i1];
-    if (adv)
-      lF = fma(n0 + n1, fma(g0, m0, g1 * m1), lF);
-    if (TRD) {
-      const double dn = n1 - n0;
-      if (p.tr_del2)
-        lmh = fma(dn, fma(__ldg(v.kd2_e2 + 2 * e), m0,
-                          -(__ldg(v.kd2_e2 + 2 * e + 1) * m1)), lmh);
-      if (p.tr_del4)
-        lmh = fma(dn, fma(__ldg(v.ckq_e2 + 2 * e), w.lL[b + i0],
-                          -(__ldg(v.ckq_e2 + 2 * e + 1) * w.lL[b + i1])), lmh);
-    }
-  }
-  const double mh = mean_h(m, a, io.h, e, k);
-  lmh = fma(u, lF, lmh);
-  w.lmh[i] = lmh;
-  w.lvnp[i] = fma(mh, lF, w.lvnp[i]);
+  pa_edge<NE, TRD>(m, p, a, v, w, io, blockIdx.x * ATPB + threadIdx.x);
 }
-
-// --- pass 5: vertices: PV q = (zeta + f) / h_v, vorticity; and, in the
-// C*K threads after the V*K vertex threads (launched with velocity
-// dissipation on), the cells' velocity-divergence adjoint, which reads only
-// the edge pass's output.  Splitting it from the cell pass lets the cell
-// and edge output passes run concurrently.
 __global__ void __launch_bounds__(ATPB)
     ka_vertex(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
               AdjIO io) {
-  const int K = m.nlayers;
-  unsigned i = blockIdx.x * ATPB + threadIdx.x;
-  const unsigned VK = unsigned(m.nvertices) * K;
-  if (i >= VK) {
-    i -= VK;
-    if (i >= unsigned(m.ncells) * K)
-      return;
-    const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
-    double ld = 0;
-    for (int j = 0; j < MAXE; ++j) {
-      const size_t ie = size_t(__ldg(m.ec + 6 * c + j)) * K + k;
-      ld = fma(__ldg(v.divadj + 6 * c + j),
-               w.ld2u4 ? w.ld2u[ie] + w.ld2u4[ie] : w.ld2u[ie], ld);
-    }
-    w.ldiv[i] = ld;
-    return;
-  }
-  const int vx = int(i / unsigned(K)), k = int(i - unsigned(vx) * K);
-  const int e0 = __ldg(m.ev + 3 * vx), e1 = __ldg(m.ev + 3 * vx + 1),
-            e2 = __ldg(m.ev + 3 * vx + 2);
-  const double lq = w.lQ[size_t(e0) * K + k] + w.lQ[size_t(e1) * K + k] +
-                    w.lQ[size_t(e2) * K + k];
-  double lz = 0;
-  if (p.vel_del2 | p.vel_del4) {
-    lz = __ldg(v.zetaadj + 3 * vx) * w.ld2u[size_t(e0) * K + k];
-    lz = fma(__ldg(v.zetaadj + 3 * vx + 1), w.ld2u[size_t(e1) * K + k], lz);
-    lz = fma(__ldg(v.zetaadj + 3 * vx + 2), w.ld2u[size_t(e2) * K + k], lz);
-    if (w.ld2u4) // the del4 chain's part, with 1/max(dv, dc/4)
-      for (int j = 0; j < 3; ++j)
-        lz = fma(__ldg(v.zetaadj4 + 3 * vx + j),
-                 w.ld2u4[size_t(__ldg(m.ev + 3 * vx + j)) * K + k], lz);
-  }
-  double r; // 1/h_vertex: the forward's value (taped, or recomputed)
-  if (a.rhv) {
-    r = a.rhv[i];
-  } else {
-    double hv = __ldg(m.kvh + 3 * vx) * io.h[size_t(__ldg(m.cv + 3 * vx)) * K + k];
-    for (int j = 1; j < 3; ++j)
-      hv = fma(__ldg(m.kvh + 3 * vx + j),
-               io.h[size_t(__ldg(m.cv + 3 * vx + j)) * K + k], hv);
-    r = fwd_rcp(hv);
-  }
-  w.lzeta[i] = fma(r, lq, lz);
-  w.lhv[i] = -(a.q[i] * r * lq);
+  pa_vertex(m, p, a, v, w, io, blockIdx.x * ATPB + threadIdx.x);
 }
-
-// --- pass 6: cells: thickness adjoint.
 __global__ void __launch_bounds__(ATPB)
-    ka_cell(MeshView m, ModelView p, AdjView v, AdjWork w, AdjIO io) {
-  const int K = m.nlayers;
-  const unsigned i = blockIdx.x * ATPB + threadIdx.x;
-  if (i >= unsigned(m.ncells) * K)
-    return;
-  const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
-  double lh = 0;
-  for (int j = 0; j < MAXE; ++j) {
-    const int e = __ldg(m.ec + 6 * c + j);
-    lh = fma(__ldg(v.hm_c + 6 * c + j), w.lmh[size_t(e) * K + k], lh);
-    if (p.do_vn)
-      lh = fma(__ldg(v.ckvh + 6 * c + j),
-               w.lhv[size_t(__ldg(v.cvtx + 6 * c + j)) * K + k], lh);
-  }
-  if (p.do_vn && !p.off_ssh)
-    lh = fma(p.grav, w.lke[i], lh); // SSH gradient: g times the KE term
-  if (p.ntracers > 0)
-    lh += w.lhtr[i];
-  emit(io, io.lh, io.acc_in_h, io.acc_h, io.nmu_h, io.lam_h, io.mh_, i, lh);
+    ka_cell(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
+            AdjIO io) {
+  pa_cell(m, p, a, v, w, io, blockIdx.x * ATPB + threadIdx.x);
 }
-
-// --- pass 7: edges: normal velocity adjoint.
 __global__ void __launch_bounds__(ATPB)
-    ka_vn(MeshView m, ModelView p, AdjView v, AdjWork w, AdjIO io) {
-  const int K = m.nlayers;
-  const unsigned i = blockIdx.x * ATPB + threadIdx.x;
-  if (i >= unsigned(m.nedges) * K)
-    return;
-  const int e = int(i / unsigned(K)), k = int(i - unsigned(e) * K);
-  double l = w.lvnp[i];
-  if (p.do_vn) {
-    const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
-    l = fma(__ldg(v.cvr_e2 + 2 * e), w.lzeta[size_t(v0) * K + k], l);
-    l = fma(__ldg(v.cvr_e2 + 2 * e + 1), w.lzeta[size_t(v1) * K + k], l);
-    if (p.vel_del2 | p.vel_del4) {
-      const int c0 = __ldg(m.ce + 2 * e), c1 = __ldg(m.ce + 2 * e + 1);
-      l = fma(__ldg(v.ccd_e2 + 2 * e), w.ldiv[size_t(c0) * K + k], l);
-      l = fma(__ldg(v.ccd_e2 + 2 * e + 1), w.ldiv[size_t(c1) * K + k], l);
-    }
-  }
-  emit(io, io.lvn, io.acc_in_vn, io.acc_vn, io.nmu_vn, io.lam_vn, io.mvn, i,
-       l);
+    ka_vn(MeshView m, ModelView p, AuxView a, AdjView v, AdjWork w,
+          AdjIO io) {
+  pa_vn(m, p, a, v, w, io, blockIdx.x * ATPB + threadIdx.x);
 }
 
 // y = alpha x1 + beta x2 (x2 may be null); dual pack / unpack
@@ -510,79 +120,6 @@ unsigned nb(long long n) { return unsigned((n + ATPB - 1) / ATPB); }
 
 using namespace swg;
 
-// Schedule actions.  ADV (a = first step, b = count) advances `cur` with
-// plain steps; STORE / RESTORE (a = slot) copy `cur` to / from a snapshot;
-// TAPE_ADJ (a = step, b = tape) tapes the step from `cur` into tape b and
-// runs its adjoint; TADV (a = step, b = tape) is a taped advance: the step
-// is taped into tape b and its result replaces `cur`; ADJ (a = step,
-// b = tape) runs the adjoint of a step taped earlier; FWD_END ends the
-// forward sweep (x_N is in `cur`).
-enum ActType { A_ADV = 0, A_STORE, A_RESTORE, A_TAPE_ADJ, A_TADV, A_ADJ,
-               A_FWD_END };
-struct AdjAction {
-  int type;
-  int a, b;
-};
-
-// A captured graph replayed while dt stays the same.
-struct AdjGraph {
-  cudaGraphExec_t exec = nullptr;
-  double dt = 0;
-  unsigned long long version = 0; // the model's term version captured
-  long long launches = 0;         // kernels per replay
-};
-
-// One step's tape: the stage inputs, the taped step's accumulator and the
-// intermediates of every stage, with the graphs that write and read it.
-struct TapeSlot {
-  swg_state X[5] = {}; // stage inputs; X[0] is the step's start state
-  swg_state acc = nullptr;
-  AuxView taux[5]{};
-  AdjGraph tape_adj; // tape without the step's result, then its adjoint
-  AdjGraph tadv;     // taped advance: X[0] <- cur, tape, result into cur
-  AdjGraph adj;      // adjoint of the taped step
-  // recorded on the caller's stream after each use of the tape by an
-  // adjoint, so that a taped advance on the advance stream waits for it
-  cudaEvent_t free_ev = nullptr;
-};
-constexpr int kTapes = 2;
-
-struct swg_adjoint_s {
-  swg_model model;
-  int nsnap;
-  AdjView av{};
-  AdjWork aw{};
-  std::vector<void *> allocs;
-  swg_stepper stepper = nullptr; // plain advances (graph replay)
-  std::vector<swg_state> snaps;
-  // stepper differentiated: RK4 (4 stages) or LSRK with 5 or 1 stages;
-  // rka / rkb are its coefficients (as in swg_stepper_create)
-  int kind = SWG_STEPPER_RK4, ns = 4;
-  std::vector<double> rka, rkb;
-  swg_state cur = nullptr, lam = nullptr, lacc = nullptr, mu = nullptr,
-            mu2 = nullptr;
-  TapeSlot tp[kTapes];
-  // tangent-linear model buffers
-  AuxViewT<Dual> daux{};
-  Dual *dS = nullptr, *dacc = nullptr, *dP0 = nullptr, *dP1 = nullptr,
-       *dT = nullptr;
-  // schedule
-  std::vector<AdjAction> actions;
-  size_t pos = 0;
-  int nsteps = 0;
-  double t0 = 0, dt = 0;
-  long long plain_steps = 0, taped_steps = 0, taped_advances = 0;
-  unsigned fwd_terms = 0; // the model's term set at the last forward sweep
-  int state = 0; // 0 idle, 1 forward done (the last steps taped)
-  bool grad_ready = false; // a backward sweep has completed
-  // backward sweep: restores, stores, plain and taped advances run on
-  // `adv`, concurrently with the caller's stream, which tapes and reverses
-  // the steps; `ready` = the advance stream's work so far is done (x_i in
-  // cur, taped advances written), `freed` = cur was copied to a tape
-  cudaStream_t adv = nullptr;
-  cudaEvent_t go = nullptr, ready = nullptr, freed = nullptr;
-};
-
 namespace {
 
 template <class T>
@@ -609,12 +146,6 @@ template <class T> int zal(std::vector<void *> &allocs, size_t n, T **d) {
   allocs.push_back(p);
   *d = static_cast<T *>(p);
   return SWG_OK;
-}
-
-size_t words(swg_model md) {
-  return (size_t(md->mesh->ncells) + md->mesh->nedges +
-          size_t(md->params.ntracers) * md->mesh->ncells) *
-         md->mesh->nlayers;
 }
 
 // The o-th slot j < n of list[base...] holding x (o = 0: the first), or -1.
@@ -898,8 +429,12 @@ void adj_passes(swg_adjoint ad, const AuxView &aux, const AdjIO &io,
   // outputs (h: lh and its stage bookkeeping; vn: the same for vn)
   fork_join(
       fk, st,
-      [&](cudaStream_t q) { ka_vn<<<nb(EK), ATPB, 0, q>>>(m, p, v, w, io); },
-      [&](cudaStream_t q) { ka_cell<<<nb(CK), ATPB, 0, q>>>(m, p, v, w, io); });
+      [&](cudaStream_t q) {
+        ka_vn<<<nb(EK), ATPB, 0, q>>>(m, p, aux, v, w, io);
+      },
+      [&](cudaStream_t q) {
+        ka_cell<<<nb(CK), ATPB, 0, q>>>(m, p, aux, v, w, io);
+      });
   g_launches += 2;
 }
 
@@ -927,95 +462,31 @@ void lincomb(swg_state y, swg_state x1, swg_state x2, double a, double b,
   ++g_launches;
 }
 
-// stage input of a tape: a disabled field keeps its start-of-step value
-void stage_ptrs(const swg_adjoint ad, const TapeSlot &tp, int s,
-                const double **h, const double **vn, const double **tr) {
-  const ModelView &p = ad->model->view;
-  *h = p.do_h ? tp.X[s]->h : tp.X[0]->h;
-  *vn = p.do_vn ? tp.X[s]->vn : tp.X[0]->vn;
-  *tr = tp.X[s]->tr;
-}
-
 // Taped low-storage RK step (lsrk.cpp:36-89) from tp.X[0]: stage s forms
 // T = a_s T + F(X_s) in tp.acc and X_{s+1} = X_s + dt b_s T in a separate
 // buffer (a copy of X_s updated by the same epilogue as the in-place
 // stepper, so the values are the stepper's bit for bit).  The last stage
 // only records its intermediates unless `out` takes the step's result.
-int tape_step_lsrk(swg_adjoint ad, TapeSlot &tp, double dt, swg_state out,
-                   cudaStream_t st) {
-  swg_model md = ad->model;
-  const ModelView &pv = md->view;
-  const int ns = ad->ns;
-  for (int s = 0; s < ns; ++s) {
-    const double *h, *vn, *tr;
-    stage_ptrs(ad, tp, s, &h, &vn, &tr);
-    swg_state o = s < ns - 1 ? tp.X[s + 1] : out;
-    if (!o) {
-      launch_aux(md->mesh->view, pv, tp.taux[s], h, vn, tr, st, &md->fork);
-      continue;
-    }
-    TRY(swg_state_copy(o, tp.X[s], st));
-    StageArgs a{};
-    a.h = h;
-    a.vn = vn;
-    a.tr = tr;
-    a.fh = {tp.acc->h, nullptr, nullptr, o->h};
-    a.fvn = {tp.acc->vn, nullptr, nullptr, o->vn};
-    a.ftr = {tp.acc->tr, nullptr, nullptr, o->tr};
-    a.ep = {EPI_LSRK, ad->rka[s], dt * ad->rkb[s], 0.0};
-    launch_tendency(md->mesh->view, pv, tp.taux[s], a, st, &md->fork);
-  }
-  cudaError_t err = cudaGetLastError();
-  return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_adjoint: taped step");
-}
-
+//
 // Taped RK4 step from tp.X[0] (the caller copies the step's start state
 // there): X1..X3 the stage inputs, and (when `out` is given) the step's
 // result.
 int tape_step(swg_adjoint ad, TapeSlot &tp, double dt, swg_state out,
               cudaStream_t st) {
-  if (ad->kind != SWG_STEPPER_RK4)
-    return tape_step_lsrk(ad, tp, dt, out, st);
   swg_model md = ad->model;
   const ModelView &pv = md->view;
-  static const double rka[3] = {1. / 2, 1. / 2, 1};
-  static const double rkb[4] = {1. / 6, 1. / 3, 1. / 3, 1. / 6};
-  swg_state S = tp.X[0];
-  const int last = out ? 3 : 2;
-  if (out) {
-    // a field whose tendency is disabled ends the step as it began; the
-    // stage epilogues write only the enabled fields of `out`
-    const size_t CK = size_t(md->mesh->ncells) * md->mesh->nlayers,
-                 EK = size_t(md->mesh->nedges) * md->mesh->nlayers;
-    cudaError_t e = cudaSuccess;
-    if (!pv.do_h)
-      e = cudaMemcpyAsync(out->h, S->h, CK * sizeof(double),
-                          cudaMemcpyDeviceToDevice, st);
-    if (e == cudaSuccess && !pv.do_vn)
-      e = cudaMemcpyAsync(out->vn, S->vn, EK * sizeof(double),
-                          cudaMemcpyDeviceToDevice, st);
-    if (e != cudaSuccess)
-      return cuda_fail(e, "swg_adjoint: taped step");
-  }
-  for (int s = 0; s <= last; ++s) {
-    StageArgs a{};
-    const double *h, *vn, *tr;
-    stage_ptrs(ad, tp, s, &h, &vn, &tr);
-    a.h = h;
-    a.vn = vn;
-    a.tr = tr;
-    swg_state o = s < 3 ? tp.X[s + 1] : out;
-    a.fh = {nullptr, S->h, tp.acc->h, o->h};
-    a.fvn = {nullptr, S->vn, tp.acc->vn, o->vn};
-    a.ftr = {nullptr, S->tr, tp.acc->tr, o->tr};
-    const int mode = s == 0 ? EPI_RK4_FIRST : (s < 3 ? EPI_RK4_MID : EPI_RK4_LAST);
-    a.ep = {mode, 0.0, dt * rkb[s], s < 3 ? dt * rka[s] : 0.0};
-    launch_tendency(md->mesh->view, pv, tp.taux[s], a, st, &md->fork);
-  }
-  if (!out) { // intermediates of the last stage input
-    const double *h, *vn, *tr;
-    stage_ptrs(ad, tp, 3, &h, &vn, &tr);
-    launch_aux(md->mesh->view, pv, tp.taux[3], h, vn, tr, st, &md->fork);
+  const int ns = ad->ns;
+  TRY(tape_prologue(ad, tp, out, st));
+  for (int s = 0; s < ns; ++s) {
+    if (s == ns - 1 && !out) { // intermediates of the last stage input
+      const double *h, *vn, *tr;
+      stage_ptrs(ad, tp, s, &h, &vn, &tr);
+      launch_aux(md->mesh->view, pv, tp.taux[s], h, vn, tr, st, &md->fork);
+      continue;
+    }
+    TRY(tape_stage_copy(ad, tp, s, out, st));
+    launch_tendency(md->mesh->view, pv, tp.taux[s],
+                    tape_stage_args(ad, tp, s, dt, out), st, &md->fork);
   }
   cudaError_t err = cudaGetLastError();
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_adjoint: taped step");
@@ -1035,57 +506,14 @@ int tape_step(swg_adjoint ad, TapeSlot &tp, double dt, swg_state out,
 // lamX_s = lamX_{s+1} + J(X_s)^T mu_s and
 // mu_{s-1} = dt b_{s-1} lamX_s + a_s mu_s; the step's adjoint is lamX_0.
 // The output passes accumulate lamX in lacc and form mu_{s-1} from it.
-const double *step_rkb(const swg_adjoint ad) {
-  static const double rk4b[4] = {1. / 6, 1. / 3, 1. / 3, 1. / 6};
-  return ad->kind != SWG_STEPPER_RK4 ? ad->rkb.data() : rk4b;
-}
-
 int adjoint_step(swg_adjoint ad, const TapeSlot &tp, double dt,
                  cudaStream_t st) {
-  static const double rk4a[3] = {1. / 2, 1. / 2, 1};
-  const bool lsrk = ad->kind != SWG_STEPPER_RK4;
   const int ns = ad->ns;
-  const bool even = ns % 2 == 0;
-  const double *rka = lsrk ? ad->rka.data() : rk4a;
-  const double *rkb = step_rkb(ad);
-  const long long n = (long long)words(ad->model);
-  if (!even)
-    lincomb(ad->mu, ad->lam, nullptr, dt * rkb[ns - 1], 0.0, n, st);
-  swg_state mus[2] = {ad->mu, ad->mu2};
-  for (int s = ns - 1; s >= 0; --s) {
-    swg_state mu = mus[(ns - 1 - s) % 2], nmu = mus[(ns - s) % 2];
-    AdjIO io{};
-    stage_ptrs(ad, tp, s, &io.h, &io.vn, &io.tr);
-    io.mh_ = mu->h;
-    io.mvn = mu->vn;
-    io.mtr = mu->tr;
-    swg_state in = s == ns - 1 ? ad->lam : ad->lacc;
-    swg_state out = s == 0 ? ad->lam : ad->lacc;
-    io.acc_in_h = in->h;
-    io.acc_in_vn = in->vn;
-    io.acc_in_tr = in->tr;
-    io.acc_h = out->h;
-    io.acc_vn = out->vn;
-    io.acc_tr = out->tr;
-    if (s > 0 || even) {
-      io.nmu_h = nmu->h;
-      io.nmu_vn = nmu->vn;
-      io.nmu_tr = nmu->tr;
-    }
-    if (s > 0) {
-      io.lam_h = ad->lam->h;
-      io.lam_vn = ad->lam->vn;
-      io.lam_tr = ad->lam->tr;
-      io.alpha = dt * rkb[s - 1];
-      io.beta = lsrk ? 0.0 : dt * rka[s - 1];
-      io.gamma = lsrk ? rka[s] : 0.0;
-      io.mode = lsrk ? 1 : 0;
-    } else if (even) { // the next step's first mu (its stage ns-1 reads mus[0])
-      io.alpha = dt * rkb[ns - 1];
-      io.mode = 2;
-    }
-    adj_passes(ad, tp.taux[s], io, st);
-  }
+  if (ns % 2 != 0)
+    lincomb(ad->mu, ad->lam, nullptr, dt * step_rkb(ad)[ns - 1], 0.0,
+            (long long)words(ad->model), st);
+  for (int s = ns - 1; s >= 0; --s)
+    adj_passes(ad, tp.taux[s], stage_io(ad, tp, s, dt), st);
   cudaError_t err = cudaGetLastError();
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_adjoint: adjoint step");
 }
@@ -1369,19 +797,6 @@ int run_action(swg_adjoint ad, const AdjAction &a, cudaStream_t st, bool two) {
   return rc;
 }
 
-// The model's tendency-term switches as a bit set: a backward sweep must
-// see the set its forward sweep ran with (its re-advances and tapes would
-// differ otherwise).
-unsigned term_set(swg_model md) {
-  const ModelView &p = md->view;
-  const int f[] = {p.off_hadv, p.off_pv, p.off_ke, p.off_ssh, p.off_tr_hadv,
-                   p.vel_del2, p.vel_del4, p.tr_del2, p.tr_del4};
-  unsigned s = 0;
-  for (int i = 0; i < 9; ++i)
-    s |= unsigned(f[i] != 0) << i;
-  return s;
-}
-
 int check_model(swg_model md) {
   if (!md)
     return fail(SWG_ERR_ARG, "swg_adjoint: NULL model");
@@ -1395,6 +810,110 @@ int check_model(swg_model md) {
 }
 
 } // namespace
+
+namespace swg {
+
+AdjIO stage_io(const swg_adjoint_s *ad, const TapeSlot &tp, int s,
+               double dt) {
+  const bool lsrk = ad->kind != SWG_STEPPER_RK4;
+  const int ns = ad->ns;
+  const bool even = ns % 2 == 0;
+  const double *rka = step_rka(ad), *rkb = step_rkb(ad);
+  swg_state mus[2] = {ad->mu, ad->mu2};
+  swg_state mu = mus[(ns - 1 - s) % 2], nmu = mus[(ns - s) % 2];
+  AdjIO io{};
+  stage_ptrs(ad, tp, s, &io.h, &io.vn, &io.tr);
+  io.mh_ = mu->h;
+  io.mvn = mu->vn;
+  io.mtr = mu->tr;
+  swg_state in = s == ns - 1 ? ad->lam : ad->lacc;
+  swg_state out = s == 0 ? ad->lam : ad->lacc;
+  io.acc_in_h = in->h;
+  io.acc_in_vn = in->vn;
+  io.acc_in_tr = in->tr;
+  io.acc_h = out->h;
+  io.acc_vn = out->vn;
+  io.acc_tr = out->tr;
+  if (s > 0 || even) {
+    io.nmu_h = nmu->h;
+    io.nmu_vn = nmu->vn;
+    io.nmu_tr = nmu->tr;
+  }
+  if (s > 0) {
+    io.lam_h = ad->lam->h;
+    io.lam_vn = ad->lam->vn;
+    io.lam_tr = ad->lam->tr;
+    io.alpha = dt * rkb[s - 1];
+    io.beta = lsrk ? 0.0 : dt * rka[s - 1];
+    io.gamma = lsrk ? rka[s] : 0.0;
+    io.mode = lsrk ? 1 : 0;
+  } else if (even) { // the next step's first mu (its stage ns-1 reads mus[0])
+    io.alpha = dt * rkb[ns - 1];
+    io.mode = 2;
+  }
+  return io;
+}
+
+StageArgs tape_stage_args(const swg_adjoint_s *ad, const TapeSlot &tp, int s,
+                          double dt, swg_state out) {
+  const int ns = ad->ns;
+  StageArgs a{};
+  stage_ptrs(ad, tp, s, &a.h, &a.vn, &a.tr);
+  swg_state o = s < ns - 1 ? tp.X[s + 1] : out;
+  if (ad->kind != SWG_STEPPER_RK4) { // in place on the copy o of X_s
+    a.fh = {tp.acc->h, nullptr, nullptr, o->h};
+    a.fvn = {tp.acc->vn, nullptr, nullptr, o->vn};
+    a.ftr = {tp.acc->tr, nullptr, nullptr, o->tr};
+    a.ep = {EPI_LSRK, ad->rka[s], dt * ad->rkb[s], 0.0};
+    return a;
+  }
+  const double *rka = step_rka(ad), *rkb = step_rkb(ad);
+  swg_state S = tp.X[0];
+  a.fh = {nullptr, S->h, tp.acc->h, o->h};
+  a.fvn = {nullptr, S->vn, tp.acc->vn, o->vn};
+  a.ftr = {nullptr, S->tr, tp.acc->tr, o->tr};
+  const int mode = s == 0 ? EPI_RK4_FIRST : (s < 3 ? EPI_RK4_MID : EPI_RK4_LAST);
+  a.ep = {mode, 0.0, dt * rkb[s], s < 3 ? dt * rka[s] : 0.0};
+  return a;
+}
+
+int tape_prologue(const swg_adjoint_s *ad, const TapeSlot &tp, swg_state out,
+                  cudaStream_t st) {
+  if (!out || ad->kind != SWG_STEPPER_RK4)
+    return SWG_OK;
+  // a field whose tendency is disabled ends the step as it began; the
+  // stage epilogues write only the enabled fields of `out`
+  const swg_model_s *md = ad->model;
+  const size_t CK = size_t(md->mesh->ncells) * md->mesh->nlayers,
+               EK = size_t(md->mesh->nedges) * md->mesh->nlayers;
+  cudaError_t e = cudaSuccess;
+  if (!md->view.do_h)
+    e = cudaMemcpyAsync(out->h, tp.X[0]->h, CK * sizeof(double),
+                        cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess && !md->view.do_vn)
+    e = cudaMemcpyAsync(out->vn, tp.X[0]->vn, EK * sizeof(double),
+                        cudaMemcpyDeviceToDevice, st);
+  return e == cudaSuccess ? SWG_OK : cuda_fail(e, "swg_adjoint: taped step");
+}
+
+int tape_stage_copy(const swg_adjoint_s *ad, const TapeSlot &tp, int s,
+                    swg_state out, cudaStream_t st) {
+  if (ad->kind == SWG_STEPPER_RK4)
+    return SWG_OK;
+  swg_state o = s < ad->ns - 1 ? tp.X[s + 1] : out;
+  return swg_state_copy(o, tp.X[s], st);
+}
+
+std::vector<AdjAction> plan_schedule(int nsteps, int nsnapshots, int nstages) {
+  return Planner(nsteps, nsnapshots - 1, nstages).schedule();
+}
+
+void adj_lincomb(swg_state y, swg_state x, double a, long long n,
+                 cudaStream_t st) {
+  lincomb(y, x, nullptr, a, 0.0, n, st);
+}
+
+} // namespace swg
 
 extern "C" int swg_adjoint_destroy(swg_adjoint ad);
 

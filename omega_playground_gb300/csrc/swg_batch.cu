@@ -27,15 +27,6 @@
 
 namespace swg {
 
-struct Member {
-  MeshView m;
-  ModelView p;
-  AuxView a;
-  StageArgs stage[5];
-  unsigned units[NPASS]; // elements of each pass (0 = pass not needed)
-  unsigned aux2_base;    // first element of the aux2 pass domain
-};
-
 struct BatchSync {
   unsigned count;
   unsigned gen;
@@ -161,6 +152,36 @@ __global__ void __launch_bounds__(512)
   }
 }
 
+template <int NE> void *pass_kernel_1(int pass) {
+  switch (pass) {
+  case P_VERTEX: return reinterpret_cast<void *>(&k_batch_pass<NE, 1, P_VERTEX>);
+  case P_CELL1: return reinterpret_cast<void *>(&k_batch_pass<NE, 1, P_CELL1>);
+  case P_EDGE1: return reinterpret_cast<void *>(&k_batch_pass<NE, 1, P_EDGE1>);
+  case P_AUX2: return reinterpret_cast<void *>(&k_batch_pass<NE, 1, P_AUX2>);
+  case P_EDGE_FINAL:
+    return reinterpret_cast<void *>(&k_batch_pass<NE, 1, P_EDGE_FINAL>);
+  default: return reinterpret_cast<void *>(&k_batch_pass<NE, 1, P_CELL_FINAL>);
+  }
+}
+
+int batch_launch_passes(const Member *mem, int nmem, const unsigned *prefix,
+                        const unsigned *prefix_h, int ne, int pass0,
+                        int pass1, int stage, cudaStream_t st) {
+  for (int pass = pass0; pass <= pass1; ++pass) {
+    const unsigned nvb = prefix_h[pass * (nmem + 1) + nmem];
+    if (nvb == 0)
+      continue;
+    void *args[] = {&mem, &nmem, &prefix, &stage};
+    cudaError_t err = cudaLaunchKernel(
+        ne == 8 ? pass_kernel_1<8>(pass) : pass_kernel_1<10>(pass), dim3(nvb),
+        dim3(256), args, 0, st);
+    if (err != cudaSuccess)
+      return cuda_fail(err, "batched passes: launch");
+    ++g_launches;
+  }
+  return SWG_OK;
+}
+
 // A wait that nothing releases, for testing the barrier's time limit: every
 // block but block 0 waits at a barrier block 0 never reaches.
 __global__ void k_barrier_selftest(BatchSync *bs, long long limit) {
@@ -206,9 +227,8 @@ struct swg_batch_s {
   long long graph_launches = 0;
 };
 
-namespace {
-
-void pass_units(const swg_model md, unsigned units[NPASS], unsigned &base) {
+void swg::batch_pass_units(const swg_model_s *md, unsigned units[NPASS],
+                           unsigned &base) {
   const ModelView &p = md->view;
   const long long K = md->mesh->nlayers, C = md->mesh->ncells,
                   E = md->mesh->nedges, V = md->mesh->nvertices;
@@ -222,6 +242,8 @@ void pass_units(const swg_model md, unsigned units[NPASS], unsigned &base) {
   units[P_EDGE_FINAL] = p.do_vn ? unsigned(E * K) : 0;
   units[P_CELL_FINAL] = (p.do_h || p.ntracers > 0) ? unsigned(C * K) : 0;
 }
+
+namespace {
 
 // Stage inputs/outputs of one member (same buffer rotation as the
 // single-instance fused stepper).
@@ -267,7 +289,7 @@ int refresh_members(swg_batch b) {
     if (b->versions[m] != b->models[m]->version) {
       Member &M = b->mem_h[m];
       M.p = b->models[m]->view;
-      pass_units(b->models[m], M.units, M.aux2_base);
+      batch_pass_units(b->models[m], M.units, M.aux2_base);
       b->versions[m] = b->models[m]->version;
       changed = true;
     }
@@ -499,7 +521,7 @@ extern "C" int swg_batch_create(int nmembers, const swg_model *models,
     M.m = models[m]->mesh->view;
     M.p = models[m]->view;
     M.a = models[m]->aux;
-    pass_units(models[m], M.units, M.aux2_base);
+    batch_pass_units(models[m], M.units, M.aux2_base);
     b->versions.push_back(models[m]->version);
   }
   cudaError_t err = cudaSuccess;

@@ -389,6 +389,27 @@ __device__ __forceinline__ void pt_cell_final(const MeshView &m,
 enum Pass { P_VERTEX = 0, P_CELL1, P_EDGE1, P_AUX2, P_EDGE_FINAL,
             P_CELL_FINAL, NPASS };
 
+// One member of a batched launch (swg_batch.cu, swg_ensemble.cu): its mesh,
+// model, intermediates, stage arguments and the element count of each pass.
+struct Member {
+  MeshView m;
+  ModelView p;
+  AuxView a;
+  StageArgs stage[5];
+  unsigned units[NPASS]; // elements of each pass (0 = pass not needed)
+  unsigned aux2_base;    // first element of the aux2 pass domain
+};
+// (swg_batch.cu) element counts of a model's passes
+void batch_pass_units(const swg_model_s *md, unsigned units[NPASS],
+                      unsigned &aux2_base);
+// (swg_batch.cu) passes [pass0, pass1] of stage `stage` over the nmem
+// members of the device table `mem`, one 256-thread block per virtual block
+// of 256 elements; prefix: [NPASS][nmem + 1] virtual-block offsets of the
+// members (device) and prefix_h its host copy (grid sizes).
+int batch_launch_passes(const Member *mem, int nmem, const unsigned *prefix,
+                        const unsigned *prefix_h, int ne, int pass0,
+                        int pass1, int stage, cudaStream_t st);
+
 // LinearShallowWaterModel (shallow_water_hierarchical.cpp:680-740):
 // vn_t = f sum_j w_j vn_j - g (h_1 - h_0) / dc and h_t = -h0 div(vn), each
 // with its stage update.

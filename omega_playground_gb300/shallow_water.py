@@ -955,6 +955,43 @@ def adjoint_batch_backward(adjs, lambdas, streams=None):
                                        _streams(streams, n)))
 
 
+class AdjointEnsemble:
+    """The members' checkpointed adjoints advanced together: every action of
+    the checkpoint schedule is one batched launch per pass over the members
+    (swg_adj_ensemble_* in swgpu.h).  Members are Adjoint objects with
+    distinct models; each keeps its own snapshot budget."""
+
+    def __init__(self, adjoints):
+        self.adjoints = list(adjoints)
+        h = C.c_void_p()
+        check(lib().swg_adj_ensemble_create(len(self.adjoints),
+                                            _handles(self.adjoints),
+                                            C.byref(h)))
+        self._h = h
+
+    def forward(self, states0, t0, dt, nsteps, finals, stream=None):
+        check(lib().swg_adj_ensemble_forward(self._h, _handles(states0),
+                                             float(t0), float(dt),
+                                             int(nsteps), _handles(finals),
+                                             _s(stream)))
+
+    def backward(self, lambdas, stream=None):
+        check(lib().swg_adj_ensemble_backward(self._h, _handles(lambdas),
+                                              _s(stream)))
+
+    def groups(self):
+        """(number of lockstep groups, each member's group)."""
+        n = C.c_int()
+        of = (C.c_int * len(self.adjoints))()
+        check(lib().swg_adj_ensemble_groups(self._h, C.byref(n), of))
+        return n.value, list(of)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _capi._lib is not None:
+            _capi._lib.swg_adj_ensemble_destroy(self._h)
+            self._h = None
+
+
 def checkpoint_cost(nsteps: int, nsnapshots: int) -> int:
     """Plain forward steps of the classic optimal binomial checkpointing
     schedule with one tape (Griewank-Walther)."""
