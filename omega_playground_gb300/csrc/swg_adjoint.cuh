@@ -68,6 +68,11 @@ struct AdjIO {
   int mode;
 };
 
+// The adds here and in the passes that take a product (x is often one) are
+// written as __dadd_rn: the compiler may not fuse them into a multiply-add,
+// which it could otherwise do differently in the single-instance and the
+// batched kernels that inline the same pass, and the two must agree bit for
+// bit.
 __device__ __forceinline__ void emit(const AdjIO &io, double *out,
                                      const double *acc_in, double *acc,
                                      double *nmu, const double *lam,
@@ -76,7 +81,7 @@ __device__ __forceinline__ void emit(const AdjIO &io, double *out,
     out[i] = x;
   double a = 0;
   if (acc) {
-    a = acc_in[i] + x;
+    a = __dadd_rn(acc_in[i], x);
     acc[i] = a;
   }
   if (nmu)
@@ -310,7 +315,7 @@ pa_edge(const MeshView &m, const ModelView &p, const AuxView &a,
         w.ld2u[i] = d;
         w.ld2u4[i] = d4;
       } else {
-        w.ld2u[i] = d + d4;
+        w.ld2u[i] = __dadd_rn(d, d4);
       }
     }
   } else {
@@ -362,7 +367,7 @@ pa_vertex(const MeshView &m, const ModelView &p, const AuxView &a,
     for (int j = 0; j < MAXE; ++j) {
       const size_t ie = size_t(__ldg(m.ec + 6 * c + j)) * K + k;
       ld = fma(__ldg(v.divadj + 6 * c + j),
-               w.ld2u4 ? w.ld2u[ie] + w.ld2u4[ie] : w.ld2u[ie], ld);
+               w.ld2u4 ? __dadd_rn(w.ld2u[ie], w.ld2u4[ie]) : w.ld2u[ie], ld);
     }
     w.ldiv[i] = ld;
     return;
@@ -415,7 +420,7 @@ pa_cell(const MeshView &m, const ModelView &p, const AuxView &a,
   if (p.do_vn && !p.off_ssh)
     lh = fma(p.grav, w.lke[i], lh); // SSH gradient: g times the KE term
   if (p.ntracers > 0)
-    lh += w.lhtr[i];
+    lh = __dadd_rn(lh, w.lhtr[i]);
   emit(io, io.lh, io.acc_in_h, io.acc_h, io.nmu_h, io.lam_h, io.mh_, i, lh);
 }
 
