@@ -43,10 +43,18 @@ struct AdjMember {
   unsigned units[NAPASS], base[NAPASS];
 };
 
+// The block's member descriptor is copied to shared memory once per
+// virtual block: the pass reads its tables and arrays through it many times
+// per thread, and shared loads are cheaper than the global ones a
+// reference into the member table would issue.
 template <int PASS, int NE, bool D2, bool D4, bool TRD>
 __global__ void __launch_bounds__(ATPB)
     kb_adj(const AdjMember *__restrict__ mem, int nmem,
            const unsigned *__restrict__ prefix) {
+  __shared__ AdjMember M;
+  constexpr int kWords = sizeof(AdjMember) / sizeof(unsigned long long);
+  static_assert(sizeof(AdjMember) % sizeof(unsigned long long) == 0,
+                "member descriptor copied in 8-byte words");
   const unsigned *pre = prefix + PASS * (nmem + 1);
   const unsigned nvb = pre[nmem];
   for (unsigned vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
@@ -58,7 +66,13 @@ __global__ void __launch_bounds__(ATPB)
       else
         hi = mid;
     }
-    const AdjMember &M = mem[lo];
+    __syncthreads(); // the previous virtual block is done with M
+    const unsigned long long *src =
+        reinterpret_cast<const unsigned long long *>(mem + lo);
+    unsigned long long *dst = reinterpret_cast<unsigned long long *>(&M);
+    for (int k = threadIdx.x; k < kWords; k += ATPB)
+      dst[k] = src[k];
+    __syncthreads();
     const unsigned j = (vb - pre[lo]) * ATPB + threadIdx.x;
     if (j < M.units[PASS])
       adj_pass<PASS, NE, D2, D4, TRD>(M.m, M.p, M.a, M.v, M.w, M.io,
@@ -98,16 +112,13 @@ KbFn kb_fn(int pass, int ne, bool d2, bool d4, bool trd) {
   }
 }
 
-// the order the passes of one adjoint stage run in (their data dependencies)
-constexpr int kAdjOrder[NAPASS] = {AP_VEL,    AP_TR1,  AP_EDGE, AP_TR2,
-                                   AP_VERTEX, AP_CELL, AP_VN};
-
 struct Group {
   std::vector<swg_adjoint> adjs; // the members, in the ensemble's order
   int ns = 4, kind = SWG_STEPPER_RK4, nsnap = 1, ne = 8;
   bool d2 = false, d4 = false, trd = false;
   cudaStream_t st = nullptr;
   cudaEvent_t done = nullptr;
+  Fork fork; // second stream for the independent passes
   swg_batch plain = nullptr; // the members' current states, plain steps
   // forward tables [kTapes][ns][n] and their prefix [NPASS][n + 1]
   Member *d_fwd = nullptr;
@@ -282,14 +293,23 @@ int batched_adjoint(Group &g, int b, cudaStream_t st) {
                   (long long)words(ad->model), st);
   for (int s = ns - 1; s >= 0; --s) {
     const AdjMember *tab = g.d_adj + (size_t(b) * ns + s) * n;
-    for (int q : kAdjOrder) {
-      const unsigned nvb = g.apre[size_t(q) * (n + 1) + n];
-      if (nvb == 0)
-        continue;
-      kb_fn(q, g.ne, g.d2, g.d4, g.trd)<<<nvb, ATPB, 0, st>>>(tab, n,
-                                                             g.d_apre);
-      ++g_launches;
-    }
+    auto pass = [&](int q) {
+      return [&, q](cudaStream_t qs) {
+        const unsigned nvb = g.apre[size_t(q) * (n + 1) + n];
+        if (nvb == 0)
+          return;
+        kb_fn(q, g.ne, g.d2, g.d4, g.trd)<<<nvb, ATPB, 0, qs>>>(tab, n,
+                                                               g.d_apre);
+        ++g_launches;
+      };
+    };
+    // the independent pairs run as fork/join branches, as in the single
+    // adjoint: velocity and tracer transposes, edge and tracer output,
+    // cell and normal-velocity output
+    fork_join(&g.fork, st, pass(AP_VEL), pass(AP_TR1));
+    fork_join(&g.fork, st, pass(AP_EDGE), pass(AP_TR2));
+    pass(AP_VERTEX)(st);
+    fork_join(&g.fork, st, pass(AP_VN), pass(AP_CELL));
   }
   cudaError_t err = cudaGetLastError();
   return err == cudaSuccess ? SWG_OK
@@ -390,6 +410,7 @@ extern "C" int swg_adj_ensemble_destroy(swg_adj_ensemble e) {
     cudaFree(g.d_apre);
     if (g.done)
       cudaEventDestroy(g.done);
+    fork_destroy(g.fork);
     if (g.st)
       cudaStreamDestroy(g.st);
   }
@@ -450,6 +471,8 @@ extern "C" int swg_adj_ensemble_create(int n, const swg_adjoint *adjs,
       err = cudaStreamCreateWithFlags(&g.st, cudaStreamNonBlocking);
     if (err == cudaSuccess)
       err = cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming);
+    if (err == cudaSuccess && fork_create(g.fork) != SWG_OK)
+      err = cudaErrorMemoryAllocation;
     if (err != cudaSuccess)
       break;
     std::vector<swg_model> models;
