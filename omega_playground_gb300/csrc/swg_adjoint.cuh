@@ -300,22 +300,28 @@ pa_edge(const MeshView &m, const ModelView &p, const AuxView &a,
     }
     if (p.vel_del2 | p.vel_del4) {
       const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
-      const double mk = m.mask ? m.mask[i] : 1.0; // the dissipation's mask
-      double d = p.vel_del2 ? __ldg(p.c2e + e) * (mu * mk) : 0.0;
+      // the dissipation terms are masked per edge and level (no multiply
+      // without a mask)
+      const double mum = m.mask ? mu * m.mask[i] : mu;
+      double d = p.vel_del2 ? __ldg(p.c2e + e) * mum : 0.0;
       if (p.vel_del2 && w.gc2e) // parameter gradient of the del2 coefficient
-        w.gc2e[i] = fma(mu * mk, a.d2u[i], w.gc2e[i]);
-      double d4 = 0; // the del4 chain's first Laplacian
+        w.gc2e[i] = fma(mum, a.d2u[i], w.gc2e[i]);
       if (p.vel_del4) {
-        d4 = __ldg(v.cvr_e2 + 2 * e) * w.lz4[size_t(v0) * K + k];
+        // the del4 chain's first Laplacian: accumulated onto the del2 part,
+        // or kept apart (ld2u4) where 1/max(dv, dc/4) differs from 1/dv
+        double d4 = w.ld2u4 ? 0.0 : d;
+        d4 = fma(__ldg(v.cvr_e2 + 2 * e), w.lz4[size_t(v0) * K + k], d4);
         d4 = fma(__ldg(v.cvr_e2 + 2 * e + 1), w.lz4[size_t(v1) * K + k], d4);
         d4 = fma(__ldg(v.ccd_e2 + 2 * e), w.ld4[i0], d4);
         d4 = fma(__ldg(v.ccd_e2 + 2 * e + 1), w.ld4[i1], d4);
-      }
-      if (w.ld2u4) { // 1/max(dv, dc/4) differs: kept apart
-        w.ld2u[i] = d;
-        w.ld2u4[i] = d4;
+        if (w.ld2u4) {
+          w.ld2u[i] = d;
+          w.ld2u4[i] = d4;
+        } else {
+          w.ld2u[i] = d4;
+        }
       } else {
-        w.ld2u[i] = __dadd_rn(d, d4);
+        w.ld2u[i] = d;
       }
     }
   } else {
