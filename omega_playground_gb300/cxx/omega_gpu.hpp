@@ -756,6 +756,62 @@ struct CheckpointedAdjoint {
   }
 };
 
+// Many members' gradients at once (swg_adj_ensemble_*): members with the
+// same schedule run in lockstep, every action one launch per pass over all
+// of them.  Each member's result equals its own CheckpointedAdjoint's bit
+// for bit; the adjoints stay owned by the caller and must outlive this.
+//   CheckpointedAdjointEnsemble ens({&a0, &a1, ...});
+//   ens.forward({&x0_0, ...}, t0, dt, n, {&xN_0, ...});
+//   ens.backward({&lambda_0, ...});
+struct CheckpointedAdjointEnsemble {
+  swg_adj_ensemble m_handle = nullptr;
+  Int m_size = 0;
+  explicit CheckpointedAdjointEnsemble(
+      const std::vector<CheckpointedAdjoint *> &adjoints) {
+    std::vector<swg_adjoint> h;
+    for (CheckpointedAdjoint *a : adjoints)
+      h.push_back(a->m_handle);
+    m_size = Int(h.size());
+    swg_check(swg_adj_ensemble_create(m_size, h.data(), &m_handle));
+  }
+  CheckpointedAdjointEnsemble(const CheckpointedAdjointEnsemble &) = delete;
+  CheckpointedAdjointEnsemble &
+  operator=(const CheckpointedAdjointEnsemble &) = delete;
+  ~CheckpointedAdjointEnsemble() { swg_adj_ensemble_destroy(m_handle); }
+  void forward(const std::vector<const ShallowWaterState *> &x0, Real t0,
+               Real dt, Int nsteps,
+               const std::vector<const ShallowWaterState *> &xN) {
+    const std::vector<swg_state> a = handles(x0), b = handles(xN);
+    swg_check(swg_adj_ensemble_forward(m_handle, a.data(), t0, dt, nsteps,
+                                       b.data(), nullptr));
+  }
+  void backward(const std::vector<const ShallowWaterState *> &lambda) {
+    const std::vector<swg_state> l = handles(lambda);
+    swg_check(swg_adj_ensemble_backward(m_handle, l.data(), nullptr));
+  }
+  // lockstep groups, and each member's group
+  Int groups(std::vector<int> *group_of = nullptr) const {
+    int n = 0;
+    if (group_of)
+      group_of->resize(m_size);
+    swg_check(swg_adj_ensemble_groups(m_handle, &n,
+                                      group_of ? group_of->data() : nullptr));
+    return n;
+  }
+
+private:
+  std::vector<swg_state>
+  handles(const std::vector<const ShallowWaterState *> &s) const {
+    if (Int(s.size()) != m_size)
+      throw std::runtime_error(
+          "CheckpointedAdjointEnsemble: one state per member");
+    std::vector<swg_state> h;
+    for (const ShallowWaterState *x : s)
+      h.push_back(x->handle());
+    return h;
+  }
+};
+
 // ------------------------------------------------------------ diagnostics --
 
 inline Real energy_integral(const ShallowWaterState &state,

@@ -4,7 +4,10 @@
 // <J dx0, lamN> = <dx0, J^T lamN> to 1e-12; (2) three members of different
 // sizes advanced by EnsembleStepper, and by HostStepper from host arrays,
 // equal, bit for bit, the same members advanced one at a time by
-// RK4Stepper.  Exits non-zero on failure.
+// RK4Stepper; (3) three members' gradients through
+// CheckpointedAdjointEnsemble (two share a schedule and run in lockstep)
+// equal, bit for bit, each member's own CheckpointedAdjoint.  Exits
+// non-zero on failure.
 #include <omega_gpu.hpp>
 
 #include <cmath>
@@ -168,11 +171,85 @@ bool ensemble_test() {
   return worst == 0.0 && worst_host == 0.0;
 }
 
+bool same(const Fields &a, const Fields &b) {
+  return a.h == b.h && a.vn == b.vn && a.tr == b.tr;
+}
+
+bool adjoint_ensemble_test() {
+  struct Member {
+    std::unique_ptr<PlanarHexagonalMesh> mesh;
+    ShallowWaterParams p;
+    std::unique_ptr<ShallowWaterModel> model;
+    std::unique_ptr<CheckpointedAdjoint> adj;
+    std::unique_ptr<ShallowWaterState> x0, xN, lam;
+    Fields f0, g;
+  };
+  // members 0 and 1: same schedule (4 snapshots, RK4, 2 tracers), different
+  // sizes; member 2: 3 snapshots, its own group
+  const Int nx[3] = {10, 14, 8}, K[3] = {4, 3, 6}, nsnap[3] = {4, 4, 3};
+  const Real dt = 20, t0 = 0;
+  const Int nsteps = 9;
+  std::vector<Member> mem(3);
+  for (int m = 0; m < 3; ++m) {
+    Member &u = mem[m];
+    u.mesh = std::make_unique<PlanarHexagonalMesh>(nx[m], nx[m] - 2, 1e4, K[m]);
+    u.p.m_f0 = 1e-4;
+    u.p.m_visc_del2 = 1e3;
+    u.p.m_visc_del4 = 1e9;
+    u.p.m_eddy_diff2 = 1e3;
+    u.p.m_ntracers = 2;
+    u.model = std::make_unique<ShallowWaterModel>(u.mesh.get(), u.p);
+    u.adj = std::make_unique<CheckpointedAdjoint>(*u.model, nsnap[m]);
+    u.x0 = std::make_unique<ShallowWaterState>(u.mesh.get(), u.p);
+    u.xN = std::make_unique<ShallowWaterState>(u.mesh.get(), u.p);
+    u.lam = std::make_unique<ShallowWaterState>(u.mesh.get(), u.p);
+    u.f0 = random_state(*u.mesh, 2, 100 + m, 1000, 2, 0.2, 1);
+    u.g = random_state(*u.mesh, 2, 200 + m, 0, 1, 1, 1);
+    u.x0->upload(u.f0.h, u.f0.vn, u.f0.tr);
+  }
+  // each member's own adjoint
+  std::vector<Fields> ref(3), refN(3);
+  for (Member &u : mem) {
+    u.adj->forward(*u.x0, t0, dt, nsteps, *u.xN);
+    u.lam->upload(u.g.h, u.g.vn, u.g.tr);
+    u.adj->backward(*u.lam);
+  }
+  for (int m = 0; m < 3; ++m) {
+    ref[m] = download(*mem[m].lam);
+    refN[m] = download(*mem[m].xN);
+  }
+  // the same through the ensemble
+  std::vector<CheckpointedAdjoint *> adjs;
+  std::vector<const ShallowWaterState *> x0s, xNs, lams;
+  for (Member &u : mem) {
+    adjs.push_back(u.adj.get());
+    x0s.push_back(u.x0.get());
+    xNs.push_back(u.xN.get());
+    lams.push_back(u.lam.get());
+  }
+  CheckpointedAdjointEnsemble ens(adjs);
+  std::vector<int> group_of;
+  const Int ngroups = ens.groups(&group_of);
+  ens.forward(x0s, t0, dt, nsteps, xNs);
+  for (Member &u : mem)
+    u.lam->upload(u.g.h, u.g.vn, u.g.tr);
+  ens.backward(lams);
+  bool ok = ngroups == 2 && group_of[0] == group_of[1] &&
+            group_of[0] != group_of[2];
+  for (int m = 0; m < 3; ++m)
+    ok = ok && same(download(*mem[m].lam), ref[m]) &&
+         same(download(*mem[m].xN), refN[m]);
+  std::printf("adjoint ensemble groups=%lld bitwise=%d\n", (long long)ngroups,
+              ok);
+  return ok;
+}
+
 } // namespace
 
 int main() {
   const bool a = dot_product_test();
   const bool b = ensemble_test();
-  std::printf("%s\n", a && b ? "PASS" : "FAIL");
-  return a && b ? 0 : 1;
+  const bool c = adjoint_ensemble_test();
+  std::printf("%s\n", a && b && c ? "PASS" : "FAIL");
+  return a && b && c ? 0 : 1;
 }

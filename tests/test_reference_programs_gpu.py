@@ -99,13 +99,15 @@ def test_cpp_gradient_and_ensemble_classes():
     """The C++ drop-in's CheckpointedAdjoint (dot product against the
     tangent-linear model, 10 RK4 steps, every term on, <= 1e-12) and
     EnsembleStepper and HostStepper (three uneven members bitwise equal to
-    RK4Stepper)."""
+    RK4Stepper), and CheckpointedAdjointEnsemble (three members in two
+    lockstep groups bitwise equal to their own adjoints)."""
     out = run("gradients_and_ensembles")
     assert "PASS" in out, out
     rel = float(re.search(r"rel=(\S+)", out).group(1))
     assert rel <= 1e-12
     assert "ensemble max_abs_diff=0.000e+00" in out
     assert "host max_abs_diff=0.000e+00" in out
+    assert "adjoint ensemble groups=2 bitwise=1" in out
 
 
 def test_cpp_term_members_and_f_vertex():
