@@ -39,6 +39,12 @@ METRIC = ("cell·level·stage updates/s FP64 (% HBM roofline); "
 UNIT = "cell·level·stage updates/s"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
+# FP64 thread instructions (DFMA + DADD + DMUL) per cell-level of
+# k_cell_final on the LSRK5 512x512x64x8 workload's physics, counted by ncu
+# (smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum over the
+# launch's cell-levels); it is a property of the compiled kernel and the
+# enabled terms, not of the mesh size
+K_CELL_FINAL_FP64 = 142
 
 
 def parse():
@@ -441,10 +447,11 @@ def run_ours(args, wl):
         pk_clk = pk_clocks.stop()
         pk_mhz = pk_clk.get("sm_mhz") or 0.0
         peak_inst = rates["dfma"][0]
-        got_inst = 155.0 * CK / (dom_ms / 1e3)
+        got_inst = K_CELL_FINAL_FP64 * CK / (dom_ms / 1e3)
         fp64 = {"bound": "fp64", "kernel": dom, "achieved": got_inst / 1e9,
                 "peak": peak_inst / 1e9, "unit": "G FP64 inst/s",
-                "frac": got_inst / peak_inst, "inst_per_cell_level": 155,
+                "frac": got_inst / peak_inst,
+                "inst_per_cell_level": K_CELL_FINAL_FP64,
                 "peak_source": "measured: swg_fp64_issue_rate (DFMA), this run",
                 "issue_rates": {
                     op: {"G_inst_per_s": r / 1e9, "ms": round(ms, 3),

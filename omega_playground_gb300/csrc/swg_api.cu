@@ -236,6 +236,9 @@ extern "C" int swg_mesh_create(const swg_mesh_desc *d, swg_mesh *out) {
     m->scale2_h.assign(d->mesh_scaling_del2, d->mesh_scaling_del2 + E);
   if (d->mesh_scaling_del4)
     m->scale4_h.assign(d->mesh_scaling_del4, d->mesh_scaling_del4 + E);
+  m->scale2_uniform = E > 0;
+  for (size_t e = 1; e < size_t(E) && m->scale2_uniform; ++e)
+    m->scale2_uniform = m->scale2_h[e] == m->scale2_h[0];
   m->ckq_h = ckq;
   m->ec_h = ec;
   m->nec_h.assign(d->nedges_on_cell, d->nedges_on_cell + C);
@@ -475,11 +478,13 @@ extern "C" int swg_model_create_ex(swg_mesh mesh, const swg_params *p,
   pv.drag_level = int(K) - 1; // the lowest level
 
   std::vector<double> f(V, p->f0), c2(E), c4(E), kd2(6 * C), r4(6 * C),
-      r4s(C), gidc(E);
+      r4s(C), gidc(E), r4f, c4i(E), c4v(E);
   for (size_t e = 0; e < E; ++e) {
     gidc[e] = p->grav * mesh->inv_dc_h[e];
     c2[e] = p->visc_del2 * mesh->scale2_h[e];
     c4[e] = -(p->visc_del4 * mesh->scale4_h[e]);
+    c4i[e] = c4[e] * mesh->inv_dc_h[e];
+    c4v[e] = -(c4[e] * mesh->inv_dv_h[e]);
   }
   for (size_t c = 0; c < C; ++c) {
     double s = 0;
@@ -491,15 +496,25 @@ extern "C" int swg_model_create_ex(swg_mesh mesh, const swg_params *p,
     }
     r4s[c] = s;
   }
+  // the tracer del2 term folded into the del4 stencil (ModelView::r4f)
+  if (mesh->scale2_uniform && T > 0 && pv.tr_del2 && pv.tr_del4) {
+    const double k2 = p->eddy_diff2 * mesh->scale2_h[0];
+    r4f.resize(C);
+    for (size_t c = 0; c < C; ++c)
+      r4f[c] = k2 - r4s[c];
+  }
   auto &A = md->allocs;
   int rc = SWG_OK;
   if ((rc = upload(A, f.data(), V, &pv.f_vertex)) ||
       (rc = upload(A, gidc.data(), E, &pv.gidc)) ||
       (rc = upload(A, c2.data(), E, &pv.c2e)) ||
       (rc = upload(A, c4.data(), E, &pv.c4e)) ||
+      (pv.vel_del4 && (rc = upload(A, c4i.data(), E, &pv.c4i))) ||
+      (pv.vel_del4 && (rc = upload(A, c4v.data(), E, &pv.c4v))) ||
       (rc = upload(A, kd2.data(), 6 * C, &pv.kd2)) ||
       (rc = upload(A, r4.data(), 6 * C, &pv.r4)) ||
-      (rc = upload(A, r4s.data(), C, &pv.r4sum))) {
+      (rc = upload(A, r4s.data(), C, &pv.r4sum)) ||
+      (!r4f.empty() && (rc = upload(A, r4f.data(), C, &pv.r4f)))) {
     swg_model_destroy(md);
     return rc;
   }

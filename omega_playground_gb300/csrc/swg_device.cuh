@@ -303,8 +303,13 @@ __device__ __forceinline__ void pt_edge_final(const MeshView &m,
     const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
     const T dd = a.d4[size_t(c1) * K + k] - a.d4[size_t(c0) * K + k];
     const T dz = a.z4[size_t(v1) * K + k] - a.z4[size_t(v0) * K + k];
-    const T l = fma(dd, idc, -(dz * __ldg(m.inv_dv + e)));
-    t = fma(m.mask ? __ldg(p.c4e + e) * mk : __ldg(p.c4e + e), l, t);
+    if (!m.mask && p.c4i) {
+      t = fma(__ldg(p.c4i + e), dd, t);
+      t = fma(__ldg(p.c4v + e), dz, t);
+    } else {
+      const T l = fma(dd, idc, -(dz * __ldg(m.inv_dv + e)));
+      t = fma(m.mask ? __ldg(p.c4e + e) * mk : __ldg(p.c4e + e), l, t);
+    }
   }
   epilogue(s.ep, s.fvn, i, t);
 }
@@ -347,9 +352,12 @@ __device__ __forceinline__ void pt_cell_final(const MeshView &m,
     for (int j = 0; j < MAXE; ++j)
       w[j] = T{};
   }
-  // advection + del2: sum_j a_j (n_c + n_j) + b_j (n_j - n_c)
+  // advection + del2: sum_j a_j (n_c + n_j) + b_j (n_j - n_c); with a
+  // uniform del2 scaling the del2 part is eddy_diff2 s L_c instead, taken
+  // with the del4 stencil's centre weight (r4f)
+  const bool fold = p.tr_del2 && p.tr_del4 && p.r4f;
   T wc = Sa;
-  if (p.tr_del2) {
+  if (p.tr_del2 && !fold) {
     T b[MAXE], Sb;
 #pragma unroll
     for (int j = 0; j < MAXE; ++j) {
@@ -366,7 +374,37 @@ __device__ __forceinline__ void pt_cell_final(const MeshView &m,
 #pragma unroll
   for (int j = 0; j < MAXE; ++j)
     nb[j] = __ldg(m.nbc + 6 * c + j);
-  for (int l = 0; l < p.ntracers; ++l) {
+  // del4 centre weight: -sum r4, plus eddy_diff2 s when del2 is folded in
+  const double rc = !p.tr_del4 ? 0.0 : fold ? __ldg(p.r4f + c)
+                                            : -__ldg(p.r4sum + c);
+  // tracers in pairs: two independent FMA chains per thread keep more
+  // loads and FP64 operations in flight (each tracer's operation sequence
+  // is the same as alone, so the results are too)
+  int l = 0;
+  for (; l + 1 < p.ntracers; l += 2) {
+    const size_t b0 = size_t(l) * CK, b1 = b0 + CK;
+    const T *n0 = a.ntr + b0, *n1 = a.ntr + b1;
+    T acc0 = wc * n0[i], acc1 = wc * n1[i];
+#pragma unroll
+    for (int j = 0; j < MAXE; ++j) {
+      acc0 = fma(w[j], n0[size_t(nb[j]) * K + k], acc0);
+      acc1 = fma(w[j], n1[size_t(nb[j]) * K + k], acc1);
+    }
+    if (p.tr_del4) {
+      const T *L0 = a.lap + b0, *L1 = a.lap + b1;
+      acc0 = fma(rc, L0[i], acc0);
+      acc1 = fma(rc, L1[i], acc1);
+#pragma unroll
+      for (int j = 0; j < MAXE; ++j) {
+        const double r = __ldg(p.r4 + 6 * c + j);
+        acc0 = fma(r, L0[size_t(nb[j]) * K + k], acc0);
+        acc1 = fma(r, L1[size_t(nb[j]) * K + k], acc1);
+      }
+    }
+    epilogue(s.ep, s.ftr, b0 + i, acc0);
+    epilogue(s.ep, s.ftr, b1 + i, acc1);
+  }
+  for (; l < p.ntracers; ++l) {
     const size_t base = size_t(l) * CK;
     const T *n = a.ntr + base;
     T acc = wc * n[i];
@@ -375,7 +413,7 @@ __device__ __forceinline__ void pt_cell_final(const MeshView &m,
       acc = fma(w[j], n[size_t(nb[j]) * K + k], acc);
     if (p.tr_del4) {
       const T *L = a.lap + base;
-      acc = fma(-__ldg(p.r4sum + c), L[i], acc);
+      acc = fma(rc, L[i], acc);
 #pragma unroll
       for (int j = 0; j < MAXE; ++j)
         acc = fma(__ldg(p.r4 + 6 * c + j), L[size_t(nb[j]) * K + k], acc);

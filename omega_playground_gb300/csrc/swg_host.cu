@@ -13,6 +13,13 @@
 // out on a third, so with page-locked host arrays the copies of one chunk
 // overlap the compute of its neighbours.  Each level sees the same kernels
 // and operands as in the unsliced model, so the results are bitwise equal.
+//
+// With page-locked mapped host arrays and a few steps per call, the whole
+// call (copies in, the chunks' steps, copies out, across the three streams)
+// is captured once into one CUDA graph and replayed: the host then makes one
+// launch per call instead of a hundred-odd API calls, so a host thread that
+// is held up while it issues them (by another process's driver calls, say)
+// no longer leaves the copy engines and the SMs idle mid-call.
 #include "swg_internal.h"
 
 #include <algorithm>
@@ -130,13 +137,31 @@ double *mapped(double *p, size_t n) {
 
 } // namespace
 
+// One captured call: valid for the same host arrays (and their device
+// mappings), dt, step count and model term version.
+struct CallGraph {
+  cudaGraphExec_t exec = nullptr;
+  const double *h = nullptr, *vn = nullptr, *tr = nullptr;
+  const double *mh = nullptr, *mv = nullptr, *mt = nullptr;
+  double dt = 0;
+  int nsteps = 0;
+  unsigned long long version = 0;
+  long long launches = 0;       // kernels one replay runs
+  unsigned long long used = 0;  // last use (least recently used is replaced)
+};
+constexpr int kCallGraphs = 4;     // cached captured calls per stepper
+constexpr int kCallGraphSteps = 4; // calls of more steps launch directly
+
 struct swg_host_stepper_s {
   swg_model model = nullptr;
   int K = 0, T = 0;
   int copy_grid = 0; // blocks of the SM copies (8 per SM)
   std::vector<Chunk> chunks;
   cudaStream_t h2d = nullptr, comp = nullptr, d2h = nullptr;
+  cudaStream_t cap = nullptr; // origin of the call captures
   cudaEvent_t go = nullptr, done = nullptr;
+  CallGraph graphs[kCallGraphs];
+  unsigned long long uses = 0;
 };
 
 extern "C" int swg_host_stepper_destroy(swg_host_stepper hs) {
@@ -152,7 +177,10 @@ extern "C" int swg_host_stepper_destroy(swg_host_stepper hs) {
     if (c.out)
       cudaEventDestroy(c.out);
   }
-  for (cudaStream_t s : {hs->h2d, hs->comp, hs->d2h})
+  for (CallGraph &g : hs->graphs)
+    if (g.exec)
+      cudaGraphExecDestroy(g.exec);
+  for (cudaStream_t s : {hs->h2d, hs->comp, hs->d2h, hs->cap})
     if (s)
       cudaStreamDestroy(s);
   for (cudaEvent_t e : {hs->go, hs->done})
@@ -222,7 +250,7 @@ extern "C" int swg_host_stepper_create_levels(swg_model model, int kind,
   if ((err = cudaGetDevice(&dev)) == cudaSuccess)
     err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   hs->copy_grid = 8 * std::max(sms, 1);
-  for (cudaStream_t *s : {&hs->h2d, &hs->comp, &hs->d2h})
+  for (cudaStream_t *s : {&hs->h2d, &hs->comp, &hs->d2h, &hs->cap})
     if (err == cudaSuccess)
       err = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
   for (cudaEvent_t *e : {&hs->go, &hs->done})
@@ -261,22 +289,21 @@ extern "C" int swg_host_stepper_chunks(swg_host_stepper hs, int *levels,
   return SWG_OK;
 }
 
-static int host_step(swg_host_stepper hs, double *h, double *vn, double *tr,
-                     double t0, double dt, int nsteps, void *stream) {
+// Everything one call does, ordered after `origin` and before it again:
+// copies in, each chunk's steps (its step graph when use_graph, else direct
+// launches, as inside a capture), copies out.  mh, mv, mt: the device
+// addresses of the mapped host arrays, or all nullptr (copy engines only).
+static int enqueue_call(swg_host_stepper hs, double *h, double *vn, double *tr,
+                        double *mh, double *mv, double *mt, double t0,
+                        double dt, int nsteps, int use_graph,
+                        cudaStream_t origin) {
   swg_model src = hs->model;
-  if (src->forcing)
-    return fail(SWG_ERR_ARG, "swg_host_step: the model has a forcing hook "
-                             "(it would see level slices)");
   const size_t K = hs->K, C = src->mesh->ncells, E = src->mesh->nedges,
                TC = size_t(hs->T) * C;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  NvtxRange range("host_step");
   // The first chunk's copy-in precedes all compute and the last chunk's
   // copy-out follows it, so the SMs are idle then: those two go through the
   // SM copies when the arrays are mapped page-locked memory.  The other
   // chunks' copies overlap compute and stay on the copy engines.
-  double *mh = mapped(h, C * K), *mv = mapped(vn, E * K),
-         *mt = TC ? mapped(tr, TC * K) : nullptr;
   const bool sm_copies = mh && mv && (mt || !TC);
   auto levels_in = [&](double *dst, const double *host, size_t rows, int k0,
                        int kc) {
@@ -297,7 +324,7 @@ static int host_step(swg_host_stepper hs, double *h, double *vn, double *tr,
     ++g_launches;
     return cudaGetLastError();
   };
-  cudaError_t err = cudaEventRecord(hs->go, st);
+  cudaError_t err = cudaEventRecord(hs->go, origin);
   for (cudaStream_t s : {hs->h2d, hs->comp, hs->d2h})
     if (err == cudaSuccess)
       err = cudaStreamWaitEvent(s, hs->go, 0);
@@ -340,7 +367,7 @@ static int host_step(swg_host_stepper hs, double *h, double *vn, double *tr,
     c.model->view.drag_level = src->view.drag_level - c.k0;
     c.model->version = src->version;
     c.model->terms_switched = src->terms_switched;
-    TRY(swg_step(c.stepper, c.state, t0, dt, nsteps, 1, hs->comp));
+    TRY(swg_step(c.stepper, c.state, t0, dt, nsteps, use_graph, hs->comp));
     err = cudaEventRecord(c.out, hs->comp);
     if (err != cudaSuccess)
       return cuda_fail(err, "swg_host_step: stream order");
@@ -372,7 +399,97 @@ static int host_step(swg_host_stepper hs, double *h, double *vn, double *tr,
   if (err == cudaSuccess)
     err = cudaEventRecord(hs->done, hs->d2h);
   if (err == cudaSuccess)
-    err = cudaStreamWaitEvent(st, hs->done, 0);
+    err = cudaStreamWaitEvent(origin, hs->done, 0);
+  return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_host_step");
+}
+
+// The captured call for these arrays, dt, step count and term version,
+// captured now if no cached one matches; nullptr when the capture fails
+// (the caller then launches the call directly).
+static CallGraph *call_graph(swg_host_stepper hs, double *h, double *vn,
+                             double *tr, double *mh, double *mv, double *mt,
+                             double t0, double dt, int nsteps) {
+  const unsigned long long version = hs->model->version;
+  for (CallGraph &g : hs->graphs)
+    if (g.exec && g.h == h && g.vn == vn && g.tr == tr && g.mh == mh &&
+        g.mv == mv && g.mt == mt && g.dt == dt && g.nsteps == nsteps &&
+        g.version == version) {
+      g.used = ++hs->uses;
+      return &g;
+    }
+  CallGraph *slot = &hs->graphs[0];
+  for (CallGraph &g : hs->graphs)
+    if (!g.exec || g.used < slot->used)
+      slot = &g;
+  if (slot->exec) {
+    cudaGraphExecDestroy(slot->exec);
+    slot->exec = nullptr;
+  }
+  const long long before = g_launches.load();
+  cudaError_t err =
+      cudaStreamBeginCapture(hs->cap, cudaStreamCaptureModeThreadLocal);
+  int rc = SWG_OK;
+  if (err == cudaSuccess)
+    rc = enqueue_call(hs, h, vn, tr, mh, mv, mt, t0, dt, nsteps, 0, hs->cap);
+  cudaGraph_t g = nullptr;
+  const cudaError_t err2 =
+      err == cudaSuccess ? cudaStreamEndCapture(hs->cap, &g) : err;
+  const long long launches = g_launches.load() - before;
+  g_launches -= launches; // captured, not launched
+  cudaGraphExec_t exec = nullptr;
+  if (err == cudaSuccess && err2 == cudaSuccess && rc == SWG_OK && g)
+    err = cudaGraphInstantiate(&exec, g, 0);
+  if (g)
+    cudaGraphDestroy(g);
+  if (err != cudaSuccess || err2 != cudaSuccess || rc != SWG_OK || !exec) {
+    (void)cudaGetLastError();
+    if (exec)
+      cudaGraphExecDestroy(exec);
+    return nullptr;
+  }
+  slot->exec = exec;
+  slot->h = h;
+  slot->vn = vn;
+  slot->tr = tr;
+  slot->mh = mh;
+  slot->mv = mv;
+  slot->mt = mt;
+  slot->dt = dt;
+  slot->nsteps = nsteps;
+  slot->version = version;
+  slot->launches = launches;
+  slot->used = ++hs->uses;
+  return slot;
+}
+
+static int host_step(swg_host_stepper hs, double *h, double *vn, double *tr,
+                     double t0, double dt, int nsteps, void *stream) {
+  swg_model src = hs->model;
+  if (src->forcing)
+    return fail(SWG_ERR_ARG, "swg_host_step: the model has a forcing hook "
+                             "(it would see level slices)");
+  const size_t K = hs->K, C = src->mesh->ncells, E = src->mesh->nedges,
+               TC = size_t(hs->T) * C;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  NvtxRange range("host_step");
+  double *mh = mapped(h, C * K), *mv = mapped(vn, E * K),
+         *mt = TC ? mapped(tr, TC * K) : nullptr;
+  if (!(mh && mv && (mt || !TC)))
+    mh = mv = mt = nullptr;
+  cudaError_t err = cudaSuccess;
+  // the steps carry no time (the model has no forcing hook), so t0 does not
+  // enter the captured call
+  CallGraph *g = mh && nsteps > 0 && nsteps <= kCallGraphSteps &&
+                         !profiling_enabled()
+                     ? call_graph(hs, h, vn, tr, mh, mv, mt, t0, dt, nsteps)
+                     : nullptr;
+  if (g) {
+    err = cudaGraphLaunch(g->exec, st);
+    if (err == cudaSuccess)
+      g_launches += g->launches;
+  } else {
+    TRY(enqueue_call(hs, h, vn, tr, mh, mv, mt, t0, dt, nsteps, 1, st));
+  }
   if (err == cudaSuccess)
     err = cudaStreamSynchronize(st);
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_host_step");

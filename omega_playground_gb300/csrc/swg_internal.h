@@ -74,9 +74,17 @@ struct ModelView {
   const double *gidc;     // [E] grav / dc
   const double *c2e;      // [E] visc_del2 * scale2
   const double *c4e;      // [E] -visc_del4 * scale4
+  // [E] c4e / dc and -c4e / dv: the del4 tendency's outer Laplacian with
+  // the coefficient folded in (used without an edge mask; nullptr = unused)
+  const double *c4i, *c4v;
   const double *kd2;      // [C][6] eddy_diff2 * scale2 * ckq
   const double *r4;       // [C][6] -eddy_diff4 * scale4 * ckq
   const double *r4sum;    // [C] sum of r4
+  // [C] eddy_diff2 * s - r4sum when mesh_scaling_del2 is s on every edge,
+  // else nullptr.  The tracer del2 term is then eddy_diff2 * s times the
+  // thickness-weighted Laplacian the del4 term already computes, so it
+  // folds into the centre weight of the del4 stencil.
+  const double *r4f;
   int ntracers;
   int vel_del2, vel_del4, tr_del2, tr_del4, do_h, do_vn;
   // LinearShallowWaterModel (mean thickness h0; f4 = 4 f0, the Coriolis
@@ -225,6 +233,7 @@ struct swg_mesh_s {
   std::vector<void *> allocs;
   // host copies of the per-edge scaling (the model scales them)
   std::vector<double> scale2_h, scale4_h, ckq_h, inv_dc_h;
+  bool scale2_uniform = false; // mesh_scaling_del2 the same on every edge
   std::vector<int> ec_h, nec_h; // edges_on_cell (padded), nedges_on_cell
   // host copies of the derived tables (the adjoint builds transposes)
   std::vector<int> ev_h, cv_h, nbc_h, ce_h, ve_h, eoe_h;

@@ -120,14 +120,18 @@ __global__ void k_noalloc_tables(MeshView m, double f0, double grav,
                                  double visc2, double visc4, double kappa2,
                                  double kappa4, double *f_vertex, double *gidc,
                                  double *c2e, double *c4e, double *kd2,
-                                 double *r4, double *r4sum) {
+                                 double *r4, double *r4sum, double *r4f,
+                                 double *c4i, double *c4v) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i < m.nvertices)
     f_vertex[i] = f0;
   if (i < m.nedges) {
     gidc[i] = grav * m.inv_dc[i];
     c2e[i] = visc2 * m.scale2[i];
-    c4e[i] = -(visc4 * m.scale4[i]);
+    const double c4 = -(visc4 * m.scale4[i]);
+    c4e[i] = c4;
+    c4i[i] = c4 * m.inv_dc[i];
+    c4v[i] = -(c4 * m.inv_dv[i]);
   }
   if (i < m.ncells) {
     double s = 0;
@@ -139,6 +143,8 @@ __global__ void k_noalloc_tables(MeshView m, double f0, double grav,
       s += r;
     }
     r4sum[i] = s;
+    if (r4f) // uniform del2 scaling: the tracer del2 folded into del4
+      r4f[i] = kappa2 * m.scale2[0] - s;
   }
 }
 
@@ -157,7 +163,7 @@ struct Carve {
 // Lays out the model tables and the intermediates the enabled terms need;
 // with base == nullptr it only measures.
 size_t layout(const swg_mesh_s *mesh, const ModelView &pv, unsigned char *base,
-              double *tab[7], AuxView &a) {
+              double *tab[10], AuxView &a) {
   const size_t C = mesh->ncells, E = mesh->nedges, V = mesh->nvertices,
                K = mesh->nlayers, T = pv.ntracers;
   Carve cv{base};
@@ -168,6 +174,9 @@ size_t layout(const swg_mesh_s *mesh, const ModelView &pv, unsigned char *base,
   tab[4] = cv.take(6 * C); // kd2
   tab[5] = cv.take(6 * C); // r4
   tab[6] = cv.take(C);     // r4sum
+  tab[7] = cv.take(C);     // r4f
+  tab[8] = cv.take(E);     // c4i
+  tab[9] = cv.take(E);     // c4v
   const bool vn = pv.do_vn;
   const bool vdiss = vn && (pv.vel_del2 || pv.vel_del4);
   const bool v4 = vn && pv.vel_del4;
@@ -216,7 +225,7 @@ extern "C" int swg_compute_tendency_noalloc(swg_mesh mesh,
   pv.tr_del4 = params->eddy_diff4 > 0;
   pv.do_h = !params->disable_h_tendency;
   pv.do_vn = !params->disable_vn_tendency;
-  double *tab[7];
+  double *tab[10];
   AuxView a;
   const size_t need = layout(mesh, pv, nullptr, tab, a);
   if (need > kScratchBytes) {
@@ -246,6 +255,11 @@ extern "C" int swg_compute_tendency_noalloc(swg_mesh mesh,
   pv.kd2 = tab[4];
   pv.r4 = tab[5];
   pv.r4sum = tab[6];
+  const bool fold = mesh->scale2_uniform && pv.ntracers > 0 && pv.tr_del2 &&
+                    pv.tr_del4;
+  pv.r4f = fold ? tab[7] : nullptr;
+  pv.c4i = tab[8];
+  pv.c4v = tab[9];
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const MeshView &m = mesh->view;
   const long long n = std::max<long long>(
@@ -253,7 +267,7 @@ extern "C" int swg_compute_tendency_noalloc(swg_mesh mesh,
   k_noalloc_tables<<<unsigned((n + 255) / 256), 256, 0, st>>>(
       m, params->f0, params->grav, params->visc_del2, params->visc_del4,
       params->eddy_diff2, params->eddy_diff4, tab[0], tab[1], tab[2], tab[3],
-      tab[4], tab[5], tab[6]);
+      tab[4], tab[5], tab[6], fold ? tab[7] : nullptr, tab[8], tab[9]);
   ++g_launches;
   StageArgs s{};
   s.h = h;
