@@ -503,7 +503,9 @@ def run_ours(args, wl):
                     "d2h_gbs": round(nbytes_in / min(down) / 1e6, 1)}
         link_before = link_rates()
         e2e_clocks = ClockSampler(uuid)
-        time.sleep(0.3)
+        # let the sampler's start-up (driver queries of its own) finish
+        # before the first timed call
+        time.sleep(1.0)
         barrier()
         call_ms = []
         e0.record(stream)

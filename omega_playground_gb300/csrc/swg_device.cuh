@@ -315,8 +315,10 @@ __device__ __forceinline__ void pt_edge_final(const MeshView &m,
 }
 
 // Cell final pass: thickness tendency and tracer tendencies (advection,
-// del2, del4) with their stage updates.
-template <class T>
+// del2, del4) with their stage updates.  PAIRS: tracers two at a time (the
+// single-instance kernel; the batched kernels, which already give each
+// thread several elements, keep one at a time and their registers).
+template <class T, bool PAIRS = false>
 __device__ __forceinline__ void pt_cell_final(const MeshView &m,
                                               const ModelView &p,
                                               const AuxViewT<T> &a,
@@ -381,7 +383,7 @@ __device__ __forceinline__ void pt_cell_final(const MeshView &m,
   // loads and FP64 operations in flight (each tracer's operation sequence
   // is the same as alone, so the results are too)
   int l = 0;
-  for (; l + 1 < p.ntracers; l += 2) {
+  for (; PAIRS && l + 1 < p.ntracers; l += 2) {
     const size_t b0 = size_t(l) * CK, b1 = b0 + CK;
     const T *n0 = a.ntr + b0, *n1 = a.ntr + b1;
     T acc0 = wc * n0[i], acc1 = wc * n1[i];

@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(TPB)
     k_cell_final(MeshView m, ModelView p, AuxViewT<T> a, StageArgsT<T> s) {
   const unsigned i = blockIdx.x * TPB + threadIdx.x;
   if (i < unsigned(m.ncells) * unsigned(m.nlayers))
-    pt_cell_final<T>(m, p, a, s, i);
+    pt_cell_final<T, std::is_same<T, double>::value>(m, p, a, s, i);
 }
 
 template <int NE, class T>
