@@ -190,3 +190,65 @@ def test_autotuned_picks_a_timed_candidate_and_leaves_the_state():
         a[...] = b
     hs.step(*arrs, 0.0, WL.dt, 2)
     assert_bitwise(arrs, want)
+
+
+def test_call_graph_cache():
+    """With page-locked arrays each call of up to 4 steps replays one
+    captured graph of the whole call, cached per array set, dt, step count
+    and term version.  Six array sets used in turn twice (the cache holds
+    four), a term switched between two one-step calls on the same arrays, a
+    new dt and a call of more steps than the cache takes (direct launches)
+    all equal the device stepper bit for bit, and a replay counts the same
+    kernels as the call that captured it."""
+    mesh = og.PlanarHexagonalMesh(WL.nx, WL.ny, WL.dc, WL.nlayers)
+    params = WL.params()
+    model = og.ShallowWaterModel(mesh, params)
+    x = initial_state(mesh, WL)
+    hs = og.HostStepper(model, "lsrk", 5, 3)
+    rng = np.random.default_rng(17)
+    sets, starts = [], []
+    for _ in range(6):
+        arrs = hs.pinned_state()
+        x0 = [x[0] * (1 + 1e-3 * rng.standard_normal(x[0].shape)),
+              x[1] + 0.01 * rng.standard_normal(x[1].shape), x[2].copy()]
+        for a, b in zip(arrs, x0):
+            a[...] = b
+        sets.append(arrs)
+        starts.append(x0)
+    # six array sets, two rounds: the second round's sets were evicted
+    # from the cache, or (the last four) replay their captured call
+    for rnd in range(2):
+        for arrs in sets:
+            n0 = og.kernel_launches()
+            hs.step(*arrs, 0.0, WL.dt, 2)
+            n1 = og.kernel_launches()
+            hs.step(*arrs, 2 * WL.dt, WL.dt, 2)
+            assert og.kernel_launches() - n1 == n1 - n0 > 0
+    for arrs, x0 in zip(sets, starts):
+        want = device_run(model, mesh, params, x0, "lsrk", 5, 0.0, WL.dt, 8)
+        assert_bitwise(arrs, want)
+    # a term switched between two one-step calls on the same arrays
+    arrs, x0 = sets[0], starts[0]
+    for a, b in zip(arrs, x0):
+        a[...] = b
+    hs.step(*arrs, 0.0, WL.dt, 1)
+    model.m_ke_grad_edge.m_enabled = False
+    hs.step(*arrs, WL.dt, WL.dt, 1)
+    model.m_ke_grad_edge.m_enabled = True
+    S = og.ShallowWaterState(mesh, params)
+    S.upload(*x0)
+    st = og.LSRKStepper(model, 5)
+    st.step(S, 0.0, WL.dt, 1)
+    model.m_ke_grad_edge.m_enabled = False
+    st.step(S, WL.dt, WL.dt, 1)
+    model.m_ke_grad_edge.m_enabled = True
+    assert_bitwise(arrs, S.download())
+    # a new dt, then more steps per call than the cache takes
+    for a, b in zip(arrs, x0):
+        a[...] = b
+    hs.step(*arrs, 0.0, 0.5 * WL.dt, 1)
+    hs.step(*arrs, 0.5 * WL.dt, WL.dt, 6)
+    S.upload(*x0)
+    st.step(S, 0.0, 0.5 * WL.dt, 1)
+    st.step(S, 0.5 * WL.dt, WL.dt, 6)
+    assert_bitwise(arrs, S.download())
