@@ -316,7 +316,10 @@ def adjoint_ratio(stream, nsteps=0, nsnap=0):
     X0 = og.ShallowWaterState(mesh, params)
     X0.upload(*x0)
     XN = og.ShallowWaterState(mesh, params)
-    adj.forward(X0, 0.0, wl.dt, 2, XN, stream=sh)      # warm-up
+    # warm-up: a full-length forward sweep plans the schedule (host, once
+    # per step and snapshot count), a 2-step pair captures the graphs
+    adj.forward(X0, 0.0, wl.dt, wl.nsteps, XN, stream=sh)
+    adj.forward(X0, 0.0, wl.dt, 2, XN, stream=sh)
     G = og.ShallowWaterState(mesh, params)
     G.fill(0.0, stream=sh)
     adj.backward(G, stream=sh)
@@ -746,7 +749,11 @@ def adjoint_ensemble_line():
     # the batched ensemble: every schedule action one launch per pass over
     # the members of a lockstep group (one group per snapshot budget)
     ens = og.AdjointEnsemble(adjs)
-    ens.forward(X0, 0.0, dt, 2, XN)                    # warm-up, tables
+    # warm-up: a full-length forward sweep plans the members' schedules
+    # (host, once per step and snapshot count), a 2-step pair builds the
+    # tables and captures the graphs
+    ens.forward(X0, 0.0, dt, nsteps, XN)
+    ens.forward(X0, 0.0, dt, 2, XN)
     Gw = []
     for m in mem:
         G = og.ShallowWaterState(m["mesh"], m["params"])

@@ -35,6 +35,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <new>
 
 namespace swg {
@@ -574,7 +575,9 @@ struct Planner {
   long long cADV = 100, cTADV = 104, cTAPE = 85;
   std::vector<long long> f, h;
   std::vector<int> fm, hm; // 0: the taped pair; m > 0: split after m steps
-  size_t at(int n, int s) const { return size_t(n) * (S + 1) + s; }
+  // one row of n per snapshot count: the split search walks f(m, s) and
+  // f(n - m, s - 1) through contiguous memory
+  size_t at(int n, int s) const { return size_t(s) * (N + 1) + n; }
   Planner(int n, int s, int ns)
       : N(n), S(std::max(0, std::min(s, n - 1))) {
     cTAPE = (100LL * (ns - 1) + 40) / ns;
@@ -904,8 +907,35 @@ int tape_stage_copy(const swg_adjoint_s *ad, const TapeSlot &tp, int s,
   return swg_state_copy(o, tp.X[s], st);
 }
 
+// The schedule of (steps, snapshots, stages), planned once per process and
+// kept: the dynamic program is O(steps^2 snapshots) on the host (tens of ms
+// at 1000 steps and 32 snapshots), which a forward sweep would otherwise
+// spend before its first launch every time.
 std::vector<AdjAction> plan_schedule(int nsteps, int nsnapshots, int nstages) {
-  return Planner(nsteps, nsnapshots - 1, nstages).schedule();
+  struct Entry {
+    int n, s, ns;
+    std::vector<AdjAction> acts;
+  };
+  static std::mutex mu;
+  static std::vector<Entry> cache; // most recently used last
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    for (size_t i = 0; i < cache.size(); ++i)
+      if (cache[i].n == nsteps && cache[i].s == nsnapshots &&
+          cache[i].ns == nstages) {
+        Entry e = std::move(cache[i]);
+        cache.erase(cache.begin() + i);
+        cache.push_back(std::move(e));
+        return cache.back().acts;
+      }
+  }
+  std::vector<AdjAction> acts =
+      Planner(nsteps, nsnapshots - 1, nstages).schedule();
+  std::lock_guard<std::mutex> lock(mu);
+  if (cache.size() >= 16)
+    cache.erase(cache.begin());
+  cache.push_back({nsteps, nsnapshots, nstages, acts});
+  return acts;
 }
 
 void adj_lincomb(swg_state y, swg_state x, double a, long long n,
@@ -1160,8 +1190,7 @@ int fwd_begin(swg_adjoint ad, swg_state state0, double t0, double dt,
   if (nsteps > kMaxAdjointSteps)
     return fail(SWG_ERR_ARG, "swg_adj_forward: more steps than the schedule "
                              "planner takes (10000); split the trajectory");
-  Planner pl(nsteps, ad->nsnap - 1, ad->ns);
-  std::vector<AdjAction> acts = pl.schedule();
+  std::vector<AdjAction> acts = plan_schedule(nsteps, ad->nsnap, ad->ns);
   long long plain, tadv;
   count_actions(acts, &plain, &tadv);
   if (plain > kMaxReadvance * (long long)nsteps)
@@ -1449,7 +1478,7 @@ extern "C" int swg_adj_plan(int nsteps, int nsnapshots, int nstages,
       !(nstages == 4 || nstages == 5 || nstages == 1))
     return fail(SWG_ERR_ARG, "swg_adj_plan: bad argument");
   long long p = 0, t = 0;
-  count_actions(Planner(nsteps, nsnapshots - 1, nstages).schedule(), &p, &t);
+  count_actions(plan_schedule(nsteps, nsnapshots, nstages), &p, &t);
   if (plain_steps)
     *plain_steps = p;
   if (taped_advances)
@@ -1464,7 +1493,7 @@ extern "C" int swg_adj_schedule(int nsteps, int nsnapshots, int nstages,
       max_actions < 0 || (max_actions > 0 && !actions))
     return fail(SWG_ERR_ARG, "swg_adj_schedule: bad argument");
   const std::vector<AdjAction> acts =
-      Planner(nsteps, nsnapshots - 1, nstages).schedule();
+      plan_schedule(nsteps, nsnapshots, nstages);
   *count = int(acts.size());
   const int n = std::min<int>(max_actions, int(acts.size()));
   for (int i = 0; i < n; ++i) {
