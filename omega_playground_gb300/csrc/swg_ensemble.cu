@@ -119,6 +119,12 @@ struct Group {
   cudaStream_t st = nullptr;
   cudaEvent_t done = nullptr;
   Fork fork; // second stream for the independent passes
+  // backward sweep: restores, stores, plain and taped advances run on
+  // `adv`, tapes and adjoints on `st`, as in the single adjoint; `ready`
+  // hands the advanced state to `st`, `freed` gives `cur` back once its tape
+  // input is copied, free_ev[b] marks tape b read by its adjoint
+  cudaStream_t adv = nullptr;
+  cudaEvent_t ready = nullptr, freed = nullptr, free_ev[kTapes] = {};
   swg_batch plain = nullptr; // the members' current states, plain steps
   // forward tables [kTapes][ns][n] and their prefix [NPASS][n + 1]
   Member *d_fwd = nullptr;
@@ -265,11 +271,14 @@ int g_replay(AdjGraph &gr, cudaStream_t st, Fn record) {
 
 // The taped step of every member into tape b: out_cur = the result replaces
 // `cur` (a taped advance); otherwise the last stage records only its
-// intermediates (a tape from a state).
-int batched_tape(Group &g, int b, bool out_cur, cudaStream_t st) {
+// intermediates (a tape from a state).  copy_in: copy `cur` to the tape's
+// step input first (else the caller did).
+int batched_tape(Group &g, int b, bool out_cur, bool copy_in,
+                 cudaStream_t st) {
   const int n = g.n(), ns = g.ns;
   for (swg_adjoint ad : g.adjs) {
-    TRY(swg_state_copy(ad->tp[b].X[0], ad->cur, st));
+    if (copy_in)
+      TRY(swg_state_copy(ad->tp[b].X[0], ad->cur, st));
     TRY(tape_prologue(ad, ad->tp[b], out_cur ? ad->cur : nullptr, st));
   }
   for (int s = 0; s < ns; ++s) {
@@ -316,46 +325,73 @@ int batched_adjoint(Group &g, int b, cudaStream_t st) {
                             : cuda_fail(err, "swg_adj_ensemble: adjoint step");
 }
 
-int group_action(Group &g, const AdjAction &a) {
-  cudaStream_t st = g.st;
+cudaError_t hand_over(cudaEvent_t ev, cudaStream_t from, cudaStream_t to) {
+  cudaError_t e = cudaEventRecord(ev, from);
+  return e == cudaSuccess ? cudaStreamWaitEvent(to, ev, 0) : e;
+}
+
+// One schedule action for every member of the group.  two: the backward
+// sweep's two streams (advances on g.adv, tapes and adjoints on g.st).
+int group_action(Group &g, const AdjAction &a, bool two) {
+  cudaStream_t st = g.st, q = two ? g.adv : g.st;
+  cudaError_t e = cudaSuccess;
   switch (a.type) {
   case A_ADV: {
     swg_adjoint ad0 = g.adjs[0];
     for (swg_adjoint ad : g.adjs)
       ad->plain_steps += a.b;
     return swg_batch_step(g.plain, ad0->t0 + a.a * ad0->dt, ad0->dt, a.b, 1,
-                          st);
+                          q);
   }
   case A_STORE:
     for (swg_adjoint ad : g.adjs)
-      TRY(swg_state_copy(ad->snaps[a.a], ad->cur, st));
+      TRY(swg_state_copy(ad->snaps[a.a], ad->cur, q));
     return SWG_OK;
   case A_RESTORE:
     for (swg_adjoint ad : g.adjs)
-      TRY(swg_state_copy(ad->cur, ad->snaps[a.a], st));
+      TRY(swg_state_copy(ad->cur, ad->snaps[a.a], q));
     return SWG_OK;
   case A_TADV:
     for (swg_adjoint ad : g.adjs) {
       ++ad->taped_steps;
       ++ad->taped_advances;
     }
-    return g_replay(g.g_tadv[a.b], st, [&](cudaStream_t cs) {
-      return batched_tape(g, a.b, true, cs);
+    if (two && (e = cudaStreamWaitEvent(q, g.free_ev[a.b], 0)) != cudaSuccess)
+      return cuda_fail(e, "swg_adj_ensemble: stream handshake");
+    return g_replay(g.g_tadv[a.b], q, [&](cudaStream_t cs) {
+      return batched_tape(g, a.b, true, true, cs);
     });
   case A_TAPE_ADJ:
-    for (swg_adjoint ad : g.adjs)
-      ++ad->taped_steps;
-    return g_replay(g.g_tape_adj[a.b], st, [&](cudaStream_t cs) {
-      TRY(batched_tape(g, a.b, false, cs));
-      return batched_adjoint(g, a.b, cs);
-    });
   case A_ADJ:
-    return g_replay(g.g_adj[a.b], st, [&](cudaStream_t cs) {
-      return batched_adjoint(g, a.b, cs);
-    });
+    break;
   default:
     return SWG_OK;
   }
+  // the state (and a taped advance's tape) from the advance stream
+  if (two && (e = hand_over(g.ready, g.adv, st)) != cudaSuccess)
+    return cuda_fail(e, "swg_adj_ensemble: stream handshake");
+  int rc;
+  if (a.type == A_TAPE_ADJ) {
+    for (swg_adjoint ad : g.adjs) {
+      ++ad->taped_steps;
+      TRY(swg_state_copy(ad->tp[a.b].X[0], ad->cur, st));
+    }
+    // `cur` may be advanced again once its copy is taken
+    if (two && (e = hand_over(g.freed, st, g.adv)) != cudaSuccess)
+      return cuda_fail(e, "swg_adj_ensemble: stream handshake");
+    rc = g_replay(g.g_tape_adj[a.b], st, [&](cudaStream_t cs) {
+      TRY(batched_tape(g, a.b, false, false, cs));
+      return batched_adjoint(g, a.b, cs);
+    });
+  } else {
+    rc = g_replay(g.g_adj[a.b], st, [&](cudaStream_t cs) {
+      return batched_adjoint(g, a.b, cs);
+    });
+  }
+  if (rc == SWG_OK && two &&
+      (e = cudaEventRecord(g.free_ev[a.b], st)) != cudaSuccess)
+    return cuda_fail(e, "swg_adj_ensemble: stream handshake");
+  return rc;
 }
 
 // the caller's stream (st) before the groups' streams, or after them
@@ -363,8 +399,9 @@ int streams_follow(const std::vector<Group> &gs, cudaStream_t st,
                    cudaEvent_t ev) {
   cudaError_t err = cudaEventRecord(ev, st);
   for (const Group &g : gs)
-    if (err == cudaSuccess)
-      err = cudaStreamWaitEvent(g.st, ev, 0);
+    for (cudaStream_t s : {g.st, g.adv})
+      if (err == cudaSuccess)
+        err = cudaStreamWaitEvent(s, ev, 0);
   return err == cudaSuccess ? SWG_OK
                             : cuda_fail(err, "swg_adj_ensemble: streams");
 }
@@ -408,11 +445,16 @@ extern "C" int swg_adj_ensemble_destroy(swg_adj_ensemble e) {
     cudaFree(g.d_fpre);
     cudaFree(g.d_adj);
     cudaFree(g.d_apre);
-    if (g.done)
-      cudaEventDestroy(g.done);
+    for (cudaEvent_t ev : {g.done, g.ready, g.freed})
+      if (ev)
+        cudaEventDestroy(ev);
+    for (cudaEvent_t ev : g.free_ev)
+      if (ev)
+        cudaEventDestroy(ev);
     fork_destroy(g.fork);
-    if (g.st)
-      cudaStreamDestroy(g.st);
+    for (cudaStream_t s : {g.st, g.adv})
+      if (s)
+        cudaStreamDestroy(s);
   }
   if (e->go)
     cudaEventDestroy(e->go);
@@ -467,10 +509,15 @@ extern "C" int swg_adj_ensemble_create(int n, const swg_adjoint *adjs,
   int rc = SWG_OK;
   cudaError_t err = cudaEventCreateWithFlags(&e->go, cudaEventDisableTiming);
   for (Group &g : e->groups) {
-    if (err == cudaSuccess)
-      err = cudaStreamCreateWithFlags(&g.st, cudaStreamNonBlocking);
-    if (err == cudaSuccess)
-      err = cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming);
+    for (cudaStream_t *s : {&g.st, &g.adv})
+      if (err == cudaSuccess)
+        err = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
+    for (cudaEvent_t *ev : {&g.done, &g.ready, &g.freed})
+      if (err == cudaSuccess)
+        err = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    for (cudaEvent_t &ev : g.free_ev)
+      if (err == cudaSuccess)
+        err = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     if (err == cudaSuccess && fork_create(g.fork) != SWG_OK)
       err = cudaErrorMemoryAllocation;
     if (err != cudaSuccess)
@@ -546,7 +593,7 @@ extern "C" int swg_adj_ensemble_forward(swg_adj_ensemble e,
     for (Group &g : e->groups) {
       if (g.pos >= g.acts.size() || g.acts[g.pos].type == A_FWD_END)
         continue;
-      TRY(group_action(g, g.acts[g.pos++]));
+      TRY(group_action(g, g.acts[g.pos++], false));
       ++left;
     }
   }
@@ -608,9 +655,14 @@ extern "C" int swg_adj_ensemble_backward(swg_adj_ensemble e,
     for (Group &g : e->groups) {
       if (g.pos >= g.acts.size())
         continue;
-      TRY(group_action(g, g.acts[g.pos++]));
+      TRY(group_action(g, g.acts[g.pos++], true));
       ++left;
     }
+  }
+  for (Group &g : e->groups) { // the advance stream's last work before st's
+    cudaError_t err = hand_over(g.ready, g.adv, g.st);
+    if (err != cudaSuccess)
+      return cuda_fail(err, "swg_adj_ensemble_backward: streams");
   }
   for (int a = 0; a < n; ++a) {
     swg_adjoint ad = e->adjs[a];
