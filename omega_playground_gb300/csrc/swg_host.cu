@@ -9,9 +9,10 @@
 // that shares the caller's device tables but has kc levels (and its own
 // slice of the per-level edge mask), a model whose view is the caller's,
 // a device state of kc levels and an ordinary stepper with its graph.
-// A call copies chunk c in on one stream, steps it on another and copies it
-// out on a third, so with page-locked host arrays the copies of one chunk
-// overlap the compute of its neighbours.  Each level sees the same kernels
+// A call copies chunk c in on one stream, steps it on another (two compute
+// streams take the chunks in turn) and copies it out on a fourth, so with
+// page-locked host arrays the copies of one chunk overlap the compute of its
+// neighbours.  Each level sees the same kernels
 // and operands as in the unsliced model, so the results are bitwise equal.
 //
 // With page-locked mapped host arrays and a few steps per call, the whole
@@ -157,7 +158,9 @@ struct swg_host_stepper_s {
   int K = 0, T = 0;
   int copy_grid = 0; // blocks of the SM copies (8 per SM)
   std::vector<Chunk> chunks;
-  cudaStream_t h2d = nullptr, comp = nullptr, d2h = nullptr;
+  // copies in, compute (even chunks on comp, odd ones on comp2, so a
+  // chunk's last passes overlap the next chunk's first ones), copies out
+  cudaStream_t h2d = nullptr, comp = nullptr, comp2 = nullptr, d2h = nullptr;
   cudaStream_t cap = nullptr; // origin of the call captures
   cudaEvent_t go = nullptr, done = nullptr;
   CallGraph graphs[kCallGraphs];
@@ -180,7 +183,7 @@ extern "C" int swg_host_stepper_destroy(swg_host_stepper hs) {
   for (CallGraph &g : hs->graphs)
     if (g.exec)
       cudaGraphExecDestroy(g.exec);
-  for (cudaStream_t s : {hs->h2d, hs->comp, hs->d2h, hs->cap})
+  for (cudaStream_t s : {hs->h2d, hs->comp, hs->comp2, hs->d2h, hs->cap})
     if (s)
       cudaStreamDestroy(s);
   for (cudaEvent_t e : {hs->go, hs->done})
@@ -250,7 +253,7 @@ extern "C" int swg_host_stepper_create_levels(swg_model model, int kind,
   if ((err = cudaGetDevice(&dev)) == cudaSuccess)
     err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   hs->copy_grid = 8 * std::max(sms, 1);
-  for (cudaStream_t *s : {&hs->h2d, &hs->comp, &hs->d2h, &hs->cap})
+  for (cudaStream_t *s : {&hs->h2d, &hs->comp, &hs->comp2, &hs->d2h, &hs->cap})
     if (err == cudaSuccess)
       err = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
   for (cudaEvent_t *e : {&hs->go, &hs->done})
@@ -325,7 +328,7 @@ static int enqueue_call(swg_host_stepper hs, double *h, double *vn, double *tr,
     return cudaGetLastError();
   };
   cudaError_t err = cudaEventRecord(hs->go, origin);
-  for (cudaStream_t s : {hs->h2d, hs->comp, hs->d2h})
+  for (cudaStream_t s : {hs->h2d, hs->comp, hs->comp2, hs->d2h})
     if (err == cudaSuccess)
       err = cudaStreamWaitEvent(s, hs->go, 0);
   // copies in, back to back on the copy-in stream
@@ -354,11 +357,15 @@ static int enqueue_call(swg_host_stepper hs, double *h, double *vn, double *tr,
   }
   if (err != cudaSuccess)
     return cuda_fail(err, "swg_host_step: copy in");
-  // each chunk's steps once its levels are in; the slice model takes the
-  // caller's current view (term switches, f_vertex) and its version, so a
-  // switch recaptures the chunk's step graph
+  // each chunk's steps once its levels are in, alternating between two
+  // compute streams (chunks own their models and intermediates, so two can
+  // run at once); the slice model takes the caller's current view (term
+  // switches, f_vertex) and its version, so a switch recaptures the chunk's
+  // step graph
+  int ci = 0;
   for (Chunk &c : hs->chunks) {
-    err = cudaStreamWaitEvent(hs->comp, c.in, 0);
+    cudaStream_t cs = (ci++ % 2) ? hs->comp2 : hs->comp;
+    err = cudaStreamWaitEvent(cs, c.in, 0);
     if (err != cudaSuccess)
       return cuda_fail(err, "swg_host_step: stream order");
     c.model->view = src->view;
@@ -367,8 +374,8 @@ static int enqueue_call(swg_host_stepper hs, double *h, double *vn, double *tr,
     c.model->view.drag_level = src->view.drag_level - c.k0;
     c.model->version = src->version;
     c.model->terms_switched = src->terms_switched;
-    TRY(swg_step(c.stepper, c.state, t0, dt, nsteps, use_graph, hs->comp));
-    err = cudaEventRecord(c.out, hs->comp);
+    TRY(swg_step(c.stepper, c.state, t0, dt, nsteps, use_graph, cs));
+    err = cudaEventRecord(c.out, cs);
     if (err != cudaSuccess)
       return cuda_fail(err, "swg_host_step: stream order");
   }
@@ -502,7 +509,7 @@ extern "C" int swg_host_step(swg_host_stepper hs, double *h, double *vn,
     return fail(SWG_ERR_ARG, "swg_host_step: bad argument");
   const int rc = host_step(hs, h, vn, tr, t0, dt, nsteps, stream);
   if (rc != SWG_OK) // no copy queued before the failure outlives the call
-    for (cudaStream_t s : {hs->h2d, hs->comp, hs->d2h})
+    for (cudaStream_t s : {hs->h2d, hs->comp, hs->comp2, hs->d2h})
       cudaStreamSynchronize(s);
   return rc;
 }
