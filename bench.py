@@ -507,8 +507,10 @@ def run_ours(args, wl):
         link_before = link_rates()
         e2e_clocks = ClockSampler(uuid)
         # let the sampler's start-up (driver queries of its own) finish
-        # before the first timed call
+        # before the first timed call, then one untimed call: after the
+        # idle second the clocks ramp up again during it
         time.sleep(1.0)
+        hs.step(hh, vv, tt, 0.0, wl.dt, 1, stream=sh)
         barrier()
         call_ms = []
         e0.record(stream)

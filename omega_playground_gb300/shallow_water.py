@@ -716,8 +716,8 @@ class HostStepper:
         """The stepper whose chunk layout steps fastest on this machine,
         and {layout: ms per step}.  A candidate is a level chunk (int, 0:
         one chunk) or a list of chunk sizes; the default tries one chunk,
-        chunks of 32, 16 and 8, and chunks of 16 or 32 between end chunks of
-        4 or 8 levels.  Each candidate is timed (host wall clock, the call
+        chunks of 32, 16 and 8, chunks of 16 or 32 between end chunks of 4
+        or 8 levels, and chunks of 12 or 8 between end chunks of 4.  Each candidate is timed (host wall clock, the call
         being synchronous) over `reps` one-step calls after one untimed
         call, on page-locked copies of `state` = (h, vn, tr) host arrays,
         which are left unchanged; a candidate's figure is the median of its
@@ -729,7 +729,8 @@ class HostStepper:
         if candidates is None:
             candidates = [0, 32, 16, 8] + [cls.edge_layout(K, c, e)
                                            for c, e in ((16, 4), (16, 8),
-                                                        (32, 8))]
+                                                        (32, 8), (12, 4),
+                                                        (8, 4))]
         layouts = {}
         for c in candidates:
             if isinstance(c, (list, tuple)):
