@@ -71,7 +71,12 @@ def parse():
     ap.add_argument("--nx", type=int, default=0,
                     help="override nx = ny (small profiling cases)")
     ap.add_argument("--adjoint-steps", type=int, default=0,
-                    help="rk4_128x128_adjoint: override the 1000 steps")
+                    help="rk4_128x128_adjoint: override the 1000 steps; "
+                         "adjoint_ensemble32: the 300 steps")
+    ap.add_argument("--no-comparisons", action="store_true",
+                    help="adjoint_ensemble32: leave out the stream-"
+                         "interleaved and one-after-another comparisons "
+                         "(small profiling cases)")
     ap.add_argument("--snapshots", type=int, default=0,
                     help="rk4_128x128_adjoint: override the 32 snapshots")
     return ap.parse_args()
@@ -678,10 +683,12 @@ def ensemble_line(steps, warmup):
 
 
 def run_adjoint_ensemble(args):
-    print(json.dumps(adjoint_ensemble_line()), flush=True)
+    print(json.dumps(adjoint_ensemble_line(args.adjoint_steps,
+                                           not args.no_comparisons)),
+          flush=True)
 
 
-def adjoint_ensemble_line():
+def adjoint_ensemble_line(nsteps_override=0, comparisons=True):
     """Batched adjoints: 32 members (nx from {32, 64, 96, 128}, 16-64 levels,
     2 tracers, RK4, 300 steps, per-cell log-normal viscosity), gradient of
     the region loss w.r.t. the initial state and the viscosity field, each
@@ -698,7 +705,8 @@ def adjoint_ensemble_line():
                                                   loss_and_grad, region_cells,
                                                   visc_scaling)
     torch.cuda.set_device(0)
-    wls = adjoint_ensemble(n=32)
+    wls = (adjoint_ensemble(n=32, nsteps=nsteps_override) if nsteps_override
+           else adjoint_ensemble(n=32))
     mem = []
     for wl in wls:
         visc = lognormal_visc(wl.nx * wl.ny, wl.seed + 5)
@@ -777,18 +785,20 @@ def adjoint_ensemble_line():
     launches = og.kernel_launches() - l0
     gvisc = [a.grad_visc()[1] for a in adjs]
     # the same adjoints, one stream per member (stream-interleaved actions)
-    for G, g in zip(Gs, grads):
-        G.upload(*g)
-    streams = [torch.cuda.Stream() for _ in mem]
-    sh = [s.cuda_stream for s in streams]
-    l1 = og.kernel_launches()
-    s_ms = timed(lambda: og.adjoint_batch_forward(adjs, X0, 0.0, dt, nsteps,
-                                                  XN, sh))
-    s_ms += timed(lambda: og.adjoint_batch_backward(adjs, Gs, sh))
-    stream_launches = og.kernel_launches() - l1
+    s_ms = stream_launches = seq_ms = None
+    if comparisons:
+        for G, g in zip(Gs, grads):
+            G.upload(*g)
+        streams = [torch.cuda.Stream() for _ in mem]
+        sh = [s.cuda_stream for s in streams]
+        l1 = og.kernel_launches()
+        s_ms = timed(lambda: og.adjoint_batch_forward(adjs, X0, 0.0, dt,
+                                                      nsteps, XN, sh))
+        s_ms += timed(lambda: og.adjoint_batch_backward(adjs, Gs, sh))
+        stream_launches = og.kernel_launches() - l1
+        seq_ms = 0.0
     # the same adjoints one member at a time (default stream)
-    seq_ms = 0.0
-    for m in mem:
+    for m in (mem if comparisons else []):
         a = og.Adjoint(m["model"], m["nsnap"])
         x = og.ShallowWaterState(m["mesh"], m["params"])
         x.upload(*m["x0"])
@@ -815,7 +825,8 @@ def adjoint_ensemble_line():
             "stream_interleaved_ms": s_ms,
             "stream_interleaved_launches": stream_launches,
             "sequential_member_adjoints_ms": seq_ms,
-            "batched_over_sequential_speedup": seq_ms / (f_ms + b_ms),
+            "batched_over_sequential_speedup":
+                seq_ms / (f_ms + b_ms) if seq_ms else None,
             "forward_updates_per_s": units / (fwd_ms / 1e3), "loss": loss,
             "grad_visc_norm": float(np.sqrt(sum(float(np.sum(g * g))
                                                 for g in gvisc)))}
