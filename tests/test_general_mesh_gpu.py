@@ -199,3 +199,52 @@ def test_general_mesh_adjoint_dot_products(stepper, nstages, full):
     adj.tlm_apply(X, DX, 0.0, 5.0, 5)
     lhs, rhs = dot(DX.download(), mu), dot(dx, LAM.download())
     assert abs(lhs - rhs) <= TOL * max(abs(lhs), abs(rhs)), (lhs, rhs)
+
+
+@pytest.mark.parametrize("scale2", [1.0, 0.37])
+def test_uniform_del2_scaling_folds_tracer_del2(scale2):
+    """mesh_scaling_del2 equal on every edge: the tracer del2 term is
+    eddy_diff2 * s times the del4 term's thickness-weighted Laplacian and
+    enters through the centre weight of the del4 stencil.  Against the
+    oracle (which sums the reference's del2 weights): tendency and 3 LSRK5
+    steps <= 1e-12, also with tracer del4 switched off at run time (the
+    separate del2 weights again) and through the no-allocation entry point."""
+    om, gm0 = general_mesh(10, 8, 7, 6262, adjoint_ready=True)
+    t = om.tables
+    t["mesh_scaling_del2"][:] = scale2
+    gm = og.MPASMesh.from_tables(
+        {n: t[n] for n in TABLES}, 7,
+        mesh_scaling_del2=t["mesh_scaling_del2"],
+        mesh_scaling_del4=t["mesh_scaling_del4"], edge_mask=t["edge_mask"],
+        max_level_cell=om.max_level_cell,
+        max_level_vertex_bot=om.max_level_vertex_bot)
+    T = 3
+    omd, gp, model = models(om, gm, T)
+    x = state(om, T, 515)
+    want = omd.compute_tendency(*x, t=0.0)
+    S = og.ShallowWaterState(gm, gp)
+    S.upload(*x)
+    Tn = og.ShallowWaterState(gm, gp)
+    model.compute_tendency(Tn, S, 0.0)
+    for got, ref in zip(Tn.download(), want):
+        assert rel_diff(got, ref) <= TOL
+    # no-allocation entry point, same tables and parameters
+    from test_zz_no_alloc import _noalloc
+    Tz = og.ShallowWaterState(gm, gp)
+    assert _noalloc(gm, gp, S, Tz, 0) == 0
+    for got, ref in zip(Tz.download(), want):
+        assert rel_diff(got, ref) <= TOL
+    want = omd.step(*(a.copy() for a in x), 0.0, 5.0, 3, kind="lsrk",
+                    nstages=5)
+    st = og.LSRKStepper(model, 5)
+    st.step(S, 0.0, 5.0, 3)
+    for got, ref in zip(S.download(), want):
+        assert rel_diff(got, ref) <= TOL
+    # tracer del4 off: del2 through its own weights again
+    model.m_tracer_hyperdiff_cell.m_enabled = False
+    omd.set_term(8, False)
+    S.upload(*x)
+    model.compute_tendency(Tn, S, 0.0)
+    want = omd.compute_tendency(*x, t=0.0)
+    for got, ref in zip(Tn.download(), want):
+        assert rel_diff(got, ref) <= TOL
