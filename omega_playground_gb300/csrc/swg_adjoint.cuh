@@ -141,15 +141,11 @@ pa_vel(const MeshView &m, const ModelView &p, const AuxView &a,
     w.ld4[i] = d4;
 }
 
-// mean thickness of edge e (the forward's value: taped, or recomputed)
-__device__ __forceinline__ double mean_h(const MeshView &m, const AuxView &a,
-                                         const double *h, int e, int k) {
-  const int K = m.nlayers;
-  if (a.mh)
-    return a.mh[size_t(e) * K + k];
-  return 0.5 * (h[size_t(__ldg(m.ce + 2 * e)) * K + k] +
-                h[size_t(__ldg(m.ce + 2 * e + 1)) * K + k]);
-}
+// What the passes recompute when the intermediates are not taped (the
+// adjoint of a single tendency, and the PV sum of a tape's last stage) sits
+// in out-of-line functions: inlined, the compiler if-converted these short
+// branches, and the taped path then issued their FP64 instructions with
+// the predicate off, occupying the FP64 pipe for nothing.
 
 // the forward's Newton reciprocal of x
 __device__ __forceinline__ double fwd_rcp(double x) {
@@ -159,6 +155,49 @@ __device__ __forceinline__ double fwd_rcp(double x) {
   r = fma(r, e, r);
   e = fma(-x, r, 1.0);
   return fma(r, e, r);
+}
+
+static __device__ __noinline__ double mean_h_of(const MeshView &m, const double *h,
+                                         int e, int k) {
+  const int K = m.nlayers;
+  return 0.5 * (h[size_t(__ldg(m.ce + 2 * e)) * K + k] +
+                h[size_t(__ldg(m.ce + 2 * e + 1)) * K + k]);
+}
+
+// mean thickness of edge e (the forward's value: taped, or recomputed)
+__device__ __forceinline__ double mean_h(const MeshView &m, const AuxView &a,
+                                         const double *h, int e, int k) {
+  if (a.mh)
+    return a.mh[size_t(e) * m.nlayers + k];
+  return mean_h_of(m, h, e, k);
+}
+
+// 1/h of cell-level i, as the forward's cell pass forms it
+static __device__ __noinline__ double cell_rcp(const double *h, unsigned i) {
+  return fwd_rcp(h[i]);
+}
+
+// 1/h_vertex of vertex vx, level k, as the forward's vertex pass forms it
+static __device__ __noinline__ double vertex_rcp(const MeshView &m, const double *h,
+                                          int vx, int k) {
+  const int K = m.nlayers;
+  double hv = __ldg(m.kvh + 3 * vx) * h[size_t(__ldg(m.cv + 3 * vx)) * K + k];
+  for (int j = 1; j < 3; ++j)
+    hv = fma(__ldg(m.kvh + 3 * vx + j),
+             h[size_t(__ldg(m.cv + 3 * vx + j)) * K + k], hv);
+  return fwd_rcp(hv);
+}
+
+// the PV flux sum S1 = sum_j w_j F_j of edge e, level k
+template <int NE>
+__device__ __noinline__ double s1_of(const MeshView &m, const AuxView &a,
+                                     int e, int k) {
+  const int K = m.nlayers;
+  double S1 = 0;
+  for (int j = 0; j < NE; ++j)
+    S1 = fma(__ldg(m.woe + NE * e + j),
+             a.F[size_t(__ldg(m.eoe + NE * e + j)) * K + k], S1);
+  return S1;
 }
 
 // --- pass 2: tracer tendency transposed to the normalised tracers (partial)
@@ -230,7 +269,7 @@ pa_tr2(const MeshView &m, const ModelView &p, const AuxView &a,
       M = fma(__ldg(m.ckq + 6 * c + j), mh, M);
     }
   // 1/h: the forward's own reciprocal (taped, or recomputed)
-  const double r = a.rh ? a.rh[i] : fwd_rcp(io.h[i]);
+  const double r = a.rh ? a.rh[i] : cell_rcp(io.h, i);
   double hsum = 0;
   for (int l = 0; l < p.ntracers; ++l) {
     const size_t t = size_t(l) * CK + i;
@@ -276,15 +315,7 @@ pa_edge(const MeshView &m, const ModelView &p, const AuxView &a,
         lG = fma(ws, io.mvn[is], lG);
         lFq = fma(ws, w.Qmu[is], lFq);
       }
-      double S1;
-      if (a.S1) {
-        S1 = a.S1[i];
-      } else {
-        S1 = 0;
-        for (int j = 0; j < NE; ++j)
-          S1 = fma(__ldg(m.woe + NE * e + j),
-                   a.F[size_t(__ldg(m.eoe + NE * e + j)) * K + k], S1);
-      }
+      const double S1 = a.S1 ? a.S1[i] : s1_of<NE>(m, a, e, k);
       w.lQ[i] = fma(S1, mu, F * lG);
       lF = fma(a.Q[i], lG, lFq);
     } else {
@@ -393,16 +424,8 @@ pa_vertex(const MeshView &m, const ModelView &p, const AuxView &a,
         lz = fma(__ldg(v.zetaadj4 + 3 * vx + j),
                  w.ld2u4[size_t(__ldg(m.ev + 3 * vx + j)) * K + k], lz);
   }
-  double r; // 1/h_vertex: the forward's value (taped, or recomputed)
-  if (a.rhv) {
-    r = a.rhv[i];
-  } else {
-    double hv = __ldg(m.kvh + 3 * vx) * io.h[size_t(__ldg(m.cv + 3 * vx)) * K + k];
-    for (int j = 1; j < 3; ++j)
-      hv = fma(__ldg(m.kvh + 3 * vx + j),
-               io.h[size_t(__ldg(m.cv + 3 * vx + j)) * K + k], hv);
-    r = fwd_rcp(hv);
-  }
+  // 1/h_vertex: the forward's value (taped, or recomputed)
+  const double r = a.rhv ? a.rhv[i] : vertex_rcp(m, io.h, vx, k);
   w.lzeta[i] = fma(r, lq, lz);
   w.lhv[i] = -(a.q[i] * r * lq);
 }

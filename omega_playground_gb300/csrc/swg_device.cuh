@@ -247,6 +247,23 @@ __device__ __forceinline__ void pt_aux2(const MeshView &m, const ModelView &p,
   }
 }
 
+// Bottom drag -c_d sqrt(ke_0 + ke_1) vn / mean_h added to t on the lowest
+// level (the term commented out at shallow_water_hierarchical.cpp:479-486),
+// with the auxiliary state's mean thickness (h_drag_edge = h_mean).  Out of
+// line: inlined, the short branch was if-converted, and every edge of every
+// model without drag issued its FP64 instructions with the predicate off.
+template <class T>
+__device__ __noinline__ T drag_add(const MeshView &m, const ModelView &p,
+                                   const AuxViewT<T> &a,
+                                   const StageArgsT<T> &s, int c0, int c1,
+                                   size_t i, int k, T t) {
+  const int K = m.nlayers;
+  const T hm = a.mh ? a.mh[i]
+                    : 0.5 * (s.h[size_t(c0) * K + k] + s.h[size_t(c1) * K + k]);
+  const T ks = a.ke[size_t(c0) * K + k] + a.ke[size_t(c1) * K + k];
+  return t + (-p.drag_coeff * sqrt(ks)) * s.vn[i] * rcp_nr(hm);
+}
+
 // Edge final pass: normal-velocity tendency (PV flux, Bernoulli gradient,
 // del2 and del4 dissipation) and its stage update.
 template <int NE, class T>
@@ -287,15 +304,8 @@ __device__ __forceinline__ void pt_edge_final(const MeshView &m,
   if (!p.off_ssh)
     t = fma(-__ldg(p.gidc + e),
             s.h[size_t(c1) * K + k] - s.h[size_t(c0) * K + k], t);
-  if (p.drag && k == p.drag_level) {
-    // bottom drag -c_d sqrt(ke_0 + ke_1) vn / mean_h on the lowest level
-    // (the term commented out at shallow_water_hierarchical.cpp:479-486),
-    // with the auxiliary state's mean thickness (h_drag_edge = h_mean)
-    const T hm = a.mh ? a.mh[i]
-                      : 0.5 * (s.h[size_t(c0) * K + k] + s.h[size_t(c1) * K + k]);
-    const T ks = a.ke[size_t(c0) * K + k] + a.ke[size_t(c1) * K + k];
-    t = t + (-p.drag_coeff * sqrt(ks)) * s.vn[i] * rcp_nr(hm);
-  }
+  if (p.drag && k == p.drag_level)
+    t = drag_add(m, p, a, s, c0, c1, i, k, t);
   const double mk = m.mask ? m.mask[i] : 1.0;
   if (p.vel_del2)
     t = fma(m.mask ? __ldg(p.c2e + e) * mk : __ldg(p.c2e + e), a.d2u[i], t);
