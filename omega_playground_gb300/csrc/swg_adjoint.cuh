@@ -84,10 +84,36 @@ __device__ __forceinline__ void emit(const AdjIO &io, double *out,
     a = __dadd_rn(acc_in[i], x);
     acc[i] = a;
   }
-  if (nmu)
-    nmu[i] = io.mode == 2   ? io.alpha * a
-             : io.mode == 1 ? fma(io.alpha, a, io.gamma * mu[i])
-                            : fma(io.alpha, lam[i], io.beta * x);
+  if (nmu) {
+    // the mode picks operands, not operations: one multiply and one
+    // multiply-add in every mode (a chain per mode was if-converted, and
+    // each element issued all three with two of them predicated off)
+    double u = a, c = 0.0, y = 0.0;
+    if (io.mode == 0) {
+      u = lam[i];
+      c = io.beta;
+      y = x;
+    } else if (io.mode == 1) {
+      c = io.gamma;
+      y = mu[i];
+    }
+    nmu[i] = fma(io.alpha, u, c * y);
+  }
+}
+
+// the del4 transpose's cell part: sum_j d4adj_j (mask mu)_j
+static __device__ __noinline__ double d4_transpose(const MeshView &m,
+                                                   const AdjView &v,
+                                                   const AdjIO &io, int c,
+                                                   int k) {
+  const int K = m.nlayers;
+  double d4 = 0;
+  for (int j = 0; j < MAXE; ++j) {
+    const size_t ie = size_t(__ldg(m.ec + 6 * c + j)) * K + k;
+    const double mu = io.mvn[ie];
+    d4 = fma(__ldg(v.d4adj + 6 * c + j), m.mask ? mu * m.mask[ie] : mu, d4);
+  }
+  return d4;
 }
 
 // --- pass 1: transposed edge stencils of the velocity tendency (cells and
@@ -125,20 +151,15 @@ pa_vel(const MeshView &m, const ModelView &p, const AuxView &a,
   // the SSH gradient's transpose is g times the kinetic-energy gradient's
   // (both are -(x_1 - x_0)/dc per edge), applied where lke is read: lke
   // serves either term
-  const bool ke_on = !p.off_ke || !p.off_ssh;
-  double ke = 0, d4 = 0;
-  for (int j = 0; j < MAXE; ++j) {
-    const size_t ie = size_t(__ldg(m.ec + 6 * c + j)) * K + k;
-    const double mu = io.mvn[ie];
-    if (ke_on)
-      ke = fma(__ldg(v.keadj + 6 * c + j), mu, ke);
-    if (p.vel_del4)
-      d4 = fma(__ldg(v.d4adj + 6 * c + j), m.mask ? mu * m.mask[ie] : mu, d4);
-  }
-  if (ke_on)
+  if (!p.off_ke || !p.off_ssh) {
+    double ke = 0;
+    for (int j = 0; j < MAXE; ++j)
+      ke = fma(__ldg(v.keadj + 6 * c + j),
+               io.mvn[size_t(__ldg(m.ec + 6 * c + j)) * K + k], ke);
     w.lke[i] = ke;
-  if (p.vel_del4)
-    w.ld4[i] = d4;
+  }
+  if (p.vel_del4) // a loop of its own: no predicated-off FMAs without del4
+    w.ld4[i] = d4_transpose(m, v, io, c, k);
 }
 
 // What the passes recompute when the intermediates are not taped (the
@@ -287,6 +308,35 @@ pa_tr2(const MeshView &m, const ModelView &p, const AuxView &a,
   w.lhtr[i] = -(r * hsum);
 }
 
+// mu times the edge mask of element i
+static __device__ __noinline__ double masked(double mu, const double *mask,
+                                            size_t i) {
+  return mu * mask[i];
+}
+
+// The del4 chain's first Laplacian at edge e, level k (element i; cells i0,
+// i1): accumulated onto the del2 part d, or kept apart (ld2u4) where
+// 1/max(dv, dc/4) differs from 1/dv.
+static __device__ __noinline__ void ld2u_del4(const MeshView &m,
+                                              const AdjView &v,
+                                              const AdjWork &w, int e, int k,
+                                              unsigned i, size_t i0,
+                                              size_t i1, double d) {
+  const int K = m.nlayers;
+  const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
+  double d4 = w.ld2u4 ? 0.0 : d;
+  d4 = fma(__ldg(v.cvr_e2 + 2 * e), w.lz4[size_t(v0) * K + k], d4);
+  d4 = fma(__ldg(v.cvr_e2 + 2 * e + 1), w.lz4[size_t(v1) * K + k], d4);
+  d4 = fma(__ldg(v.ccd_e2 + 2 * e), w.ld4[i0], d4);
+  d4 = fma(__ldg(v.ccd_e2 + 2 * e + 1), w.ld4[i1], d4);
+  if (w.ld2u4) {
+    w.ld2u[i] = d;
+    w.ld2u4[i] = d4;
+  } else {
+    w.ld2u[i] = d4;
+  }
+}
+
 // --- pass 4: edges: PV flux (transposed edges-on-edge), thickness flux,
 // mean thickness, kinetic energy, edge Laplacian.  TRD: tracer diffusion
 // on (a compile-time switch: with a runtime flag the compiler evaluated the
@@ -330,30 +380,16 @@ pa_edge(const MeshView &m, const ModelView &p, const AuxView &a,
       w.lvnp[i] = 0.0;
     }
     if (p.vel_del2 | p.vel_del4) {
-      const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
       // the dissipation terms are masked per edge and level (no multiply
       // without a mask)
-      const double mum = m.mask ? mu * m.mask[i] : mu;
-      double d = p.vel_del2 ? __ldg(p.c2e + e) * mum : 0.0;
+      const double mum = m.mask ? masked(mu, m.mask, i) : mu;
+      const double d = p.vel_del2 ? __ldg(p.c2e + e) * mum : 0.0;
       if (p.vel_del2 && w.gc2e) // parameter gradient of the del2 coefficient
         w.gc2e[i] = fma(mum, a.d2u[i], w.gc2e[i]);
-      if (p.vel_del4) {
-        // the del4 chain's first Laplacian: accumulated onto the del2 part,
-        // or kept apart (ld2u4) where 1/max(dv, dc/4) differs from 1/dv
-        double d4 = w.ld2u4 ? 0.0 : d;
-        d4 = fma(__ldg(v.cvr_e2 + 2 * e), w.lz4[size_t(v0) * K + k], d4);
-        d4 = fma(__ldg(v.cvr_e2 + 2 * e + 1), w.lz4[size_t(v1) * K + k], d4);
-        d4 = fma(__ldg(v.ccd_e2 + 2 * e), w.ld4[i0], d4);
-        d4 = fma(__ldg(v.ccd_e2 + 2 * e + 1), w.ld4[i1], d4);
-        if (w.ld2u4) {
-          w.ld2u[i] = d;
-          w.ld2u4[i] = d4;
-        } else {
-          w.ld2u[i] = d4;
-        }
-      } else {
+      if (p.vel_del4)
+        ld2u_del4(m, v, w, e, k, i, i0, i1, d);
+      else
         w.ld2u[i] = d;
-      }
     }
   } else {
     w.lvnp[i] = 0.0;
@@ -385,6 +421,33 @@ pa_edge(const MeshView &m, const ModelView &p, const AuxView &a,
   w.lvnp[i] = fma(mh, lF, w.lvnp[i]);
 }
 
+// The del4 chain's parts kept apart where 1/max(dv, dc/4) differs from 1/dv
+// (out of line, like the recompute fallbacks above): the cells' divergence
+// transpose of the two edge Laplacians, and the vertex part of the second.
+static __device__ __noinline__ double ldiv_split(const MeshView &m,
+                                                 const AdjView &v,
+                                                 const AdjWork &w, int c,
+                                                 int k) {
+  const int K = m.nlayers;
+  double ld = 0;
+  for (int j = 0; j < MAXE; ++j) {
+    const size_t ie = size_t(__ldg(m.ec + 6 * c + j)) * K + k;
+    ld = fma(__ldg(v.divadj + 6 * c + j), __dadd_rn(w.ld2u[ie], w.ld2u4[ie]),
+             ld);
+  }
+  return ld;
+}
+static __device__ __noinline__ double lz_split(const MeshView &m,
+                                               const AdjView &v,
+                                               const AdjWork &w, int vx,
+                                               int k, double lz) {
+  const int K = m.nlayers;
+  for (int j = 0; j < 3; ++j)
+    lz = fma(__ldg(v.zetaadj4 + 3 * vx + j),
+             w.ld2u4[size_t(__ldg(m.ev + 3 * vx + j)) * K + k], lz);
+  return lz;
+}
+
 // --- pass 5: vertices: PV q = (zeta + f) / h_v, vorticity; and, in the
 // C*K threads after the V*K vertex threads (launched with velocity
 // dissipation on), the cells' velocity-divergence adjoint, which reads only
@@ -400,12 +463,14 @@ pa_vertex(const MeshView &m, const ModelView &p, const AuxView &a,
     if (i >= unsigned(m.ncells) * K)
       return;
     const int c = int(i / unsigned(K)), k = int(i - unsigned(c) * K);
-    double ld = 0;
-    for (int j = 0; j < MAXE; ++j) {
-      const size_t ie = size_t(__ldg(m.ec + 6 * c + j)) * K + k;
-      ld = fma(__ldg(v.divadj + 6 * c + j),
-               w.ld2u4 ? __dadd_rn(w.ld2u[ie], w.ld2u4[ie]) : w.ld2u[ie], ld);
+    if (w.ld2u4) { // a loop per case: no predicated-off adds without it
+      w.ldiv[i] = ldiv_split(m, v, w, c, k);
+      return;
     }
+    double ld = 0;
+    for (int j = 0; j < MAXE; ++j)
+      ld = fma(__ldg(v.divadj + 6 * c + j),
+               w.ld2u[size_t(__ldg(m.ec + 6 * c + j)) * K + k], ld);
     w.ldiv[i] = ld;
     return;
   }
@@ -420,9 +485,7 @@ pa_vertex(const MeshView &m, const ModelView &p, const AuxView &a,
     lz = fma(__ldg(v.zetaadj + 3 * vx + 1), w.ld2u[size_t(e1) * K + k], lz);
     lz = fma(__ldg(v.zetaadj + 3 * vx + 2), w.ld2u[size_t(e2) * K + k], lz);
     if (w.ld2u4) // the del4 chain's part, with 1/max(dv, dc/4)
-      for (int j = 0; j < 3; ++j)
-        lz = fma(__ldg(v.zetaadj4 + 3 * vx + j),
-                 w.ld2u4[size_t(__ldg(m.ev + 3 * vx + j)) * K + k], lz);
+      lz = lz_split(m, v, w, vx, k, lz);
   }
   // 1/h_vertex: the forward's value (taped, or recomputed)
   const double r = a.rhv ? a.rhv[i] : vertex_rcp(m, io.h, vx, k);
