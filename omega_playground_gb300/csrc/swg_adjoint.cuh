@@ -314,29 +314,6 @@ static __device__ __noinline__ double masked(double mu, const double *mask,
   return mu * mask[i];
 }
 
-// The del4 chain's first Laplacian at edge e, level k (element i; cells i0,
-// i1): accumulated onto the del2 part d, or kept apart (ld2u4) where
-// 1/max(dv, dc/4) differs from 1/dv.
-static __device__ __noinline__ void ld2u_del4(const MeshView &m,
-                                              const AdjView &v,
-                                              const AdjWork &w, int e, int k,
-                                              unsigned i, size_t i0,
-                                              size_t i1, double d) {
-  const int K = m.nlayers;
-  const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
-  double d4 = w.ld2u4 ? 0.0 : d;
-  d4 = fma(__ldg(v.cvr_e2 + 2 * e), w.lz4[size_t(v0) * K + k], d4);
-  d4 = fma(__ldg(v.cvr_e2 + 2 * e + 1), w.lz4[size_t(v1) * K + k], d4);
-  d4 = fma(__ldg(v.ccd_e2 + 2 * e), w.ld4[i0], d4);
-  d4 = fma(__ldg(v.ccd_e2 + 2 * e + 1), w.ld4[i1], d4);
-  if (w.ld2u4) {
-    w.ld2u[i] = d;
-    w.ld2u4[i] = d4;
-  } else {
-    w.ld2u[i] = d4;
-  }
-}
-
 // --- pass 4: edges: PV flux (transposed edges-on-edge), thickness flux,
 // mean thickness, kinetic energy, edge Laplacian.  TRD: tracer diffusion
 // on (a compile-time switch: with a runtime flag the compiler evaluated the
@@ -386,10 +363,26 @@ pa_edge(const MeshView &m, const ModelView &p, const AuxView &a,
       const double d = p.vel_del2 ? __ldg(p.c2e + e) * mum : 0.0;
       if (p.vel_del2 && w.gc2e) // parameter gradient of the del2 coefficient
         w.gc2e[i] = fma(mum, a.d2u[i], w.gc2e[i]);
-      if (p.vel_del4)
-        ld2u_del4(m, v, w, e, k, i, i0, i1, d);
-      else
+      if (p.vel_del4) {
+        // the del4 chain's first Laplacian: accumulated onto the del2 part,
+        // or kept apart (ld2u4) where 1/max(dv, dc/4) differs from 1/dv
+        // (inline: out of line the pass needed 48 registers instead of 40,
+        // which cost more than the predicated-off block does without del4)
+        const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
+        double d4 = w.ld2u4 ? 0.0 : d;
+        d4 = fma(__ldg(v.cvr_e2 + 2 * e), w.lz4[size_t(v0) * K + k], d4);
+        d4 = fma(__ldg(v.cvr_e2 + 2 * e + 1), w.lz4[size_t(v1) * K + k], d4);
+        d4 = fma(__ldg(v.ccd_e2 + 2 * e), w.ld4[i0], d4);
+        d4 = fma(__ldg(v.ccd_e2 + 2 * e + 1), w.ld4[i1], d4);
+        if (w.ld2u4) {
+          w.ld2u[i] = d;
+          w.ld2u4[i] = d4;
+        } else {
+          w.ld2u[i] = d4;
+        }
+      } else {
         w.ld2u[i] = d;
+      }
     }
   } else {
     w.lvnp[i] = 0.0;
