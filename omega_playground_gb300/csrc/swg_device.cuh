@@ -264,6 +264,33 @@ __device__ __noinline__ T drag_add(const MeshView &m, const ModelView &p,
   return t + (-p.drag_coeff * sqrt(ks)) * s.vn[i] * rcp_nr(hm);
 }
 
+// The del2 and del4 velocity dissipation of edge element i with a per-level
+// edge mask (mask * coefficient).  Out of line: inlined, the compiler
+// if-converted the masked and unmasked forms, and every edge of an unmasked
+// model issued the masked form's multiplies with the predicate off.
+template <class T>
+__device__ __noinline__ T masked_dissipation(const MeshView &m,
+                                             const ModelView &p,
+                                             const AuxViewT<T> &a,
+                                             const StageArgsT<T> &s, int c0,
+                                             int c1, size_t i, int k,
+                                             double idc, T t) {
+  const int K = m.nlayers;
+  const int e = int(i / unsigned(K));
+  const double mk = m.mask[i];
+  if (p.vel_del2)
+    t = fma(__ldg(p.c2e + e) * mk, a.d2u[i], t);
+  if (p.vel_del4) {
+    const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
+    const T dd = a.d4[size_t(c1) * K + k] - a.d4[size_t(c0) * K + k];
+    const T dz = a.z4[size_t(v1) * K + k] - a.z4[size_t(v0) * K + k];
+    const T l = fma(dd, idc, -(dz * __ldg(m.inv_dv + e)));
+    t = fma(__ldg(p.c4e + e) * mk, l, t);
+  }
+  (void)s;
+  return t;
+}
+
 // Edge final pass: normal-velocity tendency (PV flux, Bernoulli gradient,
 // del2 and del4 dissipation) and its stage update.
 template <int NE, class T>
@@ -306,19 +333,17 @@ __device__ __forceinline__ void pt_edge_final(const MeshView &m,
             s.h[size_t(c1) * K + k] - s.h[size_t(c0) * K + k], t);
   if (p.drag && k == p.drag_level)
     t = drag_add(m, p, a, s, c0, c1, i, k, t);
-  const double mk = m.mask ? m.mask[i] : 1.0;
-  if (p.vel_del2)
-    t = fma(m.mask ? __ldg(p.c2e + e) * mk : __ldg(p.c2e + e), a.d2u[i], t);
-  if (p.vel_del4) {
-    const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
-    const T dd = a.d4[size_t(c1) * K + k] - a.d4[size_t(c0) * K + k];
-    const T dz = a.z4[size_t(v1) * K + k] - a.z4[size_t(v0) * K + k];
-    if (!m.mask && p.c4i) {
+  if (m.mask) { // masked dissipation: out of line (see masked_dissipation)
+    t = masked_dissipation(m, p, a, s, c0, c1, i, k, idc, t);
+  } else {
+    if (p.vel_del2)
+      t = fma(__ldg(p.c2e + e), a.d2u[i], t);
+    if (p.vel_del4) { // the coefficient folded into c4e/dc and -c4e/dv
+      const int v0 = __ldg(m.ve + 2 * e), v1 = __ldg(m.ve + 2 * e + 1);
+      const T dd = a.d4[size_t(c1) * K + k] - a.d4[size_t(c0) * K + k];
+      const T dz = a.z4[size_t(v1) * K + k] - a.z4[size_t(v0) * K + k];
       t = fma(__ldg(p.c4i + e), dd, t);
       t = fma(__ldg(p.c4v + e), dz, t);
-    } else {
-      const T l = fma(dd, idc, -(dz * __ldg(m.inv_dv + e)));
-      t = fma(m.mask ? __ldg(p.c4e + e) * mk : __ldg(p.c4e + e), l, t);
     }
   }
   epilogue(s.ep, s.fvn, i, t);
