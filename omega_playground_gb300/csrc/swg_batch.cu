@@ -152,29 +152,37 @@ __global__ void __launch_bounds__(512)
   }
 }
 
-template <int NE> void *pass_kernel_1(int pass) {
+template <int NE, int ITEMS> void *pass_kernel(int pass) {
   switch (pass) {
-  case P_VERTEX: return reinterpret_cast<void *>(&k_batch_pass<NE, 1, P_VERTEX>);
-  case P_CELL1: return reinterpret_cast<void *>(&k_batch_pass<NE, 1, P_CELL1>);
-  case P_EDGE1: return reinterpret_cast<void *>(&k_batch_pass<NE, 1, P_EDGE1>);
-  case P_AUX2: return reinterpret_cast<void *>(&k_batch_pass<NE, 1, P_AUX2>);
+  case P_VERTEX:
+    return reinterpret_cast<void *>(&k_batch_pass<NE, ITEMS, P_VERTEX>);
+  case P_CELL1:
+    return reinterpret_cast<void *>(&k_batch_pass<NE, ITEMS, P_CELL1>);
+  case P_EDGE1:
+    return reinterpret_cast<void *>(&k_batch_pass<NE, ITEMS, P_EDGE1>);
+  case P_AUX2:
+    return reinterpret_cast<void *>(&k_batch_pass<NE, ITEMS, P_AUX2>);
   case P_EDGE_FINAL:
-    return reinterpret_cast<void *>(&k_batch_pass<NE, 1, P_EDGE_FINAL>);
-  default: return reinterpret_cast<void *>(&k_batch_pass<NE, 1, P_CELL_FINAL>);
+    return reinterpret_cast<void *>(&k_batch_pass<NE, ITEMS, P_EDGE_FINAL>);
+  default:
+    return reinterpret_cast<void *>(&k_batch_pass<NE, ITEMS, P_CELL_FINAL>);
   }
 }
 
 int batch_launch_passes(const Member *mem, int nmem, const unsigned *prefix,
-                        const unsigned *prefix_h, int ne, int pass0,
-                        int pass1, int stage, cudaStream_t st) {
+                        const unsigned *prefix_h, int ne, int items,
+                        int pass0, int pass1, int stage, cudaStream_t st) {
   for (int pass = pass0; pass <= pass1; ++pass) {
     const unsigned nvb = prefix_h[pass * (nmem + 1) + nmem];
     if (nvb == 0)
       continue;
     void *args[] = {&mem, &nmem, &prefix, &stage};
-    cudaError_t err = cudaLaunchKernel(
-        ne == 8 ? pass_kernel_1<8>(pass) : pass_kernel_1<10>(pass), dim3(nvb),
-        dim3(256), args, 0, st);
+    void *fn = items == 2 ? (ne == 8 ? pass_kernel<8, 2>(pass)
+                                     : pass_kernel<10, 2>(pass))
+                          : (ne == 8 ? pass_kernel<8, 1>(pass)
+                                     : pass_kernel<10, 1>(pass));
+    cudaError_t err =
+        cudaLaunchKernel(fn, dim3(nvb), dim3(256), args, 0, st);
     if (err != cudaSuccess)
       return cuda_fail(err, "batched passes: launch");
     ++g_launches;

@@ -479,11 +479,12 @@ void batch_pass_units(const swg_model_s *md, unsigned units[NPASS],
                       unsigned &aux2_base);
 // (swg_batch.cu) passes [pass0, pass1] of stage `stage` over the nmem
 // members of the device table `mem`, one 256-thread block per virtual block
-// of 256 elements; prefix: [NPASS][nmem + 1] virtual-block offsets of the
-// members (device) and prefix_h its host copy (grid sizes).
+// of 256 x items elements (items 1 or 2 per thread); prefix: [NPASS][nmem +
+// 1] virtual-block offsets of the members for that block size (device) and
+// prefix_h its host copy (grid sizes).
 int batch_launch_passes(const Member *mem, int nmem, const unsigned *prefix,
-                        const unsigned *prefix_h, int ne, int pass0,
-                        int pass1, int stage, cudaStream_t st);
+                        const unsigned *prefix_h, int ne, int items,
+                        int pass0, int pass1, int stage, cudaStream_t st);
 
 // LinearShallowWaterModel (shallow_water_hierarchical.cpp:680-740):
 // vn_t = f sum_j w_j vn_j - g (h_1 - h_0) / dc and h_t = -h0 div(vn), each

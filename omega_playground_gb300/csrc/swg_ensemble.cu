@@ -215,8 +215,10 @@ int build_tables(Group &g, double dt) {
         A.io = stage_io(ad, ad->tp[b], s, dt);
         adj_units(md, A.units, A.base);
       }
+  // the taped passes take 2 elements per thread, the shape of the plain
+  // batched steps (512-element virtual blocks)
   g.fpre = prefix_of(std::vector<Member>(fwd.begin(), fwd.begin() + n),
-                     NPASS, n, 256);
+                     NPASS, n, 512);
   g.apre = prefix_of(std::vector<AdjMember>(adj.begin(), adj.begin() + n),
                      NAPASS, n, ATPB);
   TRY(upload_table(fwd, &g.d_fwd));
@@ -287,7 +289,7 @@ int batched_tape(Group &g, int b, bool out_cur, bool copy_in,
       for (swg_adjoint ad : g.adjs)
         TRY(tape_stage_copy(ad, ad->tp[b], s, ad->cur, st));
     TRY(batch_launch_passes(g.d_fwd + (size_t(b) * ns + s) * n, n, g.d_fpre,
-                            g.fpre.data(), g.ne, P_VERTEX,
+                            g.fpre.data(), g.ne, 2, P_VERTEX,
                             aux_only ? P_AUX2 : P_CELL_FINAL, 0, st));
   }
   return SWG_OK;
