@@ -82,6 +82,39 @@ __global__ void __launch_bounds__(ATPB)
 
 using KbFn = void (*)(const AdjMember *, int, const unsigned *);
 
+// Batched state copies: every member's state (h, vn and the tracers are one
+// block of words) in one launch of kCopyChunk-word chunks, instead of a
+// copy-engine transfer per member.  first[s] is the first chunk of segment
+// s and first[nseg] the chunk count, so no chunk spans two segments.
+struct CopySeg {
+  double *dst;
+  const double *src;
+  unsigned long long n;
+};
+constexpr unsigned kCopyChunk = 4096;
+
+__global__ void __launch_bounds__(256)
+    kb_copy(const CopySeg *__restrict__ segs,
+            const unsigned *__restrict__ first, int nseg) {
+  const unsigned c = blockIdx.x;
+  int lo = 0, hi = nseg;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (first[mid] <= c)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  const CopySeg sg = segs[lo];
+  const unsigned long long base =
+      (unsigned long long)(c - first[lo]) * kCopyChunk;
+  for (unsigned j = threadIdx.x; j < kCopyChunk; j += 256) {
+    const unsigned long long w = base + j;
+    if (w < sg.n)
+      sg.dst[w] = sg.src[w];
+  }
+}
+
 // the kernel of a pass for a group's switches (the single-instance launcher
 // in swg_adjoint.cu picks the same instantiations)
 KbFn kb_fn(int pass, int ne, bool d2, bool d4, bool trd) {
@@ -139,8 +172,31 @@ struct Group {
   std::vector<AdjAction> acts;
   size_t pos = 0;
   AdjGraph g_tadv[kTapes], g_tape_adj[kTapes], g_adj[kTapes];
+  // batched state copies: tables [copy][n] of (dst, src, words) and their
+  // chunk offsets [copy][n + 1]; copy = snapshot k stored (k), restored
+  // (nsnap + k), `cur` to tape b's step input (2 nsnap + b)
+  CopySeg *d_copy = nullptr;
+  unsigned *d_cfirst = nullptr;
+  std::vector<unsigned> cchunks; // chunk count per copy
   int n() const { return int(adjs.size()); }
 };
+
+enum { COPY_STORE = 0, COPY_RESTORE = 1, COPY_X0 = 2 };
+
+// one launch: copy `kind` (slot or tape `idx`) for every member of g
+int group_copy(const Group &g, int kind, int idx, cudaStream_t st) {
+  const int n = g.n();
+  const int t = kind == COPY_STORE     ? idx
+                : kind == COPY_RESTORE ? g.nsnap + idx
+                                       : 2 * g.nsnap + idx;
+  kb_copy<<<g.cchunks[t], 256, 0, st>>>(g.d_copy + size_t(t) * n,
+                                        g.d_cfirst + size_t(t) * (n + 1), n);
+  ++g_launches;
+  const cudaError_t err = cudaGetLastError();
+  return err == cudaSuccess ? SWG_OK
+                            : cuda_fail(err, "swg_adj_ensemble: state copy");
+}
+
 
 void drop_graphs(Group &g) {
   for (int b = 0; b < kTapes; ++b)
@@ -162,6 +218,35 @@ int upload_table(const std::vector<T> &h, T **d) {
                                cudaMemcpyHostToDevice);
   return err == cudaSuccess ? SWG_OK
                             : cuda_fail(err, "swg_adj_ensemble: table upload");
+}
+
+int build_copies(Group &g) {
+  const int n = g.n(), ncopy = 2 * g.nsnap + kTapes;
+  std::vector<CopySeg> segs(size_t(ncopy) * n);
+  std::vector<unsigned> first(size_t(ncopy) * (n + 1));
+  g.cchunks.assign(ncopy, 0);
+  for (int t = 0; t < ncopy; ++t) {
+    unsigned acc = 0;
+    for (int m = 0; m < n; ++m) {
+      swg_adjoint ad = g.adjs[m];
+      auto blk = [](swg_state s) { return static_cast<double *>(s->block); };
+      double *cur = blk(ad->cur);
+      CopySeg &c = segs[size_t(t) * n + m];
+      if (t < g.nsnap) {
+        c = {blk(ad->snaps[t]), cur, words(ad->model)};
+      } else if (t < 2 * g.nsnap) {
+        c = {cur, blk(ad->snaps[t - g.nsnap]), words(ad->model)};
+      } else {
+        c = {blk(ad->tp[t - 2 * g.nsnap].X[0]), cur, words(ad->model)};
+      }
+      first[size_t(t) * (n + 1) + m] = acc;
+      acc += unsigned((c.n + kCopyChunk - 1) / kCopyChunk);
+    }
+    first[size_t(t) * (n + 1) + n] = acc;
+    g.cchunks[t] = acc;
+  }
+  TRY(upload_table(segs, &g.d_copy));
+  return upload_table(first, &g.d_cfirst);
 }
 
 template <class U>
@@ -278,11 +363,10 @@ int g_replay(AdjGraph &gr, cudaStream_t st, Fn record) {
 int batched_tape(Group &g, int b, bool out_cur, bool copy_in,
                  cudaStream_t st) {
   const int n = g.n(), ns = g.ns;
-  for (swg_adjoint ad : g.adjs) {
-    if (copy_in)
-      TRY(swg_state_copy(ad->tp[b].X[0], ad->cur, st));
+  if (copy_in)
+    TRY(group_copy(g, COPY_X0, b, st));
+  for (swg_adjoint ad : g.adjs)
     TRY(tape_prologue(ad, ad->tp[b], out_cur ? ad->cur : nullptr, st));
-  }
   for (int s = 0; s < ns; ++s) {
     const bool aux_only = s == ns - 1 && !out_cur;
     if (!aux_only)
@@ -346,13 +430,9 @@ int group_action(Group &g, const AdjAction &a, bool two) {
                           q);
   }
   case A_STORE:
-    for (swg_adjoint ad : g.adjs)
-      TRY(swg_state_copy(ad->snaps[a.a], ad->cur, q));
-    return SWG_OK;
+    return group_copy(g, COPY_STORE, a.a, q);
   case A_RESTORE:
-    for (swg_adjoint ad : g.adjs)
-      TRY(swg_state_copy(ad->cur, ad->snaps[a.a], q));
-    return SWG_OK;
+    return group_copy(g, COPY_RESTORE, a.a, q);
   case A_TADV:
     for (swg_adjoint ad : g.adjs) {
       ++ad->taped_steps;
@@ -374,10 +454,9 @@ int group_action(Group &g, const AdjAction &a, bool two) {
     return cuda_fail(e, "swg_adj_ensemble: stream handshake");
   int rc;
   if (a.type == A_TAPE_ADJ) {
-    for (swg_adjoint ad : g.adjs) {
+    for (swg_adjoint ad : g.adjs)
       ++ad->taped_steps;
-      TRY(swg_state_copy(ad->tp[a.b].X[0], ad->cur, st));
-    }
+    TRY(group_copy(g, COPY_X0, a.b, st));
     // `cur` may be advanced again once its copy is taken
     if (two && (e = hand_over(g.freed, st, g.adv)) != cudaSuccess)
       return cuda_fail(e, "swg_adj_ensemble: stream handshake");
@@ -447,6 +526,8 @@ extern "C" int swg_adj_ensemble_destroy(swg_adj_ensemble e) {
     cudaFree(g.d_fpre);
     cudaFree(g.d_adj);
     cudaFree(g.d_apre);
+    cudaFree(g.d_copy);
+    cudaFree(g.d_cfirst);
     for (cudaEvent_t ev : {g.done, g.ready, g.freed})
       if (ev)
         cudaEventDestroy(ev);
@@ -532,6 +613,8 @@ extern "C" int swg_adj_ensemble_create(int n, const swg_adjoint *adjs,
     }
     rc = swg_batch_create(g.n(), models.data(), curs.data(), g.kind, g.ns,
                           &g.plain);
+    if (rc == SWG_OK)
+      rc = build_copies(g);
     // one launch per pass, 256 threads x 2 elements (the ensemble's usual
     // fastest shape)
     if (rc == SWG_OK)
