@@ -616,25 +616,34 @@ struct Planner {
         hm[at(nn, ss)] = mh;
       }
   }
+  // The two tapes alternate.  A taped advance runs on the advance stream
+  // into the tape whose adjoint ran first in the previous pair (1 -
+  // recent_), so it can overlap the adjoint still reading the other tape;
+  // tapes from a state run on the adjoints' stream into the tape its last
+  // adjoint read (recent_).  With fixed roles the taped advance of most
+  // pairs (those with no plain advance before it) had to wait for the
+  // previous pair's last adjoint, and ran alone.
+  mutable int recent_ = 0;
   // reverse [i0, i0 + n): x_{i0} in `cur` (cur_ok) or in snapshot `slot`;
-  // slots slot+1 ... slot+s are free.  Tape 0 takes steps taped from a
-  // state, tape 1 the taped advances of the pairs.
+  // slots slot+1 ... slot+s are free
   void gen_f(std::vector<AdjAction> &out, int i0, int n, int s, int slot,
              bool cur_ok) const {
     while (n > 0) {
       if (!cur_ok)
         out.push_back({A_RESTORE, slot, 0});
       if (n == 1) {
-        out.push_back({A_TAPE_ADJ, i0, 0});
+        out.push_back({A_TAPE_ADJ, i0, recent_});
         return;
       }
       const int m = fm[at(n, s)];
       if (m == 0) {
+        const int tadv = 1 - recent_, tape = recent_;
         if (n > 2)
           out.push_back({A_ADV, i0, n - 2});
-        out.push_back({A_TADV, i0 + n - 2, 1});
-        out.push_back({A_TAPE_ADJ, i0 + n - 1, 0});
-        out.push_back({A_ADJ, i0 + n - 2, 1});
+        out.push_back({A_TADV, i0 + n - 2, tadv});
+        out.push_back({A_TAPE_ADJ, i0 + n - 1, tape});
+        out.push_back({A_ADJ, i0 + n - 2, tadv});
+        recent_ = tadv;
         n -= 2;
       } else {
         out.push_back({A_ADV, i0, m});
@@ -654,6 +663,7 @@ struct Planner {
       out.push_back({A_TADV, i0, 0});
       out.push_back({A_FWD_END, 0, 0});
       out.push_back({A_ADJ, i0, 0});
+      recent_ = 0;
       return;
     }
     const int m = hm[at(n, s)];
@@ -665,6 +675,7 @@ struct Planner {
       out.push_back({A_FWD_END, 0, 0});
       out.push_back({A_ADJ, i0 + n - 1, 0});
       out.push_back({A_ADJ, i0 + n - 2, 1});
+      recent_ = 1;
       gen_f(out, i0, n - 2, s, slot, false);
       return;
     }
