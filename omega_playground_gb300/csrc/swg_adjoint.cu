@@ -89,6 +89,14 @@ __global__ void ka_lincomb(double *y, const double *x1, const double *x2,
   if (i < n)
     y[i] = x2 ? fma(alpha, x1[i], beta * x2[i]) : alpha * x1[i];
 }
+// y = x over n words, by the SMs: a state copy on the adjoint's critical
+// path (the tape input of a step) finishes sooner than on a copy engine
+__global__ void ka_copy(double *__restrict__ y, const double *__restrict__ x,
+                        long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] = x[i];
+}
 __global__ void ka_sum_levels(const double *x, double *out, int n, int K) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n)
@@ -790,7 +798,16 @@ int run_action(swg_adjoint ad, const AdjAction &a, cudaStream_t st, bool two) {
     return cuda_fail(e, "swg_adjoint: stream handshake");
   int rc;
   if (a.type == A_TAPE_ADJ) {
-    TRY(swg_state_copy(tp.X[0], ad->cur, st));
+    {
+      const long long n = (long long)words(ad->model);
+      ka_copy<<<unsigned(std::min<long long>((n + 255) / 256, 1024)), 256,
+                0, st>>>(static_cast<double *>(tp.X[0]->block),
+                         static_cast<const double *>(ad->cur->block), n);
+      ++g_launches;
+      const cudaError_t ce = cudaGetLastError();
+      if (ce != cudaSuccess)
+        return cuda_fail(ce, "swg_adjoint: tape input copy");
+    }
     if (two && ((e = cudaEventRecord(ad->freed, st)) != cudaSuccess ||
                 (e = cudaStreamWaitEvent(ad->adv, ad->freed, 0)) != cudaSuccess))
       return cuda_fail(e, "swg_adjoint: stream handshake");
