@@ -228,6 +228,27 @@ def test_adjoint_schedule_is_valid_and_optimal():
     assert lib.swg_adj_schedule(10, 32, 3, 0, None, C.byref(n)) == 1
 
 
+def test_adjoint_schedule_alternates_tapes():
+    """In the backward sweep a taped advance never writes the tape that the
+    most recent reversal read (it runs on the advance stream while that
+    reversal may still run), and a tape from a state always writes it (it
+    runs on the reversals' stream, after that reversal)."""
+    for N, nsnap in ((12, 3), (77, 5), (300, 16), (1000, 32)):
+        acts = _schedule(N, nsnap, 4)
+        end = [i for i, a in enumerate(acts) if a[0] == 6][0]
+        recent, checked = None, 0
+        for t, a, b in acts[end + 1:]:
+            if t == 4:
+                assert recent is None or b != recent, (N, nsnap)
+                checked += 1
+            elif t == 3:
+                assert recent is None or b == recent, (N, nsnap)
+                recent = b
+            elif t == 5:
+                recent = b
+        assert checked > 0
+
+
 def test_host_stepper_edge_layout():
     """Chunk layouts with small end chunks (host-state stepper autotuning)."""
     import omega_playground_gb300 as og
