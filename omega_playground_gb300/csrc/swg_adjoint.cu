@@ -97,6 +97,20 @@ __global__ void ka_copy(double *__restrict__ y, const double *__restrict__ x,
        i += (long long)gridDim.x * blockDim.x)
     y[i] = x[i];
 }
+// a whole state copied by the SMs (ka_copy): the schedule's stores,
+// restores and tape inputs sit on the two streams' dependency chains, where
+// a copy-engine transfer of the same bytes takes about twice as long
+int sm_copy(swg_state dst, swg_state src, const swg_model_s *md,
+            cudaStream_t st) {
+  const long long n = (long long)words(md);
+  ka_copy<<<unsigned(std::min<long long>((n + 255) / 256, 1024)), 256, 0,
+            st>>>(static_cast<double *>(dst->block),
+                  static_cast<const double *>(src->block), n);
+  ++g_launches;
+  const cudaError_t err = cudaGetLastError();
+  return err == cudaSuccess ? SWG_OK
+                            : cuda_fail(err, "swg_adjoint: state copy");
+}
 __global__ void ka_sum_levels(const double *x, double *out, int n, int K) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n)
@@ -357,8 +371,10 @@ int alloc_tape(swg_adjoint ad, int b, int s) {
   TRY(alloc_aux_like(ad, t));
   if (md->view.do_vn) {
     TRY(zal(A, V * K, &t.rhv));
-    if (s < ad->ns - 1)
-      TRY(zal(A, E * K, &t.S1));
+    // the last stage's PV sum is written only when the step's final
+    // passes run (a taped advance); the adjoint of a tape from a state
+    // recomputes it (adjoint_step's last_s1)
+    TRY(zal(A, E * K, &t.S1));
   }
   if (md->params.ntracers > 0)
     TRY(zal(A, C * K, &t.rh));
@@ -515,14 +531,20 @@ int tape_step(swg_adjoint ad, TapeSlot &tp, double dt, swg_state out,
 // lamX_s = lamX_{s+1} + J(X_s)^T mu_s and
 // mu_{s-1} = dt b_{s-1} lamX_s + a_s mu_s; the step's adjoint is lamX_0.
 // The output passes accumulate lamX in lacc and form mu_{s-1} from it.
-int adjoint_step(swg_adjoint ad, const TapeSlot &tp, double dt,
+// last_s1: the tape was written by a taped advance, whose last stage ran
+// its final passes and taped that stage's PV sum too
+int adjoint_step(swg_adjoint ad, const TapeSlot &tp, double dt, bool last_s1,
                  cudaStream_t st) {
   const int ns = ad->ns;
   if (ns % 2 != 0)
     lincomb(ad->mu, ad->lam, nullptr, dt * step_rkb(ad)[ns - 1], 0.0,
             (long long)words(ad->model), st);
-  for (int s = ns - 1; s >= 0; --s)
-    adj_passes(ad, tp.taux[s], stage_io(ad, tp, s, dt), st);
+  for (int s = ns - 1; s >= 0; --s) {
+    AuxView aux = tp.taux[s];
+    if (s == ns - 1 && !last_s1)
+      aux.S1 = nullptr;
+    adj_passes(ad, aux, stage_io(ad, tp, s, dt), st);
+  }
   cudaError_t err = cudaGetLastError();
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_adjoint: adjoint step");
 }
@@ -772,9 +794,9 @@ int run_action(swg_adjoint ad, const AdjAction &a, cudaStream_t st, bool two) {
     return swg_step(ad->stepper, ad->cur, ad->t0 + a.a * ad->dt, ad->dt, a.b,
                     1, q);
   case A_STORE:
-    return swg_state_copy(ad->snaps[a.a], ad->cur, q);
+    return sm_copy(ad->snaps[a.a], ad->cur, ad->model, q);
   case A_RESTORE:
-    return swg_state_copy(ad->cur, ad->snaps[a.a], q);
+    return sm_copy(ad->cur, ad->snaps[a.a], ad->model, q);
   case A_TADV: {
     TapeSlot &tp = ad->tp[a.b];
     if (two && (e = cudaStreamWaitEvent(q, tp.free_ev, 0)) != cudaSuccess)
@@ -782,7 +804,7 @@ int run_action(swg_adjoint ad, const AdjAction &a, cudaStream_t st, bool two) {
     ++ad->taped_steps;
     ++ad->taped_advances;
     return replay(ad, tp.tadv, q, [&](cudaStream_t cs) {
-      TRY(swg_state_copy(tp.X[0], ad->cur, cs));
+      TRY(sm_copy(tp.X[0], ad->cur, ad->model, cs));
       return tape_step(ad, tp, ad->dt, ad->cur, cs);
     });
   }
@@ -798,16 +820,7 @@ int run_action(swg_adjoint ad, const AdjAction &a, cudaStream_t st, bool two) {
     return cuda_fail(e, "swg_adjoint: stream handshake");
   int rc;
   if (a.type == A_TAPE_ADJ) {
-    {
-      const long long n = (long long)words(ad->model);
-      ka_copy<<<unsigned(std::min<long long>((n + 255) / 256, 1024)), 256,
-                0, st>>>(static_cast<double *>(tp.X[0]->block),
-                         static_cast<const double *>(ad->cur->block), n);
-      ++g_launches;
-      const cudaError_t ce = cudaGetLastError();
-      if (ce != cudaSuccess)
-        return cuda_fail(ce, "swg_adjoint: tape input copy");
-    }
+    TRY(sm_copy(tp.X[0], ad->cur, ad->model, st));
     if (two && ((e = cudaEventRecord(ad->freed, st)) != cudaSuccess ||
                 (e = cudaStreamWaitEvent(ad->adv, ad->freed, 0)) != cudaSuccess))
       return cuda_fail(e, "swg_adjoint: stream handshake");
@@ -816,11 +829,12 @@ int run_action(swg_adjoint ad, const AdjAction &a, cudaStream_t st, bool two) {
     // forcing), replayed from a graph captured on first use
     rc = replay(ad, tp.tape_adj, st, [&](cudaStream_t cs) {
       TRY(tape_step(ad, tp, ad->dt, nullptr, cs));
-      return adjoint_step(ad, tp, ad->dt, cs);
+      return adjoint_step(ad, tp, ad->dt, false, cs);
     });
   } else {
+    // a reversal without its own tape follows a taped advance into tp
     rc = replay(ad, tp.adj, st, [&](cudaStream_t cs) {
-      return adjoint_step(ad, tp, ad->dt, cs);
+      return adjoint_step(ad, tp, ad->dt, true, cs);
     });
   }
   if (rc == SWG_OK && two && (e = cudaEventRecord(tp.free_ev, st)) != cudaSuccess)

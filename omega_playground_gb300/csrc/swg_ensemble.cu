@@ -295,6 +295,11 @@ int build_tables(Group &g, double dt) {
         A.m = md->mesh->view;
         A.p = md->view;
         A.a = ad->tp[b].taux[s];
+        // the last stage's PV sum is taped only by a taped advance; the
+        // batched reversals share one table for both kinds of tape and
+        // recompute it
+        if (s == ns - 1)
+          A.a.S1 = nullptr;
         A.v = ad->av;
         A.w = ad->aw;
         A.io = stage_io(ad, ad->tp[b], s, dt);
