@@ -974,6 +974,9 @@ std::vector<AdjAction> plan_schedule(int nsteps, int nsnapshots, int nstages) {
   std::vector<AdjAction> acts =
       Planner(nsteps, nsnapshots - 1, nstages).schedule();
   std::lock_guard<std::mutex> lock(mu);
+  for (const Entry &c : cache) // another thread planned it meanwhile
+    if (c.n == nsteps && c.s == nsnapshots && c.ns == nstages)
+      return acts;
   if (cache.size() >= 16)
     cache.erase(cache.begin());
   cache.push_back({nsteps, nsnapshots, nstages, acts});

@@ -256,3 +256,36 @@ def test_host_stepper_edge_layout():
     assert og.HostStepper.edge_layout(64, 16, 4) == [4, 16, 16, 16, 8, 4]
     assert og.HostStepper.edge_layout(7, 3, 1) == [1, 3, 2, 1]
     assert og.HostStepper.edge_layout(6, 3, 3) == [6]
+
+
+def test_adjoint_plans_from_concurrent_threads():
+    """The planner's process-wide cache under concurrent callers (ctypes
+    releases the GIL during the call): every thread gets the counts that a
+    lone call gives, for fresh and cached plans alike."""
+    import threading
+    import omega_playground_gb300 as og
+    cases = [(n, s, ns) for n in (37, 120, 301) for s in (3, 7)
+             for ns in (4, 5)]
+    want = {c: og.adjoint_plan(*c) for c in cases}
+    got, errors = [], []
+
+    def worker(seed):
+        try:
+            order = cases[seed % len(cases):] + cases[:seed % len(cases)]
+            for c in order + [(400 + seed, 5, 4)]:
+                got.append((c, og.adjoint_plan(*c)))
+        except Exception as e:  # reported below, not lost in the thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(i,)) for i in range(8)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors
+    for c, r in got:
+        if c in want:
+            assert r == want[c], c
+        else:
+            assert r == og.adjoint_plan(*c), c
+    assert len(got) == 8 * (len(cases) + 1)
