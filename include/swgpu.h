@@ -9,9 +9,12 @@
  * paths inside the omega_playground checkout.
  *
  * Conventions
- *  - Every function returns an int status (SWG_OK = 0); nothing throws or
- *    aborts across the ABI.  swg_last_error() gives the calling thread's
- *    message for the last failed call.
+ *  - Every function returns an int status (SWG_OK = 0), except the
+ *    accessors swg_last_error, swg_version, swg_kernel_launches and
+ *    swg_checkpoint_cost (-1 on error); nothing throws or aborts across the
+ *    ABI (a host allocation that fails inside a call is SWG_ERR_OOM).
+ *    swg_last_error() gives the calling thread's message for the last
+ *    failed call.
  *  - Arrays are FP64 [entity][k] row-major with the level index k contiguous;
  *    tracers are [l][cell][k]; connectivity is int32.  "host" pointers are
  *    CPU memory, "device" pointers are CUDA global memory on the current

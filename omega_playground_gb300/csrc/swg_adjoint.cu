@@ -993,13 +993,13 @@ void adj_lincomb(swg_state y, swg_state x, double a, long long n,
 extern "C" int swg_adjoint_destroy(swg_adjoint ad);
 
 extern "C" int swg_adjoint_create(swg_model md, int nsnapshots,
-                                  swg_adjoint *out) {
+                                  swg_adjoint *out) try {
   return swg_adjoint_create_stepper(md, nsnapshots, SWG_STEPPER_RK4, 4, out);
-}
+} SWG_ABI_CATCH("swg_adjoint_create")
 
 extern "C" int swg_adjoint_create_stepper(swg_model md, int nsnapshots,
                                           int kind, int nstages,
-                                          swg_adjoint *out) {
+                                          swg_adjoint *out) try {
   if (!out || nsnapshots < 1)
     return fail(SWG_ERR_ARG, "swg_adjoint_create: bad argument");
   *out = nullptr;
@@ -1079,9 +1079,9 @@ extern "C" int swg_adjoint_create_stepper(swg_model md, int nsnapshots,
   }
   *out = ad;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_adjoint_create_stepper")
 
-extern "C" int swg_adjoint_destroy(swg_adjoint ad) {
+extern "C" int swg_adjoint_destroy(swg_adjoint ad) try {
   if (!ad)
     return SWG_OK;
   swg_stepper_destroy(ad->stepper);
@@ -1109,7 +1109,7 @@ extern "C" int swg_adjoint_destroy(swg_adjoint ad) {
     cudaFree(p);
   delete ad;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_adjoint_destroy")
 
 // no adjoint or model appears twice (members run concurrently)
 static bool distinct_members(int n, const swg_adjoint *adjs) {
@@ -1126,7 +1126,7 @@ static bool same_layout(swg_adjoint ad, swg_state s) {
 }
 
 extern "C" int swg_adj_tendency(swg_adjoint ad, swg_state x, swg_state mu,
-                                swg_state lambda_out, void *stream) {
+                                swg_state lambda_out, void *stream) try {
   if (!ad || !same_layout(ad, x) || !same_layout(ad, mu) ||
       !same_layout(ad, lambda_out))
     return fail(SWG_ERR_ARG, "swg_adj_tendency: bad argument");
@@ -1134,10 +1134,10 @@ extern "C" int swg_adj_tendency(swg_adjoint ad, swg_state x, swg_state mu,
   adj_tendency(ad, x->h, x->vn, x->tr, mu, lambda_out, st);
   cudaError_t err = cudaGetLastError();
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_adj_tendency");
-}
+} SWG_ABI_CATCH("swg_adj_tendency")
 
 extern "C" int swg_tlm_tendency(swg_adjoint ad, swg_state x, swg_state dx,
-                                swg_state dtend_out, void *stream) {
+                                swg_state dtend_out, void *stream) try {
   if (!ad || !same_layout(ad, x) || !same_layout(ad, dx) ||
       !same_layout(ad, dtend_out))
     return fail(SWG_ERR_ARG, "swg_tlm_tendency: bad argument");
@@ -1163,10 +1163,11 @@ extern "C" int swg_tlm_tendency(swg_adjoint ad, swg_state x, swg_state dx,
   g_launches += 2;
   cudaError_t err = cudaGetLastError();
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_tlm_tendency");
-}
+} SWG_ABI_CATCH("swg_tlm_tendency")
 
 extern "C" int swg_tlm_apply(swg_adjoint ad, swg_state x0, swg_state dx,
-                             double t0, double dt, int nsteps, void *stream) {
+                             double t0, double dt, int nsteps,
+                             void *stream) try {
   (void)t0;
   if (!ad || !same_layout(ad, x0) || !same_layout(ad, dx) || nsteps < 0)
     return fail(SWG_ERR_ARG, "swg_tlm_apply: bad argument");
@@ -1224,7 +1225,7 @@ extern "C" int swg_tlm_apply(swg_adjoint ad, swg_state x0, swg_state dx,
   ++g_launches;
   cudaError_t err = cudaGetLastError();
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_tlm_apply");
-}
+} SWG_ABI_CATCH("swg_tlm_apply")
 
 namespace {
 
@@ -1310,7 +1311,7 @@ int bwd_next(swg_adjoint ad, swg_state lambda, cudaStream_t st, bool *done) {
 
 extern "C" int swg_adj_forward(swg_adjoint ad, swg_state state0, double t0,
                                double dt, int nsteps, swg_state final_out,
-                               void *stream) {
+                               void *stream) try {
   if (!ad || !same_layout(ad, state0) || !same_layout(ad, final_out) ||
       nsteps < 1)
     return fail(SWG_ERR_ARG, "swg_adj_forward: bad argument");
@@ -1320,10 +1321,10 @@ extern "C" int swg_adj_forward(swg_adjoint ad, swg_state state0, double t0,
   for (bool done = false; !done;)
     TRY(fwd_next(ad, final_out, st, &done));
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_adj_forward")
 
 extern "C" int swg_adj_backward(swg_adjoint ad, swg_state lambda,
-                                void *stream) {
+                                void *stream) try {
   if (!ad || !same_layout(ad, lambda))
     return fail(SWG_ERR_ARG, "swg_adj_backward: bad argument");
   if (ad->state != 1)
@@ -1337,13 +1338,13 @@ extern "C" int swg_adj_backward(swg_adjoint ad, swg_state lambda,
   for (bool done = false; !done;)
     TRY(bwd_next(ad, lambda, st, &done));
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_adj_backward")
 
 extern "C" int swg_adj_batch_forward(int n, const swg_adjoint *adjs,
                                      const swg_state *states0, double t0,
                                      double dt, int nsteps,
                                      const swg_state *finals,
-                                     void *const *streams) {
+                                     void *const *streams) try {
   if (n < 1 || !adjs || !states0 || !finals || nsteps < 1)
     return fail(SWG_ERR_ARG, "swg_adj_batch_forward: bad argument");
   for (int m = 0; m < n; ++m)
@@ -1372,11 +1373,11 @@ extern "C" int swg_adj_batch_forward(int n, const swg_adjoint *adjs,
       }
     }
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_adj_batch_forward")
 
 extern "C" int swg_adj_batch_backward(int n, const swg_adjoint *adjs,
                                       const swg_state *lambdas,
-                                      void *const *streams) {
+                                      void *const *streams) try {
   if (n < 1 || !adjs || !lambdas)
     return fail(SWG_ERR_ARG, "swg_adj_batch_backward: bad argument");
   for (int m = 0; m < n; ++m)
@@ -1407,10 +1408,10 @@ extern "C" int swg_adj_batch_backward(int n, const swg_adjoint *adjs,
       }
     }
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_adj_batch_backward")
 
 extern "C" int swg_adj_info(swg_adjoint ad, long long *plain_steps,
-                            long long *taped_steps) {
+                            long long *taped_steps) try {
   if (!ad)
     return fail(SWG_ERR_ARG, "swg_adj_info: NULL");
   if (plain_steps)
@@ -1418,18 +1419,18 @@ extern "C" int swg_adj_info(swg_adjoint ad, long long *plain_steps,
   if (taped_steps)
     *taped_steps = ad->taped_steps;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_adj_info")
 
 extern "C" int swg_adj_info_ex(swg_adjoint ad, long long *plain_steps,
                                long long *taped_steps,
-                               long long *taped_advances) {
+                               long long *taped_advances) try {
   if (!ad)
     return fail(SWG_ERR_ARG, "swg_adj_info_ex: NULL");
   TRY(swg_adj_info(ad, plain_steps, taped_steps));
   if (taped_advances)
     *taped_advances = ad->taped_advances;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_adj_info_ex")
 
 // bytes of the arrays of an intermediate set (null members not counted)
 size_t aux_bytes(const AuxView &a, size_t C, size_t E, size_t V, size_t K,
@@ -1449,7 +1450,8 @@ size_t aux_bytes(const AuxView &a, size_t C, size_t E, size_t V, size_t K,
 }
 
 extern "C" int swg_adj_memory(swg_adjoint ad, long long *snapshot_bytes,
-                              long long *tape_bytes, long long *total_bytes) {
+                              long long *tape_bytes,
+                              long long *total_bytes) try {
   if (!ad)
     return fail(SWG_ERR_ARG, "swg_adj_memory: NULL");
   swg_model md = ad->model;
@@ -1472,10 +1474,10 @@ extern "C" int swg_adj_memory(swg_adjoint ad, long long *snapshot_bytes,
                                    sizeof(double) +
                                (ad->aw.gc2e ? E * K * sizeof(double) : 0));
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_adj_memory")
 
 extern "C" int swg_adj_grad_visc(swg_adjoint ad, double *grad_edge,
-                                 double *grad_cell, void *stream) {
+                                 double *grad_cell, void *stream) try {
   if (!ad)
     return fail(SWG_ERR_ARG, "swg_adj_grad_visc: NULL");
   if (!ad->aw.gc2e)
@@ -1509,16 +1511,20 @@ extern "C" int swg_adj_grad_visc(swg_adjoint ad, double *grad_edge,
     }
   }
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_adj_grad_visc")
 
-extern "C" long long swg_checkpoint_cost(int nsteps, int nsnapshots) {
+extern "C" long long swg_checkpoint_cost(int nsteps, int nsnapshots) try {
   if (nsteps < 1 || nsnapshots < 1 || nsteps > kMaxAdjointSteps)
     return -1;
   return classic_binomial_cost(nsteps, nsnapshots - 1);
+} catch (...) {
+  abi_exception("swg_checkpoint_cost");
+  return -1;
 }
 
 extern "C" int swg_adj_plan(int nsteps, int nsnapshots, int nstages,
-                            long long *plain_steps, long long *taped_advances) {
+                            long long *plain_steps,
+                            long long *taped_advances) try {
   if (nsteps < 1 || nsnapshots < 1 || nsteps > kMaxAdjointSteps ||
       !(nstages == 4 || nstages == 5 || nstages == 1))
     return fail(SWG_ERR_ARG, "swg_adj_plan: bad argument");
@@ -1529,10 +1535,10 @@ extern "C" int swg_adj_plan(int nsteps, int nsnapshots, int nstages,
   if (taped_advances)
     *taped_advances = t;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_adj_plan")
 
 extern "C" int swg_adj_schedule(int nsteps, int nsnapshots, int nstages,
-                                int max_actions, int *actions, int *count) {
+                                int max_actions, int *actions, int *count) try {
   if (nsteps < 1 || nsnapshots < 1 || nsteps > kMaxAdjointSteps ||
       !(nstages == 4 || nstages == 5 || nstages == 1) || !count ||
       max_actions < 0 || (max_actions > 0 && !actions))
@@ -1547,4 +1553,4 @@ extern "C" int swg_adj_schedule(int nsteps, int nsnapshots, int nstages,
     actions[3 * i + 2] = acts[i].b;
   }
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_adj_schedule")

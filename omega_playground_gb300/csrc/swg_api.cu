@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <stdexcept>
 
 namespace swg {
 
@@ -15,6 +16,26 @@ static thread_local std::string t_last_error;
 
 int fail(int code, const std::string &msg) {
   t_last_error = msg;
+  return code;
+}
+
+int abi_exception(const char *entry) noexcept {
+  int code = SWG_ERR_ARG;
+  const char *what = "unexpected host exception";
+  try {
+    throw;
+  } catch (const std::bad_alloc &) {
+    code = SWG_ERR_OOM;
+    what = "host allocation failed";
+  } catch (const std::length_error &) {
+    code = SWG_ERR_OOM;
+    what = "host allocation too large";
+  } catch (...) {
+  }
+  try { // the message needs memory too; the status is returned without it
+    fail(code, std::string(entry) + ": " + what);
+  } catch (...) {
+  }
   return code;
 }
 
@@ -96,7 +117,7 @@ extern "C" long long swg_kernel_launches(void) { return g_launches.load(); }
 
 // ------------------------------------------------------------------ mesh ---
 
-extern "C" int swg_mesh_create(const swg_mesh_desc *d, swg_mesh *out) {
+extern "C" int swg_mesh_create(const swg_mesh_desc *d, swg_mesh *out) try {
   if (!d || !out)
     return fail(SWG_ERR_ARG, "swg_mesh_create: NULL argument");
   *out = nullptr;
@@ -298,15 +319,15 @@ extern "C" int swg_mesh_create(const swg_mesh_desc *d, swg_mesh *out) {
   mv.dv4_differs = dv4_differs;
   *out = m;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_mesh_create")
 
-extern "C" int swg_mesh_destroy(swg_mesh m) {
+extern "C" int swg_mesh_destroy(swg_mesh m) try {
   if (!m)
     return SWG_OK;
   free_all(m->allocs);
   delete m;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_mesh_destroy")
 
 // ----------------------------------------------------------------- state ---
 
@@ -314,7 +335,7 @@ static size_t state_words(swg_mesh m, int ntr) {
   return (size_t(m->ncells) + m->nedges + size_t(ntr) * m->ncells) * m->nlayers;
 }
 
-extern "C" int swg_state_create(swg_mesh m, int ntracers, swg_state *out) {
+extern "C" int swg_state_create(swg_mesh m, int ntracers, swg_state *out) try {
   if (!m || !out || ntracers < 0)
     return fail(SWG_ERR_ARG, "swg_state_create: bad argument");
   *out = nullptr;
@@ -342,18 +363,18 @@ extern "C" int swg_state_create(swg_mesh m, int ntracers, swg_state *out) {
   s->tr = s->vn + size_t(m->nedges) * m->nlayers;
   *out = s;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_state_create")
 
-extern "C" int swg_state_destroy(swg_state s) {
+extern "C" int swg_state_destroy(swg_state s) try {
   if (!s)
     return SWG_OK;
   cudaFree(s->block);
   delete s;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_state_destroy")
 
 extern "C" int swg_state_upload(swg_state s, const double *h, const double *vn,
-                                const double *tr, void *stream) {
+                                const double *tr, void *stream) try {
   if (!s || !h || !vn || (s->ntracers > 0 && !tr))
     return fail(SWG_ERR_ARG, "swg_state_upload: NULL argument");
   const size_t K = s->mesh->nlayers;
@@ -367,10 +388,10 @@ extern "C" int swg_state_upload(swg_state s, const double *h, const double *vn,
   if (err == cudaSuccess && nt)
     err = cudaMemcpyAsync(s->tr, tr, nt * 8, cudaMemcpyHostToDevice, st);
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_state_upload");
-}
+} SWG_ABI_CATCH("swg_state_upload")
 
 extern "C" int swg_state_download(swg_state s, double *h, double *vn,
-                                  double *tr, void *stream) {
+                                  double *tr, void *stream) try {
   if (!s)
     return fail(SWG_ERR_ARG, "swg_state_download: NULL state");
   const size_t K = s->mesh->nlayers;
@@ -387,10 +408,10 @@ extern "C" int swg_state_download(swg_state s, double *h, double *vn,
   if (err == cudaSuccess)
     err = cudaStreamSynchronize(st);
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_state_download");
-}
+} SWG_ABI_CATCH("swg_state_download")
 
 extern "C" int swg_state_device_ptrs(swg_state s, double **h, double **vn,
-                                     double **tr) {
+                                     double **tr) try {
   if (!s)
     return fail(SWG_ERR_ARG, "swg_state_device_ptrs: NULL state");
   if (h)
@@ -400,9 +421,9 @@ extern "C" int swg_state_device_ptrs(swg_state s, double **h, double **vn,
   if (tr)
     *tr = s->tr;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_state_device_ptrs")
 
-extern "C" int swg_state_copy(swg_state dst, swg_state src, void *stream) {
+extern "C" int swg_state_copy(swg_state dst, swg_state src, void *stream) try {
   if (!dst || !src || dst->mesh != src->mesh ||
       dst->ntracers != src->ntracers)
     return fail(SWG_ERR_ARG, "swg_state_copy: incompatible states");
@@ -410,34 +431,34 @@ extern "C" int swg_state_copy(swg_state dst, swg_state src, void *stream) {
       dst->block, src->block, state_words(dst->mesh, dst->ntracers) * 8,
       cudaMemcpyDeviceToDevice, as_stream(stream));
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_state_copy");
-}
+} SWG_ABI_CATCH("swg_state_copy")
 
-extern "C" int swg_state_fill(swg_state s, double value, void *stream) {
+extern "C" int swg_state_fill(swg_state s, double value, void *stream) try {
   if (!s)
     return fail(SWG_ERR_ARG, "swg_state_fill: NULL state");
   const long long n = (long long)state_words(s->mesh, s->ntracers);
   launch_axpby(s->h, nullptr, nullptr, value, 0.0, n, 3, as_stream(stream));
   return check_launch("swg_state_fill");
-}
+} SWG_ABI_CATCH("swg_state_fill")
 
 // ----------------------------------------------------------------- model ---
 
 extern "C" int swg_model_create(swg_mesh mesh, const swg_params *p,
-                                swg_model *out) {
+                                swg_model *out) try {
   return swg_model_create_ex(mesh, p, nullptr, out);
-}
+} SWG_ABI_CATCH("swg_model_create")
 
 extern "C" int swg_linear_model_create(swg_mesh mesh, const swg_params *p,
-                                       double h0, swg_model *out) {
+                                       double h0, swg_model *out) try {
   swg_model_options o{};
   o.linear = 1;
   o.h0 = h0;
   return swg_model_create_ex(mesh, p, &o, out);
-}
+} SWG_ABI_CATCH("swg_linear_model_create")
 
 extern "C" int swg_model_create_ex(swg_mesh mesh, const swg_params *p,
                                    const swg_model_options *opts,
-                                   swg_model *out) {
+                                   swg_model *out) try {
   if (!mesh || !p || !out || p->ntracers < 0)
     return fail(SWG_ERR_ARG, "swg_model_create: bad argument");
   *out = nullptr;
@@ -553,16 +574,16 @@ extern "C" int swg_model_create_ex(swg_mesh mesh, const swg_params *p,
   }
   *out = md;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_model_create_ex")
 
-extern "C" int swg_model_destroy(swg_model md) {
+extern "C" int swg_model_destroy(swg_model md) try {
   if (!md)
     return SWG_OK;
   fork_destroy(md->fork);
   free_all(md->allocs);
   delete md;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_model_destroy")
 
 // The reference's per-term m_enabled switches (shallow_water_model.hpp:19-29,
 // read by compute_*_tendency in shallow_water_model.cpp:43-311).
@@ -600,7 +621,7 @@ static bool created_on(swg_model md, int term) {
 }
 
 extern "C" int swg_model_set_term_enabled(swg_model md, int term,
-                                          int enabled) {
+                                          int enabled) try {
   if (!md)
     return fail(SWG_ERR_ARG, "swg_model_set_term_enabled: NULL model");
   if (md->view.linear)
@@ -626,28 +647,29 @@ extern "C" int swg_model_set_term_enabled(swg_model md, int term,
   }
   md->terms_switched = changed;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_model_set_term_enabled")
 
-extern "C" int swg_model_term_enabled(swg_model md, int term, int *enabled) {
+extern "C" int swg_model_term_enabled(swg_model md, int term,
+                                      int *enabled) try {
   bool off;
   int *f = md ? term_flag(md, term, &off) : nullptr;
   if (!f || !enabled)
     return fail(SWG_ERR_ARG, "swg_model_term_enabled: bad argument");
   *enabled = off ? !*f : *f != 0;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_model_term_enabled")
 
 extern "C" int swg_model_set_forcing(swg_model md, swg_forcing_fn fn,
-                                     void *user) {
+                                     void *user) try {
   if (!md)
     return fail(SWG_ERR_ARG, "swg_model_set_forcing: NULL model");
   md->forcing = fn;
   md->forcing_user = user;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_model_set_forcing")
 
 extern "C" int swg_model_aux(swg_model md, const char *name,
-                             const double **ptr, long long *count) {
+                             const double **ptr, long long *count) try {
   if (!md || !name || !ptr || !count)
     return fail(SWG_ERR_ARG, "swg_model_aux: NULL argument");
   const long long C = md->mesh->ncells, E = md->mesh->nedges,
@@ -685,7 +707,7 @@ extern "C" int swg_model_aux(swg_model md, const char *name,
       return SWG_OK;
     }
   return fail(SWG_ERR_ARG, std::string("swg_model_aux: unknown field ") + name);
-}
+} SWG_ABI_CATCH("swg_model_aux")
 
 namespace {
 
@@ -722,7 +744,7 @@ int run_tendency(swg_model md, const StageArgs &s, swg_state tend_for_hook,
 
 extern "C" int swg_compute_tendency(swg_model md, swg_state tend,
                                     swg_state state, double t, int add_mode,
-                                    void *stream) {
+                                    void *stream) try {
   if (!md || !compatible(md, tend) || !compatible(md, state))
     return fail(SWG_ERR_ARG, "swg_compute_tendency: incompatible handles");
   if (add_mode != SWG_ADD_REPLACE && add_mode != SWG_ADD_INCREMENT)
@@ -732,7 +754,7 @@ extern "C" int swg_compute_tendency(swg_model md, swg_state tend,
   const StageArgs s = tendency_args(
       tend, state, add_mode == SWG_ADD_REPLACE ? EPI_REPLACE : EPI_INCREMENT);
   return run_tendency(md, s, tend, state->h, state->vn, t, as_stream(stream));
-}
+} SWG_ABI_CATCH("swg_compute_tendency")
 
 // ------------------------------------------- auxiliary state, per field ---
 // The reference's model computes its auxiliary state (ShallowWaterAuxiliary-
@@ -746,7 +768,7 @@ extern "C" int swg_compute_tendency(swg_model md, swg_state tend,
 
 extern "C" int swg_model_compute_aux(swg_model md, const double *h,
                                      const double *vn, const double *tr,
-                                     void *stream) {
+                                     void *stream) try {
   if (!md || !h || !vn || (md->params.ntracers > 0 && !tr))
     return fail(SWG_ERR_ARG, "swg_model_compute_aux: bad argument");
   if (md->view.linear)
@@ -756,7 +778,7 @@ extern "C" int swg_model_compute_aux(swg_model md, const double *h,
   launch_aux(md->mesh->view, md->view, md->aux, h, vn, tr, as_stream(stream),
              &md->fork);
   return check_launch("auxiliary state kernels");
-}
+} SWG_ABI_CATCH("swg_model_compute_aux")
 
 static int field_tendency(swg_model md, int field, double *tend,
                           const double *h, const double *vn, int add_mode,
@@ -785,30 +807,30 @@ static int field_tendency(swg_model md, int field, double *tend,
 
 extern "C" int swg_compute_h_tendency(swg_model md, double *h_tend,
                                       const double *h, const double *vn,
-                                      int add_mode, void *stream) {
+                                      int add_mode, void *stream) try {
   return field_tendency(md, 0, h_tend, h, vn, add_mode, stream,
                         "swg_compute_h_tendency");
-}
+} SWG_ABI_CATCH("swg_compute_h_tendency")
 
 extern "C" int swg_compute_vn_tendency(swg_model md, double *vn_tend,
                                        const double *h, const double *vn,
-                                       int add_mode, void *stream) {
+                                       int add_mode, void *stream) try {
   return field_tendency(md, 1, vn_tend, h, vn, add_mode, stream,
                         "swg_compute_vn_tendency");
-}
+} SWG_ABI_CATCH("swg_compute_vn_tendency")
 
 extern "C" int swg_compute_tr_tendency(swg_model md, double *tr_tend,
                                        const double *tr, const double *vn,
-                                       int add_mode, void *stream) {
+                                       int add_mode, void *stream) try {
   (void)tr; // the reference reads the normalised tracers of the aux state
   return field_tendency(md, 2, tr_tend, nullptr, vn, add_mode, stream,
                         "swg_compute_tr_tendency");
-}
+} SWG_ABI_CATCH("swg_compute_tr_tendency")
 
 // -------------------------------------------------------------- steppers ---
 
 extern "C" int swg_stepper_create(swg_model md, int kind, int nstages,
-                                  swg_stepper *out) {
+                                  swg_stepper *out) try {
   if (!md || !out)
     return fail(SWG_ERR_ARG, "swg_stepper_create: NULL argument");
   *out = nullptr;
@@ -862,9 +884,9 @@ extern "C" int swg_stepper_create(swg_model md, int kind, int nstages,
   }
   *out = sp;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_stepper_create")
 
-extern "C" int swg_stepper_destroy(swg_stepper sp) {
+extern "C" int swg_stepper_destroy(swg_stepper sp) try {
   if (!sp)
     return SWG_OK;
   if (sp->graph)
@@ -876,7 +898,7 @@ extern "C" int swg_stepper_destroy(swg_stepper sp) {
   swg_state_destroy(sp->old);
   delete sp;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_stepper_destroy")
 
 namespace {
 
@@ -967,7 +989,7 @@ int hooked_step(swg_stepper sp, swg_state S, double t, double dt,
 } // namespace
 
 extern "C" int swg_step(swg_stepper sp, swg_state S, double t0, double dt,
-                        int nsteps, int use_graph, void *stream) {
+                        int nsteps, int use_graph, void *stream) try {
   if (!sp || !compatible(sp->model, S) || nsteps < 0)
     return fail(SWG_ERR_ARG, "swg_step: bad argument");
   NvtxRange range("time_integration");
@@ -1026,7 +1048,7 @@ extern "C" int swg_step(swg_stepper sp, swg_state S, double t0, double dt,
     g_launches += sp->graph_launches;
   }
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_step")
 
 // ----------------------------------------------------------- diagnostics ---
 
@@ -1039,31 +1061,31 @@ static int diag(int which, swg_model md, swg_state s, double *out,
 }
 
 extern "C" int swg_diag_mass(swg_model md, swg_state s, double *out,
-                             void *stream) {
+                             void *stream) try {
   return diag(0, md, s, out, stream);
-}
+} SWG_ABI_CATCH("swg_diag_mass")
 extern "C" int swg_diag_energy(swg_model md, swg_state s, double *out,
-                               void *stream) {
+                               void *stream) try {
   return diag(1, md, s, out, stream);
-}
+} SWG_ABI_CATCH("swg_diag_energy")
 extern "C" int swg_diag_circulation(swg_model md, swg_state s, double *out,
-                                    void *stream) {
+                                    void *stream) try {
   return diag(2, md, s, out, stream);
-}
+} SWG_ABI_CATCH("swg_diag_circulation")
 
-extern "C" int swg_profile_enable(int on) {
+extern "C" int swg_profile_enable(int on) try {
   return profile_enable(on);
-}
+} SWG_ABI_CATCH("swg_profile_enable")
 
 extern "C" int swg_profile_read(int max_kernels, char *names,
                                 double *total_ms, long long *launches,
-                                int *count) {
+                                int *count) try {
   return profile_read(max_kernels, names, total_ms, launches, count);
-}
+} SWG_ABI_CATCH("swg_profile_read")
 
-extern "C" int swg_sync(void *stream) {
+extern "C" int swg_sync(void *stream) try {
   cudaError_t err = cudaStreamSynchronize(as_stream(stream));
   if (err == cudaSuccess)
     err = cudaGetLastError();
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_sync");
-}
+} SWG_ABI_CATCH("swg_sync")

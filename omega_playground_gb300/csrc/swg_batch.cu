@@ -444,7 +444,7 @@ int set_config(swg_batch b, int config) {
 
 extern "C" int swg_batch_create(int nmembers, const swg_model *models,
                                 const swg_state *states, int kind, int nstages,
-                                swg_batch *out) {
+                                swg_batch *out) try {
   if (!out || !models || !states || nmembers < 1)
     return fail(SWG_ERR_ARG, "swg_batch_create: bad argument");
   *out = nullptr;
@@ -562,9 +562,9 @@ extern "C" int swg_batch_create(int nmembers, const swg_model *models,
   }
   *out = b;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_batch_create")
 
-extern "C" int swg_batch_destroy(swg_batch b) {
+extern "C" int swg_batch_destroy(swg_batch b) try {
   if (!b)
     return SWG_OK;
   if (b->graph)
@@ -577,10 +577,10 @@ extern "C" int swg_batch_destroy(swg_batch b) {
   cudaFree(b->d_sync);
   delete b;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_batch_destroy")
 
 extern "C" int swg_batch_step(swg_batch b, double t0, double dt, int nsteps,
-                              int use_graph, void *stream) {
+                              int use_graph, void *stream) try {
   (void)t0; // stage times only matter to forcing hooks, which batches exclude
   if (!b || nsteps < 0)
     return fail(SWG_ERR_ARG, "swg_batch_step: bad argument");
@@ -634,9 +634,9 @@ extern "C" int swg_batch_step(swg_batch b, double t0, double dt, int nsteps,
     g_launches += b->graph_launches;
   }
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_batch_step")
 
-extern "C" int swg_batch_check(swg_batch b, void *stream) {
+extern "C" int swg_batch_check(swg_batch b, void *stream) try {
   if (!b)
     return fail(SWG_ERR_ARG, "swg_batch_check: NULL batch");
   BatchSync h{};
@@ -652,18 +652,19 @@ extern "C" int swg_batch_check(swg_batch b, void *stream) {
     return fail(SWG_ERR_TIMEOUT, "swg_batch: a grid barrier wait expired");
   }
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_batch_check")
 
-extern "C" int swg_batch_set_config(swg_batch b, int config) {
+extern "C" int swg_batch_set_config(swg_batch b, int config) try {
   if (!b)
     return fail(SWG_ERR_ARG, "swg_batch_set_config: NULL batch");
   return set_config(b, config);
-}
+} SWG_ABI_CATCH("swg_batch_set_config")
 
 extern "C" int swg_batch_config_count(void) { return kNumConfigs; }
 
 extern "C" int swg_batch_autotune(swg_batch b, double dt, int reps,
-                                  void *stream, int *best, double *best_ms) {
+                                  void *stream, int *best,
+                                  double *best_ms) try {
   if (!b || !best || reps < 1)
     return fail(SWG_ERR_ARG, "swg_batch_autotune: bad argument");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -710,10 +711,10 @@ extern "C" int swg_batch_autotune(swg_batch b, double dt, int reps,
     *best_ms = t_best / reps;
   // the tuning steps advanced the members; callers re-upload their state
   return swg_batch_check(b, stream);
-}
+} SWG_ABI_CATCH("swg_batch_autotune")
 
 extern "C" int swg_batch_selftest_timeout(swg_batch b, double limit_ms,
-                                          void *stream) {
+                                          void *stream) try {
   if (!b || !(limit_ms > 0) || limit_ms > 2000)
     return fail(SWG_ERR_ARG, "swg_batch_selftest_timeout: 0 < limit_ms <= 2000");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -733,4 +734,4 @@ extern "C" int swg_batch_selftest_timeout(swg_batch b, double limit_ms,
     return cuda_fail(err, "swg_batch_selftest_timeout: launch");
   ++g_launches;
   return swg_batch_check(b, stream);
-}
+} SWG_ABI_CATCH("swg_batch_selftest_timeout")

@@ -521,7 +521,7 @@ struct swg_adj_ensemble_s {
   int state = 0; // 1: forward sweep done
 };
 
-extern "C" int swg_adj_ensemble_destroy(swg_adj_ensemble e) {
+extern "C" int swg_adj_ensemble_destroy(swg_adj_ensemble e) try {
   if (!e)
     return SWG_OK;
   for (Group &g : e->groups) {
@@ -548,10 +548,10 @@ extern "C" int swg_adj_ensemble_destroy(swg_adj_ensemble e) {
     cudaEventDestroy(e->go);
   delete e;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_adj_ensemble_destroy")
 
 extern "C" int swg_adj_ensemble_create(int n, const swg_adjoint *adjs,
-                                       swg_adj_ensemble *out) {
+                                       swg_adj_ensemble *out) try {
   if (n < 1 || !adjs || !out)
     return fail(SWG_ERR_ARG, "swg_adj_ensemble_create: bad argument");
   *out = nullptr;
@@ -635,12 +635,13 @@ extern "C" int swg_adj_ensemble_create(int n, const swg_adjoint *adjs,
   }
   *out = e;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_adj_ensemble_create")
 
 extern "C" int swg_adj_ensemble_forward(swg_adj_ensemble e,
                                         const swg_state *states0, double t0,
                                         double dt, int nsteps,
-                                        const swg_state *finals, void *stream) {
+                                        const swg_state *finals,
+                                        void *stream) try {
   if (!e || !states0 || !finals || nsteps < 1)
     return fail(SWG_ERR_ARG, "swg_adj_ensemble_forward: bad argument");
   if (nsteps > 10000)
@@ -696,11 +697,11 @@ extern "C" int swg_adj_ensemble_forward(swg_adj_ensemble e,
     ++g.pos; // past the end-of-forward marker
   e->state = 1;
   return caller_follows(e->groups, st);
-}
+} SWG_ABI_CATCH("swg_adj_ensemble_forward")
 
 extern "C" int swg_adj_ensemble_backward(swg_adj_ensemble e,
                                          const swg_state *lambdas,
-                                         void *stream) {
+                                         void *stream) try {
   if (!e || !lambdas)
     return fail(SWG_ERR_ARG, "swg_adj_ensemble_backward: bad argument");
   if (e->state != 1)
@@ -762,10 +763,10 @@ extern "C" int swg_adj_ensemble_backward(swg_adj_ensemble e,
   }
   e->state = 0;
   return caller_follows(e->groups, st);
-}
+} SWG_ABI_CATCH("swg_adj_ensemble_backward")
 
 extern "C" int swg_adj_ensemble_groups(swg_adj_ensemble e, int *ngroups,
-                                       int *group_of) {
+                                       int *group_of) try {
   if (!e || !ngroups)
     return fail(SWG_ERR_ARG, "swg_adj_ensemble_groups: bad argument");
   *ngroups = int(e->groups.size());
@@ -773,4 +774,4 @@ extern "C" int swg_adj_ensemble_groups(swg_adj_ensemble e, int *ngroups,
     for (size_t a = 0; a < e->where.size(); ++a)
       group_of[a] = e->where[a].first;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_adj_ensemble_groups")

@@ -167,7 +167,7 @@ struct swg_host_stepper_s {
   unsigned long long uses = 0;
 };
 
-extern "C" int swg_host_stepper_destroy(swg_host_stepper hs) {
+extern "C" int swg_host_stepper_destroy(swg_host_stepper hs) try {
   if (!hs)
     return SWG_OK;
   for (Chunk &c : hs->chunks) {
@@ -191,7 +191,7 @@ extern "C" int swg_host_stepper_destroy(swg_host_stepper hs) {
       cudaEventDestroy(e);
   delete hs;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_host_stepper_destroy")
 
 static int make_chunk(swg_host_stepper hs, int kind, int nstages, Chunk &c) {
   swg_model src = hs->model;
@@ -213,7 +213,7 @@ static int make_chunk(swg_host_stepper hs, int kind, int nstages, Chunk &c) {
 extern "C" int swg_host_stepper_create_levels(swg_model model, int kind,
                                               int nstages, int nchunks,
                                               const int *levels,
-                                              swg_host_stepper *out) {
+                                              swg_host_stepper *out) try {
   if (!model || !out || nchunks < 1 || !levels)
     return fail(SWG_ERR_ARG, "swg_host_stepper_create: bad argument");
   *out = nullptr;
@@ -265,11 +265,11 @@ extern "C" int swg_host_stepper_create_levels(swg_model model, int kind,
   }
   *out = hs;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_host_stepper_create_levels")
 
 extern "C" int swg_host_stepper_create(swg_model model, int kind, int nstages,
                                        int level_chunk,
-                                       swg_host_stepper *out) {
+                                       swg_host_stepper *out) try {
   if (!model || !out)
     return fail(SWG_ERR_ARG, "swg_host_stepper_create: NULL argument");
   const int K = model->mesh->nlayers;
@@ -279,10 +279,10 @@ extern "C" int swg_host_stepper_create(swg_model model, int kind, int nstages,
     levels.push_back(std::min(kc, K - k0));
   return swg_host_stepper_create_levels(model, kind, nstages,
                                         int(levels.size()), levels.data(), out);
-}
+} SWG_ABI_CATCH("swg_host_stepper_create")
 
 extern "C" int swg_host_stepper_chunks(swg_host_stepper hs, int *levels,
-                                       int *n) {
+                                       int *n) try {
   if (!hs || !n)
     return fail(SWG_ERR_ARG, "swg_host_stepper_chunks: NULL argument");
   if (levels)
@@ -290,7 +290,7 @@ extern "C" int swg_host_stepper_chunks(swg_host_stepper hs, int *levels,
       levels[i] = hs->chunks[i].kc;
   *n = int(hs->chunks.size());
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_host_stepper_chunks")
 
 // Everything one call does, ordered after `origin` and before it again:
 // copies in, each chunk's steps (its step graph when use_graph, else direct
@@ -504,7 +504,7 @@ static int host_step(swg_host_stepper hs, double *h, double *vn, double *tr,
 
 extern "C" int swg_host_step(swg_host_stepper hs, double *h, double *vn,
                              double *tr, double t0, double dt, int nsteps,
-                             void *stream) {
+                             void *stream) try {
   if (!hs || !h || !vn || (hs->T > 0 && !tr) || nsteps < 0)
     return fail(SWG_ERR_ARG, "swg_host_step: bad argument");
   const int rc = host_step(hs, h, vn, tr, t0, dt, nsteps, stream);
@@ -512,9 +512,9 @@ extern "C" int swg_host_step(swg_host_stepper hs, double *h, double *vn,
     for (cudaStream_t s : {hs->h2d, hs->comp, hs->comp2, hs->d2h})
       cudaStreamSynchronize(s);
   return rc;
-}
+} SWG_ABI_CATCH("swg_host_step")
 
-extern "C" int swg_host_alloc(unsigned long long bytes, void **out) {
+extern "C" int swg_host_alloc(unsigned long long bytes, void **out) try {
   if (!out)
     return fail(SWG_ERR_ARG, "swg_host_alloc: NULL argument");
   *out = nullptr;
@@ -525,11 +525,11 @@ extern "C" int swg_host_alloc(unsigned long long bytes, void **out) {
     return cuda_fail(err, "swg_host_alloc");
   }
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_host_alloc")
 
-extern "C" int swg_host_free(void *p) {
+extern "C" int swg_host_free(void *p) try {
   if (!p)
     return SWG_OK;
   cudaError_t err = cudaFreeHost(p);
   return err == cudaSuccess ? SWG_OK : cuda_fail(err, "swg_host_free");
-}
+} SWG_ABI_CATCH("swg_host_free")

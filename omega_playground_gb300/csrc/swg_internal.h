@@ -17,6 +17,16 @@ int fail(int code, const std::string &msg);
 // Maps a CUDA error to SWG_ERR_CUDA (or SWG_ERR_OOM) with context.
 int cuda_fail(cudaError_t err, const char *what);
 
+// The C ABI throws nothing: every entry point is a function-try-block whose
+// handler turns a host-side exception (in practice std::bad_alloc from a
+// container) into a status: SWG_ERR_OOM for a failed allocation,
+// SWG_ERR_ARG otherwise.  Called only from a handler.
+int abi_exception(const char *entry) noexcept;
+#define SWG_ABI_CATCH(entry)                                                   \
+  catch (...) {                                                                \
+    return swg::abi_exception(entry);                                          \
+  }
+
 // Return the status of a call that failed (anything but SWG_OK).
 #define TRY(x)                                                                 \
   do {                                                                         \

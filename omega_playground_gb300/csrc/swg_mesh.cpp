@@ -221,8 +221,9 @@ int build_planar_hex(int nx, int ny, double dc, swg_hex_tables *t,
 
 extern "C" int swg_planar_hex_mesh_build(int nx, int ny, double dc,
                                          swg_hex_tables *out,
-                                         double *period_x, double *period_y) {
+                                         double *period_x,
+                                         double *period_y) try {
   if (!out)
     return swg::fail(SWG_ERR_ARG, "swg_planar_hex_mesh_build: out is NULL");
   return swg::build_planar_hex(nx, ny, dc, out, period_x, period_y);
-}
+} SWG_ABI_CATCH("swg_planar_hex_mesh_build")

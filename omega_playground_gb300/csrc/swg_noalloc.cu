@@ -210,7 +210,7 @@ extern "C" int swg_compute_tendency_noalloc(swg_mesh mesh,
                                             const double *h, const double *vn,
                                             const double *tr, double *h_tend,
                                             double *vn_tend, double *tr_tend,
-                                            int add_mode, void *stream) {
+                                            int add_mode, void *stream) try {
   if (!mesh || !params || !h || !vn || !h_tend || !vn_tend ||
       params->ntracers < 0 || (params->ntracers > 0 && (!tr || !tr_tend)))
     return fail(SWG_ERR_ARG, "swg_compute_tendency_noalloc: bad argument");
@@ -287,4 +287,4 @@ extern "C" int swg_compute_tendency_noalloc(swg_mesh mesh,
   return err == cudaSuccess
              ? SWG_OK
              : cuda_fail(err, "swg_compute_tendency_noalloc: launch");
-}
+} SWG_ABI_CATCH("swg_compute_tendency_noalloc")

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(256)
 using namespace swg;
 
 extern "C" int swg_fp64_issue_rate(int op, int iters, double *inst_per_s,
-                                   double *ms, void *stream) {
+                                   double *ms, void *stream) try {
   if (op < 0 || op > 2 || iters < 1 || !inst_per_s)
     return fail(SWG_ERR_ARG, "swg_fp64_issue_rate: bad argument");
   int dev = 0, sms = 0, per_sm = 0;
@@ -110,4 +110,4 @@ extern "C" int swg_fp64_issue_rate(int op, int iters, double *inst_per_s,
   if (ms)
     *ms = t;
   return SWG_OK;
-}
+} SWG_ABI_CATCH("swg_fp64_issue_rate")

@@ -31,6 +31,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <exception>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -456,10 +457,12 @@ struct ShallowWaterModel {
                         const ShallowWaterState &state, Real t,
                         AddMode add_mode = AddMode::replace) const {
     settle_hook();
-    swg_check(swg_compute_tendency(
+    const int rc = swg_compute_tendency(
         m_handle, tend.handle(), state.handle(), t,
         add_mode == AddMode::replace ? SWG_ADD_REPLACE : SWG_ADD_INCREMENT,
-        nullptr));
+        nullptr);
+    rethrow_hook_error();
+    swg_check(rc);
   }
 
   // shallow_water_model.hpp:36-41: one field's tendency from the auxiliary
@@ -492,6 +495,19 @@ struct ShallowWaterModel {
   // resolve_hook() run it first.
   void settle_hook() const;
 
+  // An exception thrown by an additional_tendency override does not cross
+  // the C ABI: the hook's trampoline keeps it, and the call that ran the
+  // hook (compute_tendency, do_step, do_steps) rethrows it after the library
+  // returns.  The state is then unspecified, as after an exception in the
+  // reference's step.
+  void rethrow_hook_error() const {
+    if (m_hook_error) {
+      std::exception_ptr e = m_hook_error;
+      m_hook_error = nullptr;
+      std::rethrow_exception(e);
+    }
+  }
+
   // Settles whether additional_tendency is overridden: one tendency
   // evaluation on a scratch state (h = vn = 1) runs the hook once; the base
   // no-op then unregisters itself.  The ensemble and adjoint classes call it
@@ -508,6 +524,7 @@ struct ShallowWaterModel {
 
 private:
   mutable bool m_default_hook = false;
+  mutable std::exception_ptr m_hook_error; // the first one since the call
 
   static int mode(AddMode m) {
     return m == AddMode::replace ? SWG_ADD_REPLACE : SWG_ADD_INCREMENT;
@@ -549,6 +566,8 @@ private:
                          const double *h, const double *vn, double t,
                          void *) {
     auto *self = static_cast<ShallowWaterModel *>(user);
+    if (self->m_hook_error) // the rest of a failed call runs without it
+      return;
     const MPASMesh *m = self->m_mesh;
     Real2d ht, vt;
     RealConst2d hc, vc;
@@ -559,7 +578,13 @@ private:
     ht.m_ext[0] = hc.m_ext[0] = m->m_ncells;
     vt.m_ext[0] = vc.m_ext[0] = m->m_nedges;
     ht.m_ext[1] = hc.m_ext[1] = vt.m_ext[1] = vc.m_ext[1] = m->m_nlayers;
-    self->additional_tendency(ht, vt, hc, vc, t);
+    try {
+      self->additional_tendency(ht, vt, hc, vc, t);
+    } catch (...) {
+      if (!self->m_hook_error)
+        self->m_hook_error = std::current_exception();
+      return;
+    }
     if (self->m_default_hook)
       swg_model_set_forcing(self->m_handle, nullptr, nullptr);
   }
@@ -604,12 +629,17 @@ struct TimeStepper {
   swg_stepper m_handle = nullptr;
   virtual void do_step(Real t, Real dt,
                        const ShallowWaterState &state) const {
-    swg_check(swg_step(m_handle, state.handle(), t, dt, 1, 1, nullptr));
+    const int rc = swg_step(m_handle, state.handle(), t, dt, 1, 1, nullptr);
+    m_shallow_water->rethrow_hook_error();
+    swg_check(rc);
   }
   // nsteps consecutive do_step calls from t0 in one library call
   void do_steps(Real t0, Real dt, const ShallowWaterState &state,
                 Int nsteps) const {
-    swg_check(swg_step(m_handle, state.handle(), t0, dt, nsteps, 1, nullptr));
+    const int rc =
+        swg_step(m_handle, state.handle(), t0, dt, nsteps, 1, nullptr);
+    m_shallow_water->rethrow_hook_error();
+    swg_check(rc);
   }
   TimeStepper(ShallowWaterModel &shallow_water, int kind, int nstages)
       : m_shallow_water(&shallow_water) {

@@ -1,7 +1,10 @@
 // The C++ drop-in's model variants against twins made through the C ABI:
 // LinearShallowWaterModel (shallow_water_hierarchical.cpp:676-775) and the
 // opt-in bottom drag (swg_model_options.apply_drag).  Tendencies and three
-// RK4 / LSRK5 steps must be bitwise equal.  Exits non-zero on failure.
+// RK4 / LSRK5 steps must be bitwise equal.  Also: an exception thrown by an
+// additional_tendency override (shallow_water_model.hpp:42-44) reaches the
+// caller of compute_tendency / do_steps with its own type, and the model
+// works normally afterwards.  Exits non-zero on failure.
 #include <omega_gpu.hpp>
 
 #include <cstdint>
@@ -74,6 +77,63 @@ Fields state(const MPASMesh &m, int ntr) {
   return f;
 }
 
+struct HookError {
+  int calls;
+};
+
+// a forcing override that throws while armed
+struct ThrowingModel : ShallowWaterModel {
+  using ShallowWaterModel::ShallowWaterModel;
+  mutable int calls = 0;
+  bool arm = true;
+  void additional_tendency(Real2d, Real2d, RealConst2d, RealConst2d,
+                           Real) const override {
+    ++calls;
+    if (arm)
+      throw HookError{calls};
+  }
+};
+
+bool hook_exceptions(MPASMesh &mesh) {
+  ShallowWaterParams p;
+  p.m_f0 = 1e-4;
+  p.m_visc_del2 = 1e3;
+  p.m_ntracers = 1;
+  const Fields x = state(mesh, 1);
+  ThrowingModel model(&mesh, p);
+  ShallowWaterState s(&mesh, p), t(&mesh, p);
+  s.upload(x.h, x.vn, x.tr);
+  int rethrown = 0;
+  try {
+    model.compute_tendency(t, s, 0.0);
+  } catch (const HookError &e) {
+    rethrown += e.calls == 1;
+  }
+  RK4Stepper st(model);
+  try { // the first hook call throws; the rest of the call skips the hook
+    st.do_steps(0, 20, s, 2);
+  } catch (const HookError &e) {
+    rethrown += e.calls == 2 && model.calls == 2;
+  }
+  // disarmed: the same results as a model that never threw
+  model.arm = false;
+  ThrowingModel fresh(&mesh, p);
+  fresh.arm = false;
+  RK4Stepper st2(fresh);
+  ShallowWaterState a(&mesh, p), b(&mesh, p), ta(&mesh, p), tb(&mesh, p);
+  a.upload(x.h, x.vn, x.tr);
+  b.upload(x.h, x.vn, x.tr);
+  model.compute_tendency(ta, a, 0.0);
+  fresh.compute_tendency(tb, b, 0.0);
+  bool same = fields(ta) == fields(tb);
+  st.do_steps(0, 20, a, 2);
+  st2.do_steps(0, 20, b, 2);
+  same = same && fields(a) == fields(b);
+  std::printf("hook exceptions: rethrown %d, usable after %d\n",
+              rethrown == 2, same);
+  return rethrown == 2 && same;
+}
+
 } // namespace
 
 int main() {
@@ -106,6 +166,7 @@ int main() {
     ok = compare("bottom drag", drag, twin, mesh, p, state(mesh, 1)) && ok;
     swg_model_destroy(twin);
   }
+  ok = hook_exceptions(mesh) && ok;
   std::printf("%s\n", ok ? "PASS" : "FAIL");
   return ok ? 0 : 1;
 }

@@ -289,3 +289,36 @@ def test_adjoint_plans_from_concurrent_threads():
         else:
             assert r == og.adjoint_plan(*c), c
     assert len(got) == 8 * (len(cases) + 1)
+
+
+_OOM_CHILD = r"""
+import ctypes as C, resource, sys
+lib = C.CDLL(sys.argv[1])
+lib.swg_last_error.restype = C.c_char_p
+lib.swg_checkpoint_cost.restype = C.c_longlong
+vm = [int(l.split()[1]) * 1024 for l in open("/proc/self/status")
+      if l.startswith("VmSize:")][0]
+# room for ordinary work, not for the plans' tables (several GB)
+resource.setrlimit(resource.RLIMIT_AS, (vm + (256 << 20), vm + (256 << 20)))
+p, t = C.c_longlong(0), C.c_longlong(0)
+rc = lib.swg_adj_plan(10000, 10000, 4, C.byref(p), C.byref(t))
+print("plan", rc, lib.swg_last_error().decode())
+print("cost", lib.swg_checkpoint_cost(10000, 10000),
+      lib.swg_last_error().decode())
+"""
+
+
+def test_host_allocation_failure_is_a_status_not_an_exception():
+    """A host allocation that fails inside an entry point (here the
+    planner's tables under an address-space limit, in a child process)
+    comes back as SWG_ERR_OOM with a message; nothing throws across the C
+    ABI and the process does not abort."""
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, "-c", _OOM_CHILD, _build.LIB],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = dict(l.split(" ", 1) for l in r.stdout.splitlines())
+    assert lines["plan"].startswith("2 swg_adj_plan: host allocation"), r.stdout
+    assert lines["cost"].startswith("-1 swg_checkpoint_cost: host allocation"), \
+        r.stdout

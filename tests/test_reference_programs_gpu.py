@@ -124,9 +124,11 @@ def test_cpp_term_members_and_f_vertex():
 def test_cpp_model_variants():
     """The C++ LinearShallowWaterModel and the drag option against twins
     made through the C ABI: tendencies and RK4 / LSRK5 steps bitwise
-    equal."""
+    equal; an exception from an additional_tendency override reaches the
+    caller with its own type and leaves the model usable."""
     out = run("model_variants")
     assert "PASS" in out and out.count("twin 1") == 2, out
+    assert "hook exceptions: rethrown 1, usable after 1" in out, out
 
 
 def test_cpp_aux_state_and_field_tendencies():
